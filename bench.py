@@ -1,0 +1,322 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 Hermite-TENO hot path.
+
+Workload (one GPU): 2D Euler, 1024 x 1024 cells on [0,1]^2, seeded four-quadrant Riemann data,
+gamma 1.4, zero-gradient boundaries, characteristic TENO5 per direction + three-point
+Gauss-Legendre transverse reconstruction, HLLC flux, SSP-RK3, CFL 0.4, plain FP64.  A step is
+one SSP-RK3 time step (3 residual evaluations + stage updates) over the whole grid; the metric
+is cell-updates per second (interior cells x completed steps / seconds).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+With N > 1 (launched under torchrun) every rank advances its own replica of the workload (the
+path has no exchange step at this size: replicas only), timed between barriers; the reported
+value is the sum over ranks divided by the slowest rank's time.
+--impl reference times the reference algorithm on the host cores (the CPU oracle, the
+reference's own sources cannot be built on the GPU host), rank 0 only.
+"""
+from __future__ import annotations
+
+import argparse
+import csv
+import io
+import json
+import os
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+REPO = Path(__file__).resolve().parent
+sys.path.insert(0, str(REPO / "hermite-teno_gb300"))
+sys.path.insert(0, str(REPO / "oracle"))
+
+METRIC = "2D Euler Mcell-updates/s, plain FP64 vs FP32+learned; L1 err vs FP64"
+UNIT = "Mcell-updates/s"
+NX = NY = 1024
+SEED = 0
+WORKLOAD = "fv2d_fourquadrant_1024x1024_teno5_hllc_ssprk3_fp64"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+def dist_setup(torch):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    else:
+        torch.cuda.set_device(0)
+    return world, rank, local
+
+
+def barrier(torch, world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def allreduce_max(torch, world, x):
+    if world == 1:
+        return x
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def config_block(args, world):
+    return {"workload": WORKLOAD, "nx": NX, "ny": NY, "recon": "teno5", "flux": "hllc",
+            "bc": "zero-gradient", "cfl": 0.4, "gamma": 1.4, "seed": SEED,
+            "parallelism": f"replicas{world}" if world > 1 else "single-gpu",
+            "l2": "working set ~0.45 GB per GPU > 129 MB L2 (no flush needed)"}
+
+
+# ---- clocks --------------------------------------------------------------------------------
+class Clocks:
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                          "-i", str(self.idx), "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except FileNotFoundError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        self.out = ""
+        if self.proc is not None:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                self.out, _ = self.proc.communicate()
+
+    def summary(self):
+        rows = [r for r in csv.reader(io.StringIO(getattr(self, "out", ""))) if len(r) >= 9]
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        sm = [float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].strip().replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].strip().lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def peaks():
+    p = REPO / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def traffic_from_profiles(kernel: str):
+    """Per-launch DRAM bytes of `kernel` from the committed ncu summary, if present."""
+    p = REPO / "profiles" / "traffic.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        if kernel in d:
+            return d[kernel]
+    return None
+
+
+def cpu_baseline_sample(threads: int):
+    """The oracle (CPU restatement of the reference, OpenMP over rows) on a bounded sample of the
+    same workload: a 512 x 512 four-quadrant grid, 10 steps."""
+    import oracle
+    from hteno import ic
+
+    os.environ.setdefault("OMP_NUM_THREADS", str(threads))
+    q = ic.four_quadrant(512, 512, SEED)
+    oracle.fv2d_run(q, 1, flux=1)  # warm
+    t0 = time.perf_counter()
+    _, _, n = oracle.fv2d_run(q, 10, flux=1)
+    dt = time.perf_counter() - t0
+    return {"value": 512 * 512 * n / dt / 1e6, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": "512x512 four-quadrant TENO5+HLLC FP64, 10 steps, CPU oracle (OpenMP)"}
+
+
+# ---- reference arm ---------------------------------------------------------------------------
+def run_reference(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import oracle
+    from hteno import ic
+
+    threads = os.cpu_count() or 1
+    os.environ["OMP_NUM_THREADS"] = str(threads)
+    q = ic.four_quadrant(NX, NY, SEED)
+    for _ in range(max(0, args.warmup)):
+        q, _, _ = oracle.fv2d_run(q, 1, flux=1)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        q, _, _ = oracle.fv2d_run(q, 1, flux=1)
+    el = time.perf_counter() - t0
+    value = NX * NY * args.steps / el / 1e6
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": el * 1e3 / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": config_block(args, 1), "impl": "reference",
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"full {NX}x{NY} grid, one step per timed step; the reference's "
+                                       "own sources need Eigen3 and cannot be built on the GPU host, so "
+                                       "its CPU restatement (pinned bitwise to it) runs instead"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ---- GB300 arm -------------------------------------------------------------------------------
+def run_gpu(args):
+    import torch
+
+    import hteno
+    from hteno import ic
+
+    world, rank, local = dist_setup(torch)
+    lib = hteno.lib()
+    q = ic.four_quadrant(NX, NY, SEED)
+    ncell = NX * NY
+    cfg = hteno.config(dims=2, nx=NX, ny=NY, flux=hteno.FLUX_HLLC, recon=hteno.RECON_TENO5,
+                       precision=hteno.PREC_FP64)
+    stream = torch.cuda.Stream()
+    solver = hteno.Solver(cfg)
+    solver.set_stream(stream.cuda_stream)
+    solver.set_state(q)
+    launches = solver.launches_per_step()
+
+    # warm-up
+    solver.step_async(args.warmup)
+    solver.sync()
+
+    # timed region: K steps, device-resident, CUDA events on the solver's stream
+    lib.hteno_enable_kernel_timing(solver.h, 1)
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    clocks = Clocks(int(os.environ.get("CUDA_VISIBLE_DEVICES", str(local)).split(",")[0])
+                    if os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",")[0].isdigit() else local)
+    barrier(torch, world)
+    torch.cuda.synchronize()
+    with clocks:
+        time.sleep(0.3)
+        ev0.record(stream)
+        solver.step_async(args.steps)
+        ev1.record(stream)
+        ev1.synchronize()
+        torch.cuda.synchronize()
+    barrier(torch, world)
+    solver.sync()
+    ms = ev0.elapsed_time(ev1)
+    ms_max = allreduce_max(torch, world, ms)
+    value = ncell * args.steps * world / (ms_max / 1e3) / 1e6
+
+    # per-kernel times inside the timed region (events bracketing every launch)
+    KT = hteno.KernelTime * 16
+    kt = KT()
+    cnt = __import__("ctypes").c_int()
+    lib.hteno_kernel_timing(solver.h, kt, 16, __import__("ctypes").byref(cnt))
+    lib.hteno_enable_kernel_timing(solver.h, 0)
+    kernels = []
+    for k in range(cnt.value):
+        e = kt[k]
+        if e.launches:
+            kernels.append({"name": e.name.decode(), "launches": e.launches, "ms": e.ms,
+                            "bytes_per_launch": e.bytes_per_launch, "flops_per_launch": e.flops_per_launch})
+    tot = sum(k["ms"] for k in kernels) or 1.0
+    for k in kernels:
+        k["share"] = k["ms"] / tot
+    dom = max(kernels, key=lambda k: k["ms"])
+    avg_s = dom["ms"] / dom["launches"] / 1e3
+    hbm, hbm_src = peaks()
+    achieved = dom["bytes_per_launch"] / avg_s / 1e9
+    fp64_peak = hteno.measure_fma_peak(0)
+    roofline = {"bound": "hbm", "kernel": dom["name"], "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                "frac": achieved / hbm, "peak_source": f"{hbm_src} (MEASURED_PEAKS.json hbm_gbs)" if hbm_src == "measured" else "fallback 6.8 TB/s",
+                "traffic": traffic_from_profiles(dom["name"]),
+                "compute": {"pipe": "fp64", "achieved_tflops": dom["flops_per_launch"] / avg_s / 1e12,
+                            "peak_tflops": fp64_peak, "peak_source": "measured FP64 FMA microbenchmark (hteno_measure_fma_peak)",
+                            "frac": dom["flops_per_launch"] / avg_s / 1e12 / fp64_peak,
+                            "flops_note": "algorithmic flops of the reference (+,-,*,/,sqrt = 1, pow = 1), op-counted on the oracle"},
+                "kernels": kernels}
+    step_flops = sum(k["flops_per_launch"] * k["launches"] for k in kernels) / args.steps
+    roofline["step"] = {"achieved_tflops": step_flops * args.steps / (ms / 1e3) / 1e12,
+                        "frac_of_fp64_peak": step_flops * args.steps / (ms / 1e3) / 1e12 / fp64_peak}
+
+    # end to end through the C-ABI with pinned host buffers: every step copies the state in,
+    # advances one step and reads the state back
+    e2e = None
+    if not args.no_e2e:
+        hq = torch.from_numpy(q).pin_memory()
+        hout = torch.empty_like(hq).pin_memory()
+        e2e_steps = max(1, args.steps)
+        barrier(torch, world)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            solver.set_state(hq)
+            solver.step(1)
+            solver.get_state(hout)
+        el = time.perf_counter() - t0
+        el = allreduce_max(torch, world, el)
+        nbytes = q.nbytes
+        e2e = {"value": ncell * e2e_steps * world / el / 1e6, "unit": UNIT,
+               "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes}
+
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": config_block(args, world), "gpu_launches": launches * args.steps,
+            "clocks": clocks.summary(), "roofline": roofline, "e2e": e2e}
+    if rank == 0 and world == 1 and not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline_sample(os.cpu_count() or 1)
+    solver.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,28 @@
+// Constant block of the device numerics.  Plain C++ so that the host file that fills it
+// (device_consts.cpp) is compiled by the host compiler alone.
+#pragma once
+
+namespace hteno {
+
+// Filled by the host from the reference's constructor formulas.
+struct DevConst {
+  // Schemes::Lagrange (Schemes_Lagrange.cpp:6-304)
+  double crj[3][4];
+  double gp[3][3], gm[3][3];          // crjgp3L / crjgm3L
+  double linwp[3], linwm[3], linw0p[3], linw0m[3], sumw0p, sumw0m;
+  double gl3w[3];                     // Gauss-Legendre weights / 2 (FV_System2D.cpp:28)
+  double wtab_m[8][3], wtab_p[8][3];  // TENO5 weights per cut-off pattern (dkm / dkp)
+  double dkm[3], dkp[3];
+  // Schemes::Hermite (Schemes_Hermite.cpp:5-92, grid-size independent part)
+  double hdkm[3], hdkp[3], hdkmd[3], hdkpd[3];
+  double hwtab_m[8][3], hwtab_p[8][3], hwtab_md[8][3], hwtab_pd[8][3];
+  // float copies of the most used tables for the mixed path
+  float f_crj[3][4], f_gp[3][3], f_gm[3][3];
+  float f_linwp[3], f_linwm[3], f_linw0p[3], f_linw0m[3], f_sumw0p, f_sumw0m, f_gl3w[3];
+  float f_wtab_m[8][3], f_wtab_p[8][3];
+  float f_hwtab_m[8][3], f_hwtab_p[8][3], f_hwtab_md[8][3], f_hwtab_pd[8][3];
+};
+
+void fill_dev_const(DevConst* c);  // host side, device_consts.cpp
+
+}  // namespace hteno

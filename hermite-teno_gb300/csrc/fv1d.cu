@@ -1,0 +1,168 @@
+// FV::System1D on the GPU (FV_System1D.cpp:158-292): characteristic reconstruction (teno5,
+// teno5i as shipped, or linear) from a 6-cell stencil, HLLC or characteristic Rusanov, SSP-RK3.
+// One thread per face / per cell; a 1D grid of a few hundred cells is a latency case, so a step
+// is 2 + 3 x 2 small launches that the host replays without synchronising (dt on the device).
+#include "hteno_internal.h"
+
+namespace hteno {
+namespace {
+
+__constant__ DevConst c_dev;
+unsigned long long g_mask = 0;
+std::mutex g_mu;
+
+#include "common_kernels.cuh"
+
+constexpr int kThreads = 64;
+
+struct Geo1 {
+  int nx, bc, recon, flux;
+  double dx, area, gamma, g1;
+};
+
+__device__ __forceinline__ void cell_prim1(double g1, const double* q, double* w, double& h,
+                                           double& sr) {
+  w[0] = q[0];
+  w[1] = q[1] / q[0];
+  w[2] = (q[2] - 0.5 * q[1] * w[1]) * g1;
+  h = (q[2] + w[2]) / w[0];  // calcPrimitiveVariable (FV_System1D.cpp:95-119)
+  sr = sqrt(fabs(w[0]));
+}
+
+__global__ void k1_init(Geo1 G, const double* __restrict__ q, StepState* st) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double ms = 0.0;
+  if (i < G.nx) {
+    double qq[3] = {q[i], q[G.nx + i], q[2 * G.nx + i]}, w[3], h, sr;
+    cell_prim1(G.g1, qq, w, h, sr);
+    ms = max_speed1(G.gamma, w);
+  }
+  block_max_to(ms, &st->maxbits);
+}
+
+// face f in [0, nx] between cells f-1 and f (FV_System1D.cpp:194-235)
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k1_flux(Geo1 G, const double* __restrict__ q,
+                                                    T* __restrict__ F, const StepState* st) {
+  if (st->done) return;
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f > G.nx) return;
+  const int n = G.nx;
+  double qa[3], qb[3], wa[3], wb[3], ha, hb, sa, sb;
+  const int ca = bmap(f - 1, n, G.bc), cb = bmap(f, n, G.bc);
+  for (int v = 0; v < 3; ++v) {
+    qa[v] = q[v * n + ca];
+    qb[v] = q[v * n + cb];
+  }
+  cell_prim1(G.g1, qa, wa, ha, sa);
+  cell_prim1(G.g1, qb, wb, hb, sb);
+  const Roe1<T> R = roe1<T>(T(G.g1), T(sa), T(wa[1]), T(ha), T(sb), T(wb[1]), T(hb));
+  T ch[3][6];
+#pragma unroll
+  for (int m = 0; m < 6; ++m) {
+    const int c = bmap(f - 3 + m, n, G.bc);
+    T qq[3] = {T(q[c]), T(q[n + c]), T(q[2 * n + c])}, cc[3];
+    roe1_left(R, qq, cc);
+#pragma unroll
+    for (int r = 0; r < 3; ++r) ch[r][m] = cc[r];
+  }
+  T cl[3], cr[3];
+#pragma unroll
+  for (int r = 0; r < 3; ++r) lagrange_recon(c_dev, G.recon, ch[r], cl[r], cr[r]);
+  T ql[3], qr[3], Ff[3];
+  roe1_right(R, cl, ql);  // transformToConservative (FV_System1D.h:48-51)
+  roe1_right(R, cr, qr);
+  if (G.flux == HTENO_FLUX_HLLC) hllc1(T(G.g1), ql, qr, Ff);
+  else rusanov1(T(G.gamma), T(G.g1), R, ql, qr, Ff);
+  for (int v = 0; v < 3; ++v) F[v * (n + 1) + f] = Ff[v];
+}
+
+// rhs (FV_System1D.cpp:237-240) + RungeKutta3 (:243-272); max wave speed on the last stage
+template <typename T>
+__global__ void k1_update(Geo1 G, int stage, const T* __restrict__ F, double* __restrict__ q,
+                          double* __restrict__ q0, StepState* st) {
+  if (st->done) return;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int n = G.nx;
+  double ms = 0.0;
+  int bad = 0;
+  if (i < n) {
+    const double dt = st->dt;
+    double qn[3];
+    for (int v = 0; v < 3; ++v) {
+      const double rhs = (double(F[v * (n + 1) + i]) - double(F[v * (n + 1) + i + 1])) / G.area;
+      const double cur = q[v * n + i];
+      double base;
+      if (stage == 1) {
+        q0[v * n + i] = cur;
+        base = cur;
+      } else {
+        base = q0[v * n + i];
+      }
+      qn[v] = ssprk3(base, cur, rhs, dt, stage);
+      q[v * n + i] = qn[v];
+    }
+    double w[3], h, sr;
+    cell_prim1(G.g1, qn, w, h, sr);
+    if (stage == 3) ms = max_speed1(G.gamma, w);
+    bad = (isnan(qn[0]) || isnan(qn[1]) || isnan(qn[2])) ? 1 : 0;
+    bad |= (qn[0] <= 0.0 || w[2] <= 0.0) ? 2 : 0;
+  }
+  if (stage == 3) block_max_to(ms, &st->maxbits);
+  if (bad) atomicOr(&st->status, bad);
+}
+
+Geo1 geo1_of(const hteno_solver* s) {
+  Geo1 G;
+  G.nx = s->cfg.nx;
+  G.bc = s->cfg.bc;
+  G.recon = s->cfg.recon;
+  G.flux = s->cfg.flux;
+  G.dx = s->dx;
+  G.area = s->dx;
+  G.gamma = s->cfg.gamma;
+  G.g1 = s->cfg.gamma - 1.0;
+  return G;
+}
+
+template <typename T>
+void launch_step(hteno_solver* s, const Geo1& G) {
+  const unsigned gf = unsigned((G.nx + 1 + kThreads - 1) / kThreads);
+  const unsigned gc = unsigned((G.nx + kThreads - 1) / kThreads);
+  T* F = static_cast<T*>(s->work);
+  k_begin_step<<<1, 1, 0, s->stream>>>(s->dstate);
+  for (int stage = 1; stage <= 3; ++stage) {
+    k1_flux<T><<<gf, kThreads, 0, s->stream>>>(G, s->q, F, s->dstate);
+    k1_update<T><<<gc, kThreads, 0, s->stream>>>(G, stage, F, s->q, s->q0, s->dstate);
+  }
+  k_end_step<<<1, 1, 0, s->stream>>>(s->dstate);
+}
+
+}  // namespace
+
+int fv1d_setup(hteno_solver* s) {
+  if (upload_const(c_dev, &g_mask, &g_mu) != cudaSuccess)
+    return set_error(s, HTENO_ERR_CUDA, "constant upload failed");
+  s->work_bytes = 3 * size_t(s->cfg.nx + 1) * sizeof(double);
+  cudaError_t e = cudaMalloc(&s->work, s->work_bytes);
+  if (e != cudaSuccess) return cuda_error(s, e, "work buffer");
+  s->launches_per_step = 2 + 3 * 2;
+  return HTENO_OK;
+}
+
+int fv1d_prepare(hteno_solver* s) {
+  const Geo1 G = geo1_of(s);
+  k1_init<<<unsigned((G.nx + 127) / 128), 128, 0, s->stream>>>(G, s->q, s->dstate);
+  return cuda_error(s, cudaGetLastError(), "k1_init");
+}
+
+int fv1d_step_async(hteno_solver* s, int nsteps) {
+  const Geo1 G = geo1_of(s);
+  for (int n = 0; n < nsteps; ++n) {
+    if (s->cfg.precision == HTENO_PREC_MIXED) launch_step<float>(s, G);
+    else launch_step<double>(s, G);
+  }
+  return cuda_error(s, cudaGetLastError(), "fv1d step launch");
+}
+
+}  // namespace hteno

@@ -1,0 +1,115 @@
+// Internal declarations shared by the library's translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdarg>
+#include <cstdint>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/hteno.h"
+#include "device_math.cuh"
+
+namespace hteno {
+
+// Device-resident time-stepping state; the host never reads it inside a step loop.
+struct StepState {
+  double t;          // simulation time
+  double dt;         // dt of the current step
+  double t_final;    // stop time of the current hteno_step call
+  double dt_scale;   // cfl * min(dx, dy) (or cfl * dx^(5/3) for the Hermite 1D scheme)
+  unsigned long long maxbits;  // running max wave speed (bit pattern of a non-negative double)
+  long long steps;   // completed steps
+  int done;          // 1 once t >= t_final: the remaining launches of the call are no-ops
+  int status;        // bit 0: NaN seen; bit 1: non-positive density/pressure seen
+};
+
+// Per-device upload of the constant block of one translation unit.
+template <typename Sym>
+inline cudaError_t upload_const(const Sym& sym, unsigned long long* mask, std::mutex* mu) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  std::lock_guard<std::mutex> lk(*mu);
+  if (dev < 64 && (*mask & (1ull << dev))) return cudaSuccess;
+  DevConst h;
+  fill_dev_const(&h);
+  e = cudaMemcpyToSymbol(sym, &h, sizeof(DevConst));
+  if (e == cudaSuccess && dev < 64) *mask |= (1ull << dev);
+  return e;
+}
+
+}  // namespace hteno
+
+struct hteno_solver {
+  hteno_config cfg;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  int nvar = 4;
+  size_t ncell = 0;
+  double dx = 0, dy = 0;
+
+  // conserved state (double) and the step-start copy
+  double* q = nullptr;
+  double* q0 = nullptr;
+  // Hermite moments and their step-start copies
+  double* v = nullptr;
+  double* v0 = nullptr;
+  double* w = nullptr;
+  double* w0 = nullptr;
+  // scheme work buffers (layout owned by the scheme's translation unit)
+  void* work = nullptr;
+  size_t work_bytes = 0;
+
+  hteno::StepState* dstate = nullptr;  // device
+  hteno::StepState* hstate = nullptr;  // pinned host mirror
+
+  int launches_per_step = 0;
+  std::string err;
+
+  // per-kernel event timing (hteno_enable_kernel_timing)
+  struct TraceKind {
+    std::string name;
+    double bytes = 0, flops = 0;
+    long launches = 0;
+    double ms = 0;
+  };
+  bool timing = false;
+  std::vector<TraceKind> kinds;
+  std::vector<cudaEvent_t> ev;      // pairs: ev[2k] start, ev[2k+1] stop
+  std::vector<int> ev_kind;
+  size_t ev_used = 0;
+};
+
+namespace hteno {
+
+int set_error(hteno_solver* s, int code, const char* fmt, ...);
+
+// Tracing: bracket one launch with events when timing is on.  kind ids are per solver.
+int trace_kind(hteno_solver* s, const char* name, double bytes_per_launch, double flops_per_launch);
+void trace_begin(hteno_solver* s, int kind);
+void trace_end(hteno_solver* s);
+int cuda_error(hteno_solver* s, cudaError_t e, const char* what);
+
+// Scheme back ends (one translation unit each).
+int fv2d_setup(hteno_solver* s);
+int fv2d_prepare(hteno_solver* s);  // after set_state: primitives of the new state
+int fv2d_step_async(hteno_solver* s, int nsteps);
+int fv2d_residual(hteno_solver* s, const double* q, double* rhs);
+
+int fv1d_setup(hteno_solver* s);
+int fv1d_prepare(hteno_solver* s);
+int fv1d_step_async(hteno_solver* s, int nsteps);
+
+int hermite2d_setup(hteno_solver* s);
+int hermite2d_prepare(hteno_solver* s);
+int hermite2d_step_async(hteno_solver* s, int nsteps);
+
+int hermite1d_setup(hteno_solver* s);
+int hermite1d_prepare(hteno_solver* s);
+int hermite1d_step_async(hteno_solver* s, int nsteps);
+
+}  // namespace hteno

@@ -1,0 +1,209 @@
+"""Python binding of libhteno (the GB300 Hermite-TENO hot path) over its C-ABI (include/hteno.h).
+
+This is a thin ctypes layer: every call goes through the same extern "C" entry points a C or
+C++ host would bind.  Array arguments are numpy arrays (host) or torch CUDA tensors (device).
+The library must be built first (`hteno.build.build_library()`); importing this module never
+falls back to anything else.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from pathlib import Path
+
+import numpy as np
+
+from . import ic  # noqa: F401  (initial-data generators)
+
+_PKG = Path(__file__).resolve().parent.parent
+LIB_PATH = Path(os.environ.get("HTENO_LIB", _PKG / "lib" / "libhteno.so"))
+
+HOST, DEVICE = 0, 1
+SCHEME_FV, SCHEME_HERMITE = 0, 1
+RECON_TENO5, RECON_TENO5I, RECON_LINEAR = 0, 1, 2
+FLUX_RUSANOV, FLUX_HLLC = 0, 1
+BC_ZEROGRAD, BC_PERIODIC = 0, 1
+PREC_FP64, PREC_MIXED = 0, 1
+
+STATUS = {0: "ok", 1: "invalid argument", 2: "out of device memory", 3: "CUDA error",
+          4: "non-positive density or pressure", 5: "NaN in state", 6: "device wait timed out",
+          7: "unsupported configuration"}
+
+
+class HtenoError(RuntimeError):
+    def __init__(self, code: int, msg: str = ""):
+        self.code = code
+        super().__init__(f"hteno status {code} ({STATUS.get(code, '?')}){': ' + msg if msg else ''}")
+
+
+class Config(ctypes.Structure):
+    _fields_ = [("dims", ctypes.c_int), ("scheme", ctypes.c_int), ("nx", ctypes.c_int),
+                ("ny", ctypes.c_int), ("xl", ctypes.c_double), ("xr", ctypes.c_double),
+                ("yb", ctypes.c_double), ("yt", ctypes.c_double), ("cfl", ctypes.c_double),
+                ("gamma", ctypes.c_double), ("t_init", ctypes.c_double), ("recon", ctypes.c_int),
+                ("flux", ctypes.c_int), ("bc", ctypes.c_int), ("precision", ctypes.c_int),
+                ("reserved", ctypes.c_int * 8)]
+
+
+class KernelTime(ctypes.Structure):
+    _fields_ = [("name", ctypes.c_char * 32), ("launches", ctypes.c_long), ("ms", ctypes.c_double),
+                ("bytes_per_launch", ctypes.c_double), ("flops_per_launch", ctypes.c_double)]
+
+
+_lib = None
+_D = ctypes.POINTER(ctypes.c_double)
+
+
+def lib() -> ctypes.CDLL:
+    """Load libhteno.so (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise FileNotFoundError(f"{LIB_PATH} is missing: build it with hteno.build.build_library()")
+        L = ctypes.CDLL(str(LIB_PATH))
+        vp, i, d, l = ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_long
+        L.hteno_version.restype = ctypes.c_char_p
+        L.hteno_last_error.restype = ctypes.c_char_p
+        L.hteno_last_error.argtypes = [vp]
+        L.hteno_status_string.restype = ctypes.c_char_p
+        L.hteno_config_default.argtypes = [ctypes.POINTER(Config)]
+        L.hteno_create.argtypes = [ctypes.POINTER(Config), ctypes.POINTER(vp)]
+        L.hteno_destroy.argtypes = [vp]
+        L.hteno_set_stream.argtypes = [vp, vp]
+        L.hteno_set_state.argtypes = [vp, vp, i]
+        L.hteno_get_state.argtypes = [vp, vp, i]
+        L.hteno_set_moments.argtypes = [vp, vp, vp, i]
+        L.hteno_get_moments.argtypes = [vp, vp, vp, i]
+        L.hteno_step.argtypes = [vp, i, d]
+        L.hteno_step_async.argtypes = [vp, i, d]
+        L.hteno_sync.argtypes = [vp]
+        L.hteno_get_time.argtypes = [vp, _D, ctypes.POINTER(l), _D]
+        L.hteno_launches_per_step.argtypes = [vp, ctypes.POINTER(i)]
+        L.hteno_residual.argtypes = [vp, vp, vp]
+        L.hteno_lagrange_batch.argtypes = [i, i, vp, vp, l, vp]
+        L.hteno_gl3_batch.argtypes = [i, vp, vp, l, vp]
+        L.hteno_hermite_batch.argtypes = [i, i, d, vp, vp, vp, l, vp]
+        L.hteno_hlimiter_batch.argtypes = [i, d, vp, vp, vp, l, vp]
+        L.hteno_hllc2d_batch.argtypes = [i, d, i, vp, vp, vp, l, vp]
+        L.hteno_hllc1d_batch.argtypes = [i, d, vp, vp, vp, l, vp]
+        L.hteno_rusanov2d_batch.argtypes = [i, d, i, vp, vp, vp, vp, vp, l, vp]
+        L.hteno_drusanov2d_batch.argtypes = [i, d, i, vp, vp, vp, vp, vp, vp, vp, l, vp]
+        L.hteno_ssprk3_batch.argtypes = [vp, vp, vp, d, i, vp, l, vp]
+        L.hteno_enable_kernel_timing.argtypes = [vp, i]
+        L.hteno_kernel_timing.argtypes = [vp, ctypes.POINTER(KernelTime), i, ctypes.POINTER(i)]
+        L.hteno_measure_fma_peak.argtypes = [i, _D]
+        _lib = L
+    return _lib
+
+
+def _ptr(a):
+    """Host numpy array -> (pointer, HOST); torch CUDA tensor -> (pointer, DEVICE)."""
+    if isinstance(a, np.ndarray):
+        assert a.dtype == np.float64 and a.flags.c_contiguous
+        return ctypes.c_void_p(a.ctypes.data), HOST
+    if hasattr(a, "data_ptr"):
+        assert str(a.dtype) == "torch.float64" and a.is_contiguous()
+        return ctypes.c_void_p(a.data_ptr()), (DEVICE if a.is_cuda else HOST)
+    raise TypeError(type(a))
+
+
+def _check(rc: int, handle=None) -> None:
+    if rc != 0:
+        msg = lib().hteno_last_error(handle).decode() if handle else ""
+        raise HtenoError(rc, msg)
+
+
+def config(**kw) -> Config:
+    c = Config()
+    lib().hteno_config_default(ctypes.byref(c))
+    for k, v in kw.items():
+        if not hasattr(c, k):
+            raise KeyError(k)
+        setattr(c, k, v)
+    return c
+
+
+class Solver:
+    """Owner of one hteno_solver handle (mirrors FV::System2D & co.: ctor, IC, timeStepping)."""
+
+    def __init__(self, cfg: Config | None = None, **kw):
+        self.cfg = cfg if cfg is not None else config(**kw)
+        h = ctypes.c_void_p()
+        _check(lib().hteno_create(ctypes.byref(self.cfg), ctypes.byref(h)))
+        self.h = h
+        self.nvar = 4 if self.cfg.dims == 2 else 3
+        self.shape = (self.nvar, self.cfg.ny, self.cfg.nx) if self.cfg.dims == 2 else (self.nvar, self.cfg.nx)
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            lib().hteno_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def set_state(self, q) -> None:
+        p, where = _ptr(q)
+        _check(lib().hteno_set_state(self.h, p, where), self.h)
+
+    def set_moments(self, v, w=None) -> None:
+        pv, where = _ptr(v)
+        pw = _ptr(w)[0] if w is not None else ctypes.c_void_p()
+        _check(lib().hteno_set_moments(self.h, pv, pw, where), self.h)
+
+    def get_state(self, out=None):
+        out = np.empty(self.shape) if out is None else out
+        p, where = _ptr(out)
+        _check(lib().hteno_get_state(self.h, p, where), self.h)
+        return out
+
+    def get_moments(self):
+        v = np.empty(self.shape)
+        w = np.empty(self.shape) if self.cfg.dims == 2 else None
+        _check(lib().hteno_get_moments(self.h, _ptr(v)[0], _ptr(w)[0] if w is not None else None, HOST), self.h)
+        return (v, w) if w is not None else v
+
+    def step(self, nsteps: int, t_final: float = float("inf")) -> None:
+        _check(lib().hteno_step(self.h, int(nsteps), float(t_final)), self.h)
+
+    def step_async(self, nsteps: int, t_final: float = float("inf")) -> None:
+        _check(lib().hteno_step_async(self.h, int(nsteps), float(t_final)), self.h)
+
+    def sync(self) -> None:
+        _check(lib().hteno_sync(self.h), self.h)
+
+    def time(self):
+        t, n, dt = ctypes.c_double(), ctypes.c_long(), ctypes.c_double()
+        _check(lib().hteno_get_time(self.h, ctypes.byref(t), ctypes.byref(n), ctypes.byref(dt)), self.h)
+        return t.value, n.value, dt.value
+
+    def launches_per_step(self) -> int:
+        n = ctypes.c_int()
+        _check(lib().hteno_launches_per_step(self.h, ctypes.byref(n)), self.h)
+        return n.value
+
+    def set_stream(self, stream_ptr: int) -> None:
+        _check(lib().hteno_set_stream(self.h, ctypes.c_void_p(stream_ptr)), self.h)
+
+    def residual(self, q_dev, rhs_dev) -> None:
+        _check(lib().hteno_residual(self.h, _ptr(q_dev)[0], _ptr(rhs_dev)[0]), self.h)
+
+
+def measure_fma_peak(kind: int) -> float:
+    """Measured FMA throughput of the current device in TFLOP/s (kind 0 FP64, 1 FP32)."""
+    out = ctypes.c_double()
+    _check(lib().hteno_measure_fma_peak(kind, ctypes.byref(out)))
+    return out.value
+
+
+def version() -> str:
+    return lib().hteno_version().decode()

@@ -1,0 +1,100 @@
+"""Seeded initial data for the benchmark and test workloads (host side, numpy).
+
+The reference hard-codes its initial conditions; the workloads here need seeded variants, so the
+generators below are this project's definitions (the draw order is part of the definition):
+
+* four_quadrant: Riemann data split at (0.5, 0.5) of [0,1]^2.  A numpy PCG64 stream seeded with
+  `seed` draws, for the quadrants NE, NW, SW, SE in turn, rho ~ U[0.1, 1.5], u ~ U[-1, 1],
+  v ~ U[-1, 1], p ~ U[0.03, 1.5].  Quadrant membership follows the reference's
+  conservativeOfRiemann2D (Equations_Euler2D.cpp:530-617): x > 0.5 and y > 0.5 is NE, x < 0.5
+  and y > 0.5 NW, x < 0.5 and y < 0.5 SW, everything else SE.
+* sod: the reference's sodShock (Equations_Euler1D.cpp:317-332).
+* gaussian_blobs_shock: density 1 + sum of 32 seeded Gaussian blobs, p = 1, u = v = 0, with a
+  Mach 2 planar shock entering at x = 0 (Rankine-Hugoniot post-shock state for x < x_s).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+
+def conservative2(rho, u, v, p, gamma=1.4):
+    """Euler2D::conservative (Equations_Euler2D.cpp:28-34), elementwise."""
+    q1 = rho * u
+    q2 = rho * v
+    return np.stack([rho, q1, q2, p / (gamma - 1.0) + 0.5 * (q1 * u + q2 * v)])
+
+
+def quadrant_states(seed: int):
+    rng = np.random.default_rng(seed)
+    st = []
+    for _ in range(4):  # NE, NW, SW, SE
+        st.append((rng.uniform(0.1, 1.5), rng.uniform(-1.0, 1.0), rng.uniform(-1.0, 1.0),
+                   rng.uniform(0.03, 1.5)))
+    return np.array(st)
+
+
+def four_quadrant(nx: int, ny: int, seed: int, gamma: float = 1.4):
+    """Conserved state [4][ny][nx] of the seeded four-quadrant Riemann problem on [0,1]^2."""
+    st = quadrant_states(seed)
+    x = (np.arange(nx) + 0.5) / nx
+    y = (np.arange(ny) + 0.5) / ny
+    X, Y = np.meshgrid(x, y)
+    quad = np.where((X > 0.5) & (Y > 0.5), 0,
+                    np.where((X < 0.5) & (Y > 0.5), 1, np.where((X < 0.5) & (Y < 0.5), 2, 3)))
+    w = st[quad]
+    return np.ascontiguousarray(conservative2(w[..., 0], w[..., 1], w[..., 2], w[..., 3], gamma))
+
+
+def sod(nx: int, xl: float = 0.0, xr: float = 1.0, gamma: float = 1.4):
+    """Conserved state [3][nx] of Sod's shock tube (sodShock, Equations_Euler1D.cpp:317-332)."""
+    x = xl + (np.arange(nx) + 0.5) * (xr - xl) / nx
+    rho = np.where(x < 0.5, 1.0, 0.125)
+    p = np.where(x < 0.5, 1.0, 0.1)
+    u = np.zeros(nx)
+    return np.ascontiguousarray(np.stack([rho, rho * u, p / (gamma - 1.0) + 0.5 * rho * u * u]))
+
+
+def gaussian_blobs_shock(nx: int, ny: int, seed: int, gamma: float = 1.4, nblob: int = 32,
+                         mach: float = 2.0, x_shock: float = 0.02):
+    """Conserved state [4][ny][nx] on [0,1]^2: rho = 1 + sum_b A_b exp(-|x - x_b|^2 / s_b^2),
+    A ~ U[0.2, 1], s ~ U[0.01, 0.05], centres ~ U[0,1]^2 (drawn in that order per blob),
+    p = 1, u = v = 0; cells with x < x_shock hold the post-shock state of a Mach `mach` shock
+    moving in +x into rho = 1, p = 1."""
+    rng = np.random.default_rng(seed)
+    x = (np.arange(nx) + 0.5) / nx
+    y = (np.arange(ny) + 0.5) / ny
+    X, Y = np.meshgrid(x, y)
+    rho = np.ones((ny, nx))
+    for _ in range(nblob):
+        a = rng.uniform(0.2, 1.0)
+        s = rng.uniform(0.01, 0.05)
+        cx, cy = rng.uniform(0.0, 1.0, size=2)
+        rho += a * np.exp(-((X - cx) ** 2 + (Y - cy) ** 2) / s ** 2)
+    p = np.ones((ny, nx))
+    u = np.zeros((ny, nx))
+    v = np.zeros((ny, nx))
+    # Rankine-Hugoniot post-shock state for a shock of Mach M into (rho0, p0, u0 = 0)
+    g, M = gamma, mach
+    rho0, p0 = 1.0, 1.0
+    c0 = np.sqrt(g * p0 / rho0)
+    rho1 = rho0 * (g + 1) * M ** 2 / ((g - 1) * M ** 2 + 2)
+    p1 = p0 * (2 * g * M ** 2 - (g - 1)) / (g + 1)
+    u1 = M * c0 * (1 - rho0 / rho1)
+    post = X < x_shock
+    rho = np.where(post, rho1, rho)
+    p = np.where(post, p1, p)
+    u = np.where(post, u1, u)
+    return np.ascontiguousarray(conservative2(rho, u, v, p, gamma))
+
+
+def face_difference_moments(q_fn, nx, ny, xl, xr, yb, yt):
+    """Hermite moments by face differences of an initial-data function, as
+    FVHermite::System2D::Riemann2D does (FVHermite_System2D.cpp:94-100):
+    v = (q(x + dx/2, y) - q(x - dx/2, y)) / dx, w likewise in y."""
+    dx, dy = (xr - xl) / nx, (yt - yb) / ny
+    x = xl + (np.arange(nx) + 0.5) * dx
+    y = yb + (np.arange(ny) + 0.5) * dy
+    X, Y = np.meshgrid(x, y)
+    v = (q_fn(X + dx / 2.0, Y) - q_fn(X - dx / 2.0, Y)) / dx
+    w = (q_fn(X, Y + dy / 2.0) - q_fn(X, Y - dy / 2.0)) / dy
+    return np.ascontiguousarray(v), np.ascontiguousarray(w)

@@ -1,0 +1,183 @@
+/*
+ * hteno.h -- C-ABI of the GB300 (sm_103a) implementation of the Hermite-TENO solver hot path:
+ * the semi-discrete residual and the SSP-RK3 stage update of the reference's FV::System2D,
+ * FV::System1D, FVHermite::System2D and FVHermite::System1D (indrow/Hermite-TENO).
+ *
+ * Conventions
+ *   - Every entry point returns an hteno_status; nothing here calls exit() or throws.
+ *   - Conserved state is SoA: q[var][j][i] (2D, var = rho, rho*u, rho*v, E) or q[var][i]
+ *     (1D, var = rho, rho*u, E), interior cells only, row-major in i.  Ghost cells are implicit:
+ *     zero-gradient boundaries read the nearest interior cell, periodic ones wrap.
+ *   - "Batch" entry points take DEVICE pointers and an optional cudaStream_t (NULL = legacy
+ *     default stream) and are asynchronous.  Solver set/get take HOST or DEVICE pointers
+ *     (where = HTENO_HOST / HTENO_DEVICE) and synchronise their stream before returning.
+ *   - A solver handle owns its device buffers; one handle per host thread.  Handles are
+ *     independent and not internally locked.
+ */
+#ifndef HTENO_H
+#define HTENO_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  HTENO_OK = 0,
+  HTENO_ERR_INVALID_ARG = 1,
+  HTENO_ERR_OOM = 2,
+  HTENO_ERR_CUDA = 3,
+  HTENO_ERR_NONPHYSICAL = 4, /* density or pressure <= 0 seen in the state */
+  HTENO_ERR_NAN = 5,         /* a NaN appeared in the state */
+  HTENO_ERR_TIMEOUT = 6,     /* a bounded device-side wait gave up */
+  HTENO_ERR_UNSUPPORTED = 7
+} hteno_status;
+
+typedef enum { HTENO_HOST = 0, HTENO_DEVICE = 1 } hteno_where;
+
+typedef enum { HTENO_SCHEME_FV = 0, HTENO_SCHEME_HERMITE = 1 } hteno_scheme;
+
+/* Reconstruction.  FV: Schemes::Lagrange::teno5 / teno5i / linear.
+ * Hermite 2D: hteno (the reference's choice).  Hermite 1D: LMPE routing (htenoi on troubled
+ * cells, linear elsewhere, FVHermite_System1D.cpp:239-290). */
+typedef enum {
+  HTENO_RECON_TENO5 = 0,
+  HTENO_RECON_TENO5I = 1,
+  HTENO_RECON_LINEAR = 2
+} hteno_recon;
+
+typedef enum { HTENO_FLUX_RUSANOV = 0, HTENO_FLUX_HLLC = 1 } hteno_flux;
+typedef enum { HTENO_BC_ZEROGRAD = 0, HTENO_BC_PERIODIC = 1 } hteno_bc;
+
+/* HTENO_PREC_FP64: everything in double (the plain method).
+ * HTENO_PREC_MIXED: reconstruction, smoothness indicators and fluxes in float; RK stage
+ * accumulation of the conserved variables and the primitive (pressure) recovery in double. */
+typedef enum { HTENO_PREC_FP64 = 0, HTENO_PREC_MIXED = 1 } hteno_precision;
+
+/* Replaces the reference solver constructors, e.g. FV::System2D(xl, xr, nx, yb, yt, ny,
+ * cflnumber, tmax, tInit, specificHeatRatio) (FV_System2D.h:12-15; FV_System1D.h:12-14;
+ * FVHermite_System2D.h:16-19; FVHermite_System1D.h:12-14).  The scheme, flux, reconstruction
+ * and boundary choices the reference makes by commenting code in or out are fields here. */
+typedef struct {
+  int dims;      /* 1 or 2 */
+  int scheme;    /* hteno_scheme */
+  int nx, ny;    /* interior cells (ny ignored for dims == 1) */
+  double xl, xr, yb, yt;
+  double cfl;
+  double gamma;  /* specific heat ratio */
+  double t_init; /* tInit */
+  int recon;     /* hteno_recon */
+  int flux;      /* hteno_flux */
+  int bc;        /* hteno_bc */
+  int precision; /* hteno_precision */
+  int reserved[8];
+} hteno_config;
+
+typedef struct hteno_solver hteno_solver;
+
+/* Fills *cfg with the FV::System2D defaults of the reference as shipped:
+ * 2D, FV, TENO5, Rusanov, zero-gradient, FP64, gamma 1.4, CFL 0.4, [0,1]^2. */
+void hteno_config_default(hteno_config* cfg);
+
+int hteno_create(const hteno_config* cfg, hteno_solver** out);
+int hteno_destroy(hteno_solver* s);
+
+/* Selects the CUDA stream the solver launches on (default: a stream the solver creates). */
+int hteno_set_stream(hteno_solver* s, void* cuda_stream);
+
+/* Initial data (replaces the reference's IC methods, e.g. FV_System2D.cpp:101-112).
+ * q: conserved state [nvar][ny][nx].  Resets the time to t_init and the step count to 0. */
+int hteno_set_state(hteno_solver* s, const double* q, int where);
+int hteno_get_state(hteno_solver* s, double* q, int where);
+/* Hermite schemes: first moments v (d/dx) and, in 2D, w (d/dy), same layout as q. */
+int hteno_set_moments(hteno_solver* s, const double* v, const double* w, int where);
+int hteno_get_moments(hteno_solver* s, double* v, double* w, int where);
+
+/* Advances at most nsteps SSP-RK3 steps, stopping when t reaches t_final (the loop of
+ * timeStepping(), FV_System2D.cpp:614-651, with dt = cfl*min(dx,dy)/max wave speed and the
+ * last step clipped to t_final).  Launches asynchronously and synchronises at the end. */
+int hteno_step(hteno_solver* s, int nsteps, double t_final);
+/* Same as hteno_step without the final synchronisation and status check (for timing loops
+ * and graph replay); call hteno_sync() before reading results. */
+int hteno_step_async(hteno_solver* s, int nsteps, double t_final);
+int hteno_sync(hteno_solver* s);
+int hteno_get_time(hteno_solver* s, double* t, long* steps, double* last_dt);
+
+/* Number of kernel launches hteno_step_async issues per step for this configuration. */
+int hteno_launches_per_step(hteno_solver* s, int* launches);
+
+/* Message of the last failed call on this handle ("" if none). */
+const char* hteno_last_error(hteno_solver* s);
+const char* hteno_status_string(int status);
+
+/* ---- Pointwise batch kernels (device pointers), one reference function each ------------- */
+
+/* Schemes::Lagrange::teno5 / teno5i / linear (Schemes_Lagrange.cpp:481-511, 1235-1263,
+ * 1219-1233): u[n][6] -> out[n][2] = (u^-_{i+1/2}, u^+_{i+1/2}).  kind: hteno_recon.
+ * precision: HTENO_PREC_FP64 computes in double, HTENO_PREC_MIXED in float. */
+int hteno_lagrange_batch(int kind, int precision, const double* u, double* out, long n,
+                         void* stream);
+/* Schemes::Lagrange::weno5JS3PointsQuadrature (Schemes_Lagrange.cpp:1171-1217):
+ * u[n][5] -> out[n][3]. */
+int hteno_gl3_batch(int precision, const double* u, double* out, long n, void* stream);
+/* Schemes::Hermite::hteno / htenoi / linear (Schemes_Hermite.cpp:295-379, 670-758, 760-812)
+ * after setGridSize(dx): u[n][4], d[n][4] -> out[n][4] = (u^-, u^+, d^-, d^+). kind 0/1/2. */
+int hteno_hermite_batch(int kind, int precision, double dx, const double* u, const double* d,
+                        double* out, long n, void* stream);
+/* Schemes::Hermite::hermiteLimiter (Schemes_Hermite.cpp:634-662): u[n][3], d[n][3] -> out[n]. */
+int hteno_hlimiter_batch(int precision, double dx, const double* u, const double* d, double* out,
+                         long n, void* stream);
+/* Equations::Euler2D::HLLC (Equations_Euler2D.cpp:372-428): ql[n][4], qr[n][4] -> out[n][4]. */
+int hteno_hllc2d_batch(int precision, double gamma, int dir, const double* ql, const double* qr,
+                       double* out, long n, void* stream);
+/* Equations::Euler1D::HLLC (Equations_Euler1D.cpp:156-210): [n][3]. */
+int hteno_hllc1d_batch(int precision, double gamma, const double* ql, const double* qr,
+                       double* out, long n, void* stream);
+/* Characteristic Rusanov as called in FV_System2D.cpp:460-464: the face eigenvectors are the
+ * Roe average of the cell pair (qa, qb) (eigen2DEuler, FV_System2D.cpp:265-361);
+ * Rusanov(ql, qr, ..., L, R, maxLocalWaveSpeed(w(ql), w(qr)), dir).  All [n][4]. */
+int hteno_rusanov2d_batch(int precision, double gamma, int dir, const double* qa,
+                          const double* qb, const double* ql, const double* qr, double* out,
+                          long n, void* stream);
+/* Derivative-moment Rusanov (Equations_Euler2D.cpp:352-360) as called in
+ * FVHermite_System2D.cpp:553-589, eigenvectors from the cell pair (qa, qb).  All [n][4]. */
+int hteno_drusanov2d_batch(int precision, double gamma, int dir, const double* qa,
+                           const double* qb, const double* ql, const double* qr,
+                           const double* dql, const double* dqr, double* out, long n,
+                           void* stream);
+/* Schemes::SSPRK::RungeKuttaIII (Schemes_SSPRK.cpp:3-15), elementwise over n doubles. */
+int hteno_ssprk3_batch(const double* q0, const double* qn, const double* rhs, double dt,
+                       int stage, double* out, long n, void* stream);
+/* One residual evaluation of FV::System2D::rhs (FV_System2D.cpp:363-573) at state q[4][ny][nx]
+ * (device) into rhs[4][ny][nx] (device), using the solver's configuration and buffers. */
+int hteno_residual(hteno_solver* s, const double* q, double* rhs);
+
+/* ---- Tracing: per-kernel CUDA-event timing of hteno_step ---------------------------------- */
+
+/* When enabled, every kernel launch of hteno_step[_async] is bracketed by CUDA events on the
+ * solver's stream; hteno_kernel_timing() then reports, per kernel kind, the launch count, the
+ * summed device time and the algorithmic DRAM bytes and flops of one launch.  Enabling resets
+ * the counters.  (No reference counterpart: the reference's only timer is a clock() around
+ * timeStepping, FVHermite_System1D.cpp:388-404.) */
+typedef struct {
+  char name[32];
+  long launches;
+  double ms;             /* summed event time */
+  double bytes_per_launch; /* algorithmic DRAM bytes of one launch */
+  double flops_per_launch; /* algorithmic floating-point operations of one launch */
+} hteno_kernel_time;
+
+int hteno_enable_kernel_timing(hteno_solver* s, int on);
+/* Fills up to max entries (one per kernel kind); *count receives the number of kinds. */
+int hteno_kernel_timing(hteno_solver* s, hteno_kernel_time* out, int max, int* count);
+
+/* Measured throughput of this device's FMA pipes, for roofline denominators:
+ * kind 0 = FP64 FMA, 1 = FP32 FMA; result in TFLOP/s (2 flops per FMA). */
+int hteno_measure_fma_peak(int kind, double* tflops);
+
+/* Version string of the library build. */
+const char* hteno_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* HTENO_H */

@@ -30,7 +30,8 @@ using std::sqrt;
 
 template <typename T>
 inline T catchnan(T x, T machine_eps) {  // Schemes_Lagrange.cpp:1151-1153
-  return std::isnan(x) ? machine_eps : x;
+  using std::isnan;
+  return isnan(x) ? machine_eps : x;
 }
 
 // =============================================================================================
@@ -1126,6 +1127,371 @@ struct FV1D {
       ++s;
     }
     return s;
+  }
+};
+
+// FVHermite::System2D (FVHermite_System2D.cpp): u plus first moments v = d/dx, w = d/dy.
+// rhs :429-731 (zeroGradBc, limitDerivatives, zeroGradBc, primitives, eigen2DEuler, HTENO on
+// (u, v) in x and (u, w) in y, TENO5 for the cross moment, GL3 transverse for all of them,
+// Rusanov for u and dRusanov for v, w); RungeKutta3 :733-782; timeStepping :784-819.
+// The Hermite coefficients use dx for both directions (setGridSize(dx), :28).
+// limitDerivatives (:393-427) updates v in place while sweeping i (and w while sweeping j);
+// with one thread that is a Gauss-Seidel sweep, which is the semantics restated here.
+struct Hermite2D {
+  int nx, ny;
+  double dx, dy, area, cfl, gamma, t = 0.0, dt = 0.0;
+  HermiteCoef HK;
+  std::vector<double> q, v, w, q0, v0, w0, ru, rv, rw;  // [4][ny][nx]
+
+  Hermite2D(int nx_, int ny_, double xl0, double xr0, double yb, double yt, double cfl_, double g)
+      : nx(nx_), ny(ny_), cfl(cfl_), gamma(g), HK((xr0 - xl0) / nx_) {
+    dx = (xr0 - xl0) / nx;
+    dy = (yt - yb) / ny;
+    area = dx * dy;
+    const size_t n = 4 * size_t(nx) * ny;
+    q.assign(n, 0.0); v = q; w = q; q0 = q; v0 = q; w0 = q; ru = q; rv = q; rw = q;
+  }
+  size_t c(int var, int i, int j) const { return (size_t(var) * ny + j) * nx + i; }
+  size_t cm(int var, int i, int j) const {
+    return c(var, bcmap(i, nx, BC_ZEROGRAD), bcmap(j, ny, BC_ZEROGRAD));
+  }
+
+  void limit() {
+    std::vector<double> vold = v, wold = w;
+    // x: v along each row, i increasing; ghost neighbours hold the pre-sweep values
+#pragma omp parallel for
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i)
+        for (int e = 0; e < 4; ++e) {
+          double uu[3] = {q[cm(e, i - 1, j)], q[c(e, i, j)], q[cm(e, i + 1, j)]};
+          double dd[3] = {i > 0 ? v[c(e, i - 1, j)] : vold[c(e, 0, j)], v[c(e, i, j)],
+                          i + 1 < nx ? v[c(e, i + 1, j)] : vold[c(e, nx - 1, j)]};
+          v[c(e, i, j)] = hermite_limiter(HK, uu, dd);
+        }
+    // y: w along each column, j increasing
+#pragma omp parallel for
+    for (int i = 0; i < nx; ++i)
+      for (int j = 0; j < ny; ++j)
+        for (int e = 0; e < 4; ++e) {
+          double uu[3] = {q[cm(e, i, j - 1)], q[c(e, i, j)], q[cm(e, i, j + 1)]};
+          double dd[3] = {j > 0 ? w[c(e, i, j - 1)] : wold[c(e, i, 0)], w[c(e, i, j)],
+                          j + 1 < ny ? w[c(e, i, j + 1)] : wold[c(e, i, ny - 1)]};
+          w[c(e, i, j)] = hermite_limiter(HK, uu, dd);
+        }
+  }
+
+  void residual() {
+    Euler2<double> E(gamma);
+    const LagrangeCoef& K = lag();
+    limit();
+    // cell primitives
+    std::vector<double> pw(4 * size_t(nx) * ny), psr(size_t(nx) * ny), ph(size_t(nx) * ny);
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i) {
+        double qq[4], ww[4];
+        for (int e = 0; e < 4; ++e) qq[e] = q[c(e, i, j)];
+        E.primitive(qq, ww);
+        for (int e = 0; e < 4; ++e) pw[c(e, i, j)] = ww[e];
+        psr[c(0, i, j)] = std::sqrt(std::fabs(ww[0]));
+        ph[c(0, i, j)] = (qq[3] + ww[3]) / ww[0];
+      }
+    // face reconstruction, both directions.  Per face: 6 characteristic arrays x 4 fields:
+    // 0 u-, 1 u+, 2 dn- (moment along the sweep), 3 dn+, 4 dt- (cross moment), 5 dt+
+    for (int dir = 1; dir <= 2; ++dir) {
+      const int nf = dir == 1 ? nx + 1 : ny + 1, nt = dir == 1 ? ny : nx;
+      std::vector<double> fc(size_t(24) * nf * nt), fR(size_t(16) * nf * nt), fL(size_t(16) * nf * nt);
+      std::vector<double>& qn = dir == 1 ? v : w;   // moment along the sweep (HTENO)
+      std::vector<double>& qt = dir == 1 ? w : v;   // cross moment (TENO5)
+#pragma omp parallel for
+      for (int t_ = 0; t_ < nt; ++t_)
+        for (int f = 0; f < nf; ++f) {
+          auto at = [&](int e, int s) { return dir == 1 ? cm(e, s, t_) : cm(e, t_, s); };
+          double wa[4], wb[4], R[16], L[16];
+          for (int e = 0; e < 4; ++e) { wa[e] = pw[at(e, f - 1)]; wb[e] = pw[at(e, f)]; }
+          E.roe(dir, wa, psr[at(0, f - 1)], ph[at(0, f - 1)], wb, psr[at(0, f)], ph[at(0, f)], R, L);
+          auto proj = [&](const std::vector<double>& src, int s, double* out4) {
+            double x[4];
+            for (int e = 0; e < 4; ++e) x[e] = src[at(e, s)];
+            for (int r = 0; r < 4; ++r) {
+              double acc = L[4 * r] * x[0];
+              for (int k2 = 1; k2 < 4; ++k2) acc = acc + L[4 * r + k2] * x[k2];
+              out4[r] = acc;
+            }
+          };
+          double A[4][4], B[4][4], C6[4][6];
+          for (int m = 0; m < 4; ++m) {
+            double a4[4], b4[4];
+            proj(q, f - 2 + m, a4);
+            proj(qn, f - 2 + m, b4);
+            for (int r = 0; r < 4; ++r) { A[r][m] = a4[r]; B[r][m] = b4[r]; }
+          }
+          for (int m = 0; m < 6; ++m) {
+            double c4[4];
+            proj(qt, f - 3 + m, c4);
+            for (int r = 0; r < 4; ++r) C6[r][m] = c4[r];
+          }
+          const size_t o = size_t(t_) * nf + f, stride = size_t(nf) * nt;
+          for (int r = 0; r < 4; ++r) {
+            double hv[4], tv[2];
+            hermite_recon(HK, 0, A[r], B[r], hv);
+            lagrange_recon(RECON_TENO5, C6[r], tv);
+            fc[(0 * 4 + r) * stride + o] = hv[0];
+            fc[(1 * 4 + r) * stride + o] = hv[1];
+            fc[(2 * 4 + r) * stride + o] = hv[2];
+            fc[(3 * 4 + r) * stride + o] = hv[3];
+            fc[(4 * 4 + r) * stride + o] = tv[0];
+            fc[(5 * 4 + r) * stride + o] = tv[1];
+          }
+          for (int k2 = 0; k2 < 16; ++k2) { fR[k2 * stride + o] = R[k2]; fL[k2 * stride + o] = L[k2]; }
+        }
+      // transverse GL3 + fluxes
+      std::vector<double> F(size_t(12) * nf * nt);  // [3 kinds][4][face]
+#pragma omp parallel for
+      for (int t_ = 0; t_ < nt; ++t_)
+        for (int f = 0; f < nf; ++f) {
+          const size_t stride = size_t(nf) * nt, o = size_t(t_) * nf + f;
+          double G[6][4][3];
+          for (int a = 0; a < 6; ++a)
+            for (int r = 0; r < 4; ++r) {
+              double u5[5];
+              for (int m = 0; m < 5; ++m)
+                u5[m] = fc[(a * 4 + r) * stride + size_t(bcmap(t_ - 2 + m, nt, BC_ZEROGRAD)) * nf + f];
+              gl3(u5, G[a][r]);
+            }
+          double R[16], L[16];
+          for (int k2 = 0; k2 < 16; ++k2) { R[k2] = fR[k2 * stride + o]; L[k2] = fL[k2 * stride + o]; }
+          // conservative values at the Gauss points: transformToConservativeAtGQ
+          double X[6][3][4];
+          for (int a = 0; a < 6; ++a)
+            for (int m = 0; m < 3; ++m)
+              for (int i2 = 0; i2 < 4; ++i2) {
+                double acc = R[4 * i2] * G[a][0][m];
+                for (int k2 = 1; k2 < 4; ++k2) acc = acc + R[4 * i2 + k2] * G[a][k2][m];
+                X[a][m][i2] = acc;
+              }
+          double Fu[3][4], Fn[3][4], Ft[3][4];
+          for (int m = 0; m < 3; ++m) {
+            double fu[4], fn[4], ft[4];
+            E.rusanov(dir, X[0][m], X[1][m], L, R, fu);
+            E.drusanov(dir, X[0][m], X[1][m], X[2][m], X[3][m], L, R, fn);
+            E.drusanov(dir, X[0][m], X[1][m], X[4][m], X[5][m], L, R, ft);
+            for (int i2 = 0; i2 < 4; ++i2) {
+              Fu[m][i2] = K.gl3w[m] * fu[i2];
+              Fn[m][i2] = K.gl3w[m] * fn[i2];
+              Ft[m][i2] = K.gl3w[m] * ft[i2];
+            }
+          }
+          for (int i2 = 0; i2 < 4; ++i2) {
+            F[(0 * 4 + i2) * stride + o] = (Fu[0][i2] + Fu[1][i2]) + Fu[2][i2];
+            F[(1 * 4 + i2) * stride + o] = (Fn[0][i2] + Fn[1][i2]) + Fn[2][i2];
+            F[(2 * 4 + i2) * stride + o] = (Ft[0][i2] + Ft[1][i2]) + Ft[2][i2];
+          }
+        }
+      // flux differences: kind 0 -> u, 1 -> moment along this sweep, 2 -> cross moment
+      for (int j = 0; j < ny; ++j)
+        for (int i = 0; i < nx; ++i)
+          for (int e = 0; e < 4; ++e) {
+            const size_t stride = size_t(nf) * nt;
+            const int f0 = dir == 1 ? i : j, t0 = dir == 1 ? j : i;
+            const size_t oa = size_t(t0) * nf + f0, ob = oa + 1;
+            for (int kind = 0; kind < 3; ++kind) {
+              const double d = F[(kind * 4 + e) * stride + oa] - F[(kind * 4 + e) * stride + ob];
+              std::vector<double>& dst = kind == 0 ? ru : ((kind == 1) == (dir == 1) ? rv : rw);
+              if (dir == 1) dst[c(e, i, j)] = d;  // (F(i-1) - F(i)), combined below
+              else dst[c(e, i, j)] = (dst[c(e, i, j)] * dy + d * dx) / area + 0.0;
+            }
+          }
+    }
+  }
+
+  double compute_dt(double tFinal) {
+    Euler2<double> E(gamma);
+    double mx = 0.0, my = 0.0;
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i) {
+        double qq[4], ww[4];
+        for (int e = 0; e < 4; ++e) qq[e] = q[c(e, i, j)];
+        E.primitive(qq, ww);
+        mx = std::fmax(mx, E.maxSpeed(ww, 1));
+        my = std::fmax(my, E.maxSpeed(ww, 2));
+      }
+    double d = cfl * std::pow(std::fmin(dx, dy), 3.0 / 3.0) / std::fmax(mx, my) / 1.0;
+    return t + d > tFinal ? tFinal - t : d;
+  }
+  // RungeKutta3 (:733-782): save() runs after the first rhs(), so v0, w0 are the limited
+  // moments; stages 2 and 3 combine with the unlimited stage values v1, v2 (cell.v1 / cell.v2).
+  void rk3() {
+    const size_t n = q.size();
+    std::vector<double> qs = q, vs = v, ws = w;  // u_{s}, v_{s}, w_{s} as stored by update1/2
+    for (int stage = 1; stage <= 3; ++stage) {
+      residual();
+      if (stage == 1) { q0 = q; v0 = v; w0 = w; qs = q0; vs = v0; ws = w0; }
+      for (size_t k = 0; k < n; ++k) {
+        qs[k] = ssprk3(q0[k], qs[k], ru[k], dt, stage);
+        vs[k] = ssprk3(v0[k], vs[k], rv[k], dt, stage);
+        ws[k] = ssprk3(w0[k], ws[k], rw[k], dt, stage);
+      }
+      q = qs; v = vs; w = ws;
+    }
+  }
+  int run(int nsteps, double tFinal) {
+    int s = 0;
+    while (t < tFinal && s < nsteps) {
+      dt = compute_dt(tFinal);
+      rk3();
+      t += dt;
+      ++s;
+    }
+    return s;
+  }
+};
+
+// FVHermite::System1D (FVHermite_System1D.cpp): periodic boundaries (:201), LMPE troubled-cell
+// flags (:239-257) that start false and are never reset, the derivative limiter applied once
+// over the padded range when any flag in [s+1, nxx-s-1) is set (:259-273; the loop reuses the
+// outer index, so it runs at most once per rhs), htenoi on flagged cells and linear elsewhere
+// (:278-291), Rusanov + dRusanov (:306-337), dt = cfl * dx^(5/3) / max speed (:396).
+// Flags live on the ghost-padded index space [0, nx + 2k) exactly as in the reference.
+struct Hermite1D {
+  static const int k = 4, s = 1;
+  int nx, nxx;
+  double dx, area, cfl, gamma, t = 0.0, dt = 0.0;
+  HermiteCoef HK;
+  std::vector<double> u, v, u0, v0, ru, rv;  // padded [3][nxx]
+  std::vector<unsigned char> flag;           // padded [nxx][3]
+
+  Hermite1D(int nx_, double x0, double x1, double cfl_, double g)
+      : nx(nx_), nxx(nx_ + 2 * k), cfl(cfl_), gamma(g), HK((x1 - x0) / nx_) {
+    dx = (x1 - x0) / nx;
+    area = dx;
+    u.assign(3 * size_t(nxx), 0.0); v = u; u0 = u; v0 = u; ru = u; rv = u;
+    flag.assign(3 * size_t(nxx), 0);
+  }
+  double& U(int e, int i) { return u[size_t(e) * nxx + i]; }
+  double& V(int e, int i) { return v[size_t(e) * nxx + i]; }
+  void periodic() {  // periodicBc (:161-170)
+    for (int m = 0; m < k; ++m)
+      for (int e = 0; e < 3; ++e) {
+        U(e, k - 1 - m) = U(e, nx + k - 1 - m);
+        U(e, nxx - 1 - m) = U(e, k + k - 1 - m);
+        V(e, k - 1 - m) = V(e, nx + k - 1 - m);
+        V(e, nxx - 1 - m) = V(e, k + k - 1 - m);
+      }
+  }
+  void residual() {
+    Euler1<double> E(gamma);
+    periodic();
+    // LMPE
+    for (int e = 0; e < 3; ++e)
+      for (int i = s + 1; i < nxx - s - 1; ++i) {
+        if (flag[size_t(i) * 3 + e]) continue;
+        double A = std::fabs(-U(e, i - 1) + 2.0 * U(e, i) - U(e, i + 1)) / 2.0;
+        if (A > 0.5 * dx) {
+          double xc = (-2. * U(e, i - 1) + 3. * U(e, i) - U(e, i + 1)) /
+                      (-U(e, i - 1) + 2.0 * U(e, i) - U(e, i + 1)) * dx;
+          if (0.0 <= xc && xc <= 3. * dx) {
+            flag[size_t(i) * 3 + e] = 1;
+            flag[size_t(i - 1) * 3 + e] = 1;
+            flag[size_t(i + 1) * 3 + e] = 1;
+          }
+        }
+      }
+    bool any = false;
+    for (int i = s + 1; i < nxx - s - 1 && !any; ++i)
+      any = flag[size_t(i) * 3] || flag[size_t(i) * 3 + 1] || flag[size_t(i) * 3 + 2];
+    if (any)
+      for (int i = k - 1; i < nxx - k + 1; ++i) {
+        double uu[3][3], vv[3][3];
+        for (int m = 0; m < 3; ++m)
+          for (int e = 0; e < 3; ++e) { uu[e][m] = U(e, i - 1 + m); vv[e][m] = V(e, i - 1 + m); }
+        for (int e = 0; e < 3; ++e) V(e, i) = hermite_limiter(HK, uu[e], vv[e]);
+      }
+    periodic();
+    // faces i in [k-1, nxx-k): between padded cells i and i+1
+    std::vector<double> Fu(3 * size_t(nxx)), Fv(3 * size_t(nxx));
+    for (int i = k - 1; i < nxx - k; ++i) {
+      double qa[3], qb[3], wa[3], wb[3], R[9], L[9];
+      for (int e = 0; e < 3; ++e) { qa[e] = U(e, i); qb[e] = U(e, i + 1); }
+      E.primitive(qa, wa);
+      E.primitive(qb, wb);
+      E.roe(wa, std::sqrt(std::fabs(wa[0])), (qa[2] + wa[2]) / wa[0], wb,
+            std::sqrt(std::fabs(wb[0])), (qb[2] + wb[2]) / wb[0], R, L);
+      double A[3][4], B[3][4];
+      for (int m = 0; m < 4; ++m)
+        for (int r = 0; r < 3; ++r) {
+          double a = L[3 * r] * U(0, i - 1 + m), b = L[3 * r] * V(0, i - 1 + m);
+          for (int k2 = 1; k2 < 3; ++k2) {
+            a = a + L[3 * r + k2] * U(k2, i - 1 + m);
+            b = b + L[3 * r + k2] * V(k2, i - 1 + m);
+          }
+          A[r][m] = a;
+          B[r][m] = b;
+        }
+      double cl[4][3];  // [u-, u+, v-, v+][field]
+      for (int r = 0; r < 3; ++r) {
+        double o[4];
+        hermite_recon(HK, flag[size_t(i) * 3 + r] ? 1 : 2, A[r], B[r], o);
+        for (int a = 0; a < 4; ++a) cl[a][r] = o[a];
+      }
+      double X[4][3];
+      for (int a = 0; a < 4; ++a)
+        for (int i2 = 0; i2 < 3; ++i2) {
+          double acc = R[3 * i2] * cl[a][0];
+          for (int k2 = 1; k2 < 3; ++k2) acc = acc + R[3 * i2 + k2] * cl[a][k2];
+          X[a][i2] = acc;
+        }
+      double fu[3], fv[3];
+      E.rusanov(X[0], X[1], L, R, fu);
+      E.drusanov(X[0], X[1], X[2], X[3], L, R, fv);
+      for (int e = 0; e < 3; ++e) { Fu[size_t(e) * nxx + i] = fu[e]; Fv[size_t(e) * nxx + i] = fv[e]; }
+    }
+    for (int i = k; i < nxx - k; ++i)
+      for (int e = 0; e < 3; ++e) {
+        ru[size_t(e) * nxx + i] = (Fu[size_t(e) * nxx + i - 1] - Fu[size_t(e) * nxx + i]) / area;
+        rv[size_t(e) * nxx + i] = (Fv[size_t(e) * nxx + i - 1] - Fv[size_t(e) * nxx + i]) / area;
+      }
+  }
+  double compute_dt(double tFinal) {
+    Euler1<double> E(gamma);
+    double mx = 0.0;
+    for (int i = k; i < nxx - k; ++i) {
+      double qq[3] = {U(0, i), U(1, i), U(2, i)}, ww[3];
+      E.primitive(qq, ww);
+      mx = std::fmax(mx, E.maxSpeed(ww));
+    }
+    double d = cfl * std::pow(dx, 5.0 / 3.0) / mx;
+    return t + d > tFinal ? tFinal - t : d;
+  }
+  // RungeKutta3 (:345-381): save() after the first rhs() (v0 may be limited); stages 2 and 3
+  // combine with the unlimited stage values v1, v2.
+  void rk3() {
+    std::vector<double> us = u, vs = v;
+    for (int stage = 1; stage <= 3; ++stage) {
+      residual();
+      if (stage == 1) { u0 = u; v0 = v; us = u; vs = v; }
+      for (int e = 0; e < 3; ++e)
+        for (int i = k; i < nxx - k; ++i) {
+          const size_t o = size_t(e) * nxx + i;
+          us[o] = ssprk3(u0[o], us[o], ru[o], dt, stage);
+          vs[o] = ssprk3(v0[o], vs[o], rv[o], dt, stage);
+        }
+      for (int e = 0; e < 3; ++e)
+        for (int i = k; i < nxx - k; ++i) {
+          const size_t o = size_t(e) * nxx + i;
+          u[o] = us[o];
+          v[o] = vs[o];
+        }
+    }
+  }
+  int run(int nsteps, double tFinal) {
+    int st = 0;
+    while (t < tFinal && st < nsteps) {
+      dt = compute_dt(tFinal);
+      rk3();
+      t += dt;
+      ++st;
+    }
+    return st;
   }
 };
 

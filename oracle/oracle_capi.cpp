@@ -89,4 +89,40 @@ int orc_fv1d_run(int nx, double xl, double xr, double cfl, double gamma, int bc,
   return s;
 }
 
+int orc_hermite2d_run(int nx, int ny, double xl, double xr, double yb, double yt, double cfl,
+                      double gamma, int bc, double tFinal, int nsteps, const double* q_in,
+                      const double* v_in, const double* w_in, double* q_out, double* v_out,
+                      double* w_out, double* t_out) {
+  (void)bc;  // the reference's Hermite 2D rhs uses zero-gradient boundaries
+  Hermite2D S(nx, ny, xl, xr, yb, yt, cfl, gamma);
+  const size_t n = S.q.size();
+  std::memcpy(S.q.data(), q_in, sizeof(double) * n);
+  std::memcpy(S.v.data(), v_in, sizeof(double) * n);
+  std::memcpy(S.w.data(), w_in, sizeof(double) * n);
+  int s = S.run(nsteps, tFinal);
+  std::memcpy(q_out, S.q.data(), sizeof(double) * n);
+  std::memcpy(v_out, S.v.data(), sizeof(double) * n);
+  std::memcpy(w_out, S.w.data(), sizeof(double) * n);
+  *t_out = S.t;
+  return s;
+}
+int orc_hermite1d_run(int nx, double xl, double xr, double cfl, double gamma, double tFinal,
+                      int nsteps, const double* q_in, const double* v_in, double* q_out,
+                      double* v_out, double* t_out) {
+  Hermite1D S(nx, xl, xr, cfl, gamma);
+  for (int e = 0; e < 3; ++e)
+    for (int i = 0; i < nx; ++i) {
+      S.U(e, i + Hermite1D::k) = q_in[size_t(e) * nx + i];
+      S.V(e, i + Hermite1D::k) = v_in[size_t(e) * nx + i];
+    }
+  int s = S.run(nsteps, tFinal);
+  for (int e = 0; e < 3; ++e)
+    for (int i = 0; i < nx; ++i) {
+      q_out[size_t(e) * nx + i] = S.U(e, i + Hermite1D::k);
+      v_out[size_t(e) * nx + i] = S.V(e, i + Hermite1D::k);
+    }
+  *t_out = S.t;
+  return s;
+}
+
 }  // extern "C"

@@ -319,4 +319,37 @@ void ref_fv2d_entropy_wave_ic(int nx, int ny, double xl, double xr, double yb, d
       for (int v = 0; v < 4; ++v) q_out[(size_t(v) * ny + j) * nx + i] = S.cell(i + k, j + k).u(v);
 }
 
+// Face eigenvectors of cell pairs computed by the reference's own eigen2DEuler()
+// (FV_System2D.cpp:265-361): pair k sits in cells (2k, 2k+1) of a one-row (dir 1) or
+// one-column (dir 2) grid.  R, L row-major [n][16].
+void ref_roe2d(double gamma, int dir, const double* qa, const double* qb, double* Rout,
+               double* Lout, long n) {
+  Quiet quiet;
+  const int m = int(2 * n);
+  FV::System2D S(0.0, 1.0, dir == 1 ? m : 1, 0.0, 1.0, dir == 1 ? 1 : m, 0.4, 1.0, 0.0, gamma);
+  const int k = S.k;
+  for (long p = 0; p < n; ++p)
+    for (int v = 0; v < 4; ++v) {
+      if (dir == 1) {
+        S.cell(k + 2 * p, k).u(v) = qa[4 * p + v];
+        S.cell(k + 2 * p + 1, k).u(v) = qb[4 * p + v];
+      } else {
+        S.cell(k, k + 2 * p).u(v) = qa[4 * p + v];
+        S.cell(k, k + 2 * p + 1).u(v) = qb[4 * p + v];
+      }
+    }
+  S.calcPrimitiveVariable();
+  S.eigen2DEuler();
+  for (long p = 0; p < n; ++p) {
+    const auto& c = dir == 1 ? S.cell(k + 2 * p, k) : S.cell(k, k + 2 * p);
+    const Eigen::Matrix4d& R = dir == 1 ? c.rightEigenVectorX : c.rightEigenVectorY;
+    const Eigen::Matrix4d& L = dir == 1 ? c.leftEigenVectorX : c.leftEigenVectorY;
+    for (int i = 0; i < 4; ++i)
+      for (int j = 0; j < 4; ++j) {
+        Rout[16 * p + 4 * i + j] = R(i, j);
+        Lout[16 * p + 4 * i + j] = L(i, j);
+      }
+  }
+}
+
 }  // extern "C"

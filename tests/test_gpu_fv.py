@@ -1,0 +1,176 @@
+"""GPU parity of the FV solvers (FV::System2D, FV::System1D) against the oracle and the reference's
+golden runs, plus size-independent properties at full benchmark size.  Called through the C-ABI.
+
+Tolerance (FP64 plain path): relative L-infinity error <= 1e-12 per conserved variable, measured
+against max |q_v| of the reference state."""
+from __future__ import annotations
+
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+GOLD = Path(__file__).resolve().parent / "golden"
+TOL = 1e-12
+
+
+def rel_linf(a, b):
+    ax = tuple(range(1, a.ndim))
+    return (np.abs(a - b).max(axis=ax) / np.abs(b).max(axis=ax)).max()
+
+
+def gpu_run2d(h, q, nsteps, t_final=1e30, **kw):
+    cfg = h.config(dims=2, nx=q.shape[2], ny=q.shape[1], **kw)
+    with h.Solver(cfg) as s:
+        s.set_state(q)
+        s.step(nsteps, t_final)
+        t, n, _ = s.time()
+        return s.get_state(), t, n
+
+
+CONFIGS = [
+    dict(flux=0, recon=0, bc=0),  # the reference as shipped: TENO5 + characteristic Rusanov
+    dict(flux=1, recon=0, bc=0),  # HLLC (the configuration of the 2D benchmark)
+    dict(flux=1, recon=1, bc=1),  # teno5i, periodic
+    dict(flux=0, recon=2, bc=1),  # linear, periodic
+]
+
+
+@pytest.mark.parametrize("cfg", CONFIGS, ids=lambda c: f"flux{c['flux']}-recon{c['recon']}-bc{c['bc']}")
+def test_fv2d_matches_oracle(hteno_lib, cuda, oracle, cfg):
+    from hteno import ic
+
+    q = ic.four_quadrant(40, 28, 17)
+    want, t_o, n_o = oracle.fv2d_run(q, 25, **cfg)
+    got, t_g, n_g = gpu_run2d(hteno_lib, q, 25, **cfg)
+    assert n_g == n_o == 25
+    assert abs(t_g - t_o) <= 1e-14 * t_o
+    assert rel_linf(got, want) <= TOL
+
+
+def test_fv2d_matches_reference_golden(hteno_lib, cuda):
+    g = np.load(GOLD / "solvers.npz")
+    got, t, n = gpu_run2d(hteno_lib, g["fv2d_q0"], int(g["fv2d_steps"]))
+    assert n == int(g["fv2d_steps"])
+    assert rel_linf(got, g["fv2d_q"]) <= TOL
+
+
+def test_fv2d_residual_matches_oracle(hteno_lib, cuda, oracle):
+    from hteno import ic
+
+    q = ic.four_quadrant(33, 21, 2)
+    for flux in (0, 1):
+        want = oracle.fv2d_rhs(q, flux=flux)
+        cfg = hteno_lib.config(dims=2, nx=33, ny=21, flux=flux)
+        with hteno_lib.Solver(cfg) as s:
+            dq = cuda.from_numpy(q).cuda()
+            rhs = cuda.empty_like(dq)
+            s.residual(dq, rhs)
+            got = rhs.cpu().numpy()
+        scale = np.abs(want).max(axis=(1, 2), keepdims=True)
+        assert (np.abs(got - want) / scale).max() <= TOL
+
+
+def test_fv2d_edge_sizes_and_time_clipping(hteno_lib, cuda, oracle):
+    from hteno import ic
+
+    # smallest accepted grid, non-square, stop on t_final mid-run
+    for nx, ny in ((6, 6), (7, 13), (64, 9)):
+        q = ic.four_quadrant(nx, ny, nx * 100 + ny)
+        want, t_o, n_o = oracle.fv2d_run(q, 1000, t_final=0.05, flux=1)
+        got, t_g, n_g = gpu_run2d(hteno_lib, q, 1000, t_final=0.05, flux=1)
+        assert n_g == n_o and t_g == pytest.approx(0.05, abs=0) and t_o == pytest.approx(0.05, abs=0)
+        assert rel_linf(got, want) <= TOL
+
+
+def test_fv2d_constant_state_is_steady(hteno_lib, cuda):
+    q = np.ascontiguousarray(np.broadcast_to(np.array([1.3, 0.2, -0.4, 2.7])[:, None, None], (4, 16, 20)).copy())
+    got, _, _ = gpu_run2d(hteno_lib, q, 5, flux=1)
+    np.testing.assert_allclose(got, q, rtol=1e-14, atol=1e-14)
+
+
+def test_fv2d_nonphysical_state_reports_status(hteno_lib, cuda):
+    """A negative density is reported as HTENO_ERR_NONPHYSICAL after the step (the kernels,
+    like the reference, take sqrt(|rho|) and keep running; nothing faults)."""
+    from hteno import ic, HtenoError
+
+    q = ic.four_quadrant(16, 16, 1)
+    q[0, 5, 5] = -0.5
+    with pytest.raises(HtenoError) as e:
+        gpu_run2d(hteno_lib, q, 1, flux=1)
+    assert e.value.code in (4, 5)
+
+
+def test_fv2d_full_size_properties(hteno_lib, cuda):
+    """The 1024^2 benchmark configuration (HLLC, 200 steps): deterministic, positive, and with
+    periodic boundaries conservative to rounding."""
+    from hteno import ic
+
+    q = ic.four_quadrant(1024, 1024, 0)
+    a, t1, n1 = gpu_run2d(hteno_lib, q, 200, flux=1)
+    b, t2, n2 = gpu_run2d(hteno_lib, q, 200, flux=1)
+    assert n1 == 200 and t1 == t2
+    np.testing.assert_array_equal(a, b)
+    assert a[0].min() > 0
+    c, _, _ = gpu_run2d(hteno_lib, q, 50, flux=1, bc=1)
+    np.testing.assert_allclose(c.sum(axis=(1, 2)), q.sum(axis=(1, 2)), rtol=1e-12)
+
+
+def test_fv2d_transpose_symmetry_gpu(hteno_lib, cuda):
+    from hteno import ic
+
+    q = ic.four_quadrant(96, 96, 4)
+    qt = np.ascontiguousarray(q[[0, 2, 1, 3]].transpose(0, 2, 1))
+    a, _, _ = gpu_run2d(hteno_lib, q, 20, flux=1)
+    b, _, _ = gpu_run2d(hteno_lib, qt, 20, flux=1)
+    assert rel_linf(a, np.ascontiguousarray(b[[0, 2, 1, 3]].transpose(0, 2, 1))) <= TOL
+
+
+def test_fv2d_mixed_precision_error(hteno_lib, cuda, oracle):
+    from hteno import ic
+
+    q = ic.four_quadrant(64, 64, 3)
+    want, _, _ = oracle.fv2d_run(q, 40, flux=1)
+    got, _, _ = gpu_run2d(hteno_lib, q, 40, flux=1, precision=1)
+    l1 = np.abs(got[0] - want[0]).mean()
+    assert l1 <= 1e-4, l1
+
+
+# ---- FV 1D --------------------------------------------------------------------------------
+
+def gpu_run1d(h, q, nsteps, t_final=1e30, **kw):
+    cfg = h.config(dims=1, nx=q.shape[1], **kw)
+    with h.Solver(cfg) as s:
+        s.set_state(q)
+        s.step(nsteps, t_final)
+        t, n, _ = s.time()
+        return s.get_state(), t, n
+
+
+def test_fv1d_sod_teno5_hllc(hteno_lib, cuda, oracle):
+    """The 1D benchmark case: 400 cells, Sod, TENO5 + HLLC, CFL 0.5, t = 0.2."""
+    from hteno import ic
+
+    q = ic.sod(400)
+    want, t_o, n_o = oracle.fv1d_run(q, 100000, t_final=0.2, cfl=0.5, recon=0, flux=1)
+    got, t_g, n_g = gpu_run1d(hteno_lib, q, 100000, t_final=0.2, cfl=0.5, recon=0, flux=1)
+    assert n_g == n_o and t_g == pytest.approx(0.2, abs=0)
+    assert rel_linf(got, want) <= TOL
+
+
+def test_fv1d_matches_reference_golden(hteno_lib, cuda):
+    g = np.load(GOLD / "solvers.npz")
+    got, t, n = gpu_run1d(hteno_lib, g["fv1d_q0"], 100000, t_final=0.2, cfl=0.5, recon=1, flux=0)
+    assert n == int(g["fv1d_steps"])
+    assert rel_linf(got, g["fv1d_q"]) <= TOL
+
+
+def test_fv1d_periodic_and_linear(hteno_lib, cuda, oracle):
+    x = (np.arange(128) + 0.5) / 128
+    rho = 1 + 0.2 * np.sin(2 * np.pi * x)
+    q = np.ascontiguousarray(np.stack([rho, rho * 1.0, 1 / 0.4 + 0.5 * rho]))
+    for recon in (0, 1, 2):
+        want, _, _ = oracle.fv1d_run(q, 30, recon=recon, flux=0, bc=1, cfl=0.5)
+        got, _, _ = gpu_run1d(hteno_lib, q, 30, recon=recon, flux=0, bc=1, cfl=0.5)
+        assert rel_linf(got, want) <= TOL
