@@ -2,7 +2,12 @@
 // teno5i as shipped, or linear) from a 6-cell stencil, HLLC or characteristic Rusanov, SSP-RK3.
 // One thread per face / per cell; a 1D grid of a few hundred cells is a latency case, so a step
 // is 2 + 3 x 2 small launches that the host replays without synchronising (dt on the device).
+// In double the bit-reproducible functions (parity_math.cuh) are used; compiled with
+// --fmad=false.
+#include <type_traits>
+
 #include "hteno_internal.h"
+#include "parity_math.cuh"
 
 namespace hteno {
 namespace {
@@ -35,7 +40,7 @@ __global__ void k1_init(Geo1 G, const double* __restrict__ q, StepState* st) {
   if (i < G.nx) {
     double qq[3] = {q[i], q[G.nx + i], q[2 * G.nx + i]}, w[3], h, sr;
     cell_prim1(G.g1, qq, w, h, sr);
-    ms = max_speed1(G.gamma, w);
+    ms = par::max_speed1(G.gamma, w);
   }
   block_max_to(ms, &st->maxbits);
 }
@@ -56,24 +61,39 @@ __global__ void __launch_bounds__(kThreads) k1_flux(Geo1 G, const double* __rest
   }
   cell_prim1(G.g1, qa, wa, ha, sa);
   cell_prim1(G.g1, qb, wb, hb, sb);
-  const Roe1<T> R = roe1<T>(T(G.g1), T(sa), T(wa[1]), T(ha), T(sb), T(wb[1]), T(hb));
-  T ch[3][6];
-#pragma unroll
-  for (int m = 0; m < 6; ++m) {
-    const int c = bmap(f - 3 + m, n, G.bc);
-    T qq[3] = {T(q[c]), T(q[n + c]), T(q[2 * n + c])}, cc[3];
-    roe1_left(R, qq, cc);
-#pragma unroll
-    for (int r = 0; r < 3; ++r) ch[r][m] = cc[r];
+  T Ff[3];
+  if constexpr (std::is_same<T, double>::value) {
+    double R[9], L[9], ch[3][6];
+    par::eig1(G.g1, sa, wa[1], ha, sb, wb[1], hb, R, L);
+    for (int m = 0; m < 6; ++m) {
+      const int c = bmap(f - 3 + m, n, G.bc);
+      const double qq[3] = {q[c], q[n + c], q[2 * n + c]};
+      double cc[3];
+      par::mv3(L, qq, cc);
+      for (int r = 0; r < 3; ++r) ch[r][m] = cc[r];
+    }
+    double cl[3], cr[3], ql[3], qr[3];
+    for (int r = 0; r < 3; ++r) par::lagrange_recon(c_dev, G.recon, ch[r], cl[r], cr[r]);
+    par::mv3(R, cl, ql);  // transformToConservative (FV_System1D.h:48-51)
+    par::mv3(R, cr, qr);
+    if (G.flux == HTENO_FLUX_HLLC) par::hllc1(G.g1, ql, qr, Ff);
+    else par::rusanov1(G.gamma, G.g1, L, R, ql, qr, Ff);
+  } else {
+    const Roe1<T> R = roe1<T>(T(G.g1), T(sa), T(wa[1]), T(ha), T(sb), T(wb[1]), T(hb));
+    T ch[3][6];
+    for (int m = 0; m < 6; ++m) {
+      const int c = bmap(f - 3 + m, n, G.bc);
+      T qq[3] = {T(q[c]), T(q[n + c]), T(q[2 * n + c])}, cc[3];
+      roe1_left(R, qq, cc);
+      for (int r = 0; r < 3; ++r) ch[r][m] = cc[r];
+    }
+    T cl[3], cr[3], ql[3], qr[3];
+    for (int r = 0; r < 3; ++r) lagrange_recon(c_dev, G.recon, ch[r], cl[r], cr[r]);
+    roe1_right(R, cl, ql);
+    roe1_right(R, cr, qr);
+    if (G.flux == HTENO_FLUX_HLLC) hllc1(T(G.g1), ql, qr, Ff);
+    else rusanov1(T(G.gamma), T(G.g1), R, ql, qr, Ff);
   }
-  T cl[3], cr[3];
-#pragma unroll
-  for (int r = 0; r < 3; ++r) lagrange_recon(c_dev, G.recon, ch[r], cl[r], cr[r]);
-  T ql[3], qr[3], Ff[3];
-  roe1_right(R, cl, ql);  // transformToConservative (FV_System1D.h:48-51)
-  roe1_right(R, cr, qr);
-  if (G.flux == HTENO_FLUX_HLLC) hllc1(T(G.g1), ql, qr, Ff);
-  else rusanov1(T(G.gamma), T(G.g1), R, ql, qr, Ff);
   for (int v = 0; v < 3; ++v) F[v * (n + 1) + f] = Ff[v];
 }
 
@@ -104,7 +124,7 @@ __global__ void k1_update(Geo1 G, int stage, const T* __restrict__ F, double* __
     }
     double w[3], h, sr;
     cell_prim1(G.g1, qn, w, h, sr);
-    if (stage == 3) ms = max_speed1(G.gamma, w);
+    if (stage == 3) ms = par::max_speed1(G.gamma, w);
     bad = (isnan(qn[0]) || isnan(qn[1]) || isnan(qn[2])) ? 1 : 0;
     bad |= (qn[0] <= 0.0 || w[2] <= 0.0) ? 2 : 0;
   }

@@ -1,7 +1,9 @@
 // FV::System2D on the GPU (FV_System2D.cpp:363-651): characteristic TENO5 per direction,
 // transverse three-point Gauss-Legendre WENO5-JS along each face, HLLC or characteristic
-// Rusanov at the Gauss points, SSP-RK3.  T = double (plain path) or float (mixed path); the
-// conserved state, its step-start copy, the primitive recovery and the RK update stay double.
+// Rusanov at the Gauss points, SSP-RK3.  This file holds the host dispatch and the mixed path
+// (T = float for reconstruction and fluxes; the conserved state, its step-start copy, the
+// primitive recovery and the RK update stay double).  The plain FP64 path is the
+// bit-reproducible one in fv2d_fp64.cu.
 //
 // One stage = 5 launches, one step = 3 stages + 2 bookkeeping launches:
 //   faces<X>, faces<Y> : Roe average -> L, project the 6-cell stencil, TENO5 both sides for the
@@ -13,7 +15,7 @@
 // The host never synchronises inside hteno_step: dt, t and the stop flag live on the device.
 #include <algorithm>
 
-#include "hteno_internal.h"
+#include "fv2d_common.cuh"
 
 namespace hteno {
 namespace {
@@ -22,52 +24,7 @@ __constant__ DevConst c_dev;
 unsigned long long g_mask = 0;
 std::mutex g_mu;
 
-constexpr int kFaceThreads = 128;
-
 #include "common_kernels.cuh"
-
-struct Geo {
-  int nx, ny, bc, recon, flux;
-  double dx, dy, area, gamma, g1;
-};
-
-// work buffer layout ------------------------------------------------------------------------
-template <typename T>
-struct Work {
-  double* prim;  // [4][ncell]: u, v, h, sqrt|rho|
-  T* xc;         // [8][ny][nx+1]  characteristic face values (l0..l3, r0..r3)
-  T* xroe;       // [7][ny][nx+1]  vxm, vym, hm, qm, cm, rcm, b1
-  T* yc;         // [8][ny+1][nx]
-  T* yroe;       // [7][ny+1][nx]
-  T* fx;         // [4][ny][nx+1]
-  T* fy;         // [4][ny+1][nx]
-};
-
-template <typename T>
-size_t work_bytes(int nx, int ny) {
-  const size_t nc = size_t(nx) * ny, nxf = size_t(nx + 1) * ny, nyf = size_t(ny + 1) * nx;
-  return 4 * nc * sizeof(double) + (8 + 7 + 4) * (nxf + nyf) * sizeof(T) + 256 * 8;
-}
-
-template <typename T>
-Work<T> carve(void* base, int nx, int ny) {
-  const size_t nc = size_t(nx) * ny, nxf = size_t(nx + 1) * ny, nyf = size_t(ny + 1) * nx;
-  char* p = static_cast<char*>(base);
-  auto take = [&](size_t bytes) {
-    char* r = p;
-    p += (bytes + 255) & ~size_t(255);
-    return r;
-  };
-  Work<T> w;
-  w.prim = reinterpret_cast<double*>(take(4 * nc * sizeof(double)));
-  w.xc = reinterpret_cast<T*>(take(8 * nxf * sizeof(T)));
-  w.xroe = reinterpret_cast<T*>(take(7 * nxf * sizeof(T)));
-  w.yc = reinterpret_cast<T*>(take(8 * nyf * sizeof(T)));
-  w.yroe = reinterpret_cast<T*>(take(7 * nyf * sizeof(T)));
-  w.fx = reinterpret_cast<T*>(take(4 * nxf * sizeof(T)));
-  w.fy = reinterpret_cast<T*>(take(4 * nyf * sizeof(T)));
-  return w;
-}
 
 // primitives of one cell: calcPrimitiveVariable (FV_System2D.cpp:226-263)
 __device__ __forceinline__ void cell_prim(double g1, const double* q, double& u, double& v,
@@ -272,13 +229,6 @@ __global__ void k_update(Geo G, int stage, const T* __restrict__ fx, const T* __
   if (bad && st) atomicOr(&st->status, bad);
 }
 
-// Algorithmic flops of the reference per face / per cell of one stage (op-counted on the
-// oracle build, oracle/opcount.cpp): +, -, *, /, sqrt count one each, pow one per call.
-constexpr double kFacesFlops = 1131.0;       // Roe average, 6 projections, TENO5 x 4 fields
-constexpr double kFluxFlopsHllc = 1603.07;   // GL3 x 8, 6 back-projections, 3 HLLC, quadrature
-constexpr double kFluxFlopsRusanov = 1628.0; // same with characteristic Rusanov
-constexpr double kUpdateFlops = 52.0;        // primitives, flux difference, RK stage
-
 template <typename T>
 int launch_stage(hteno_solver* s, const Geo& G, const Work<T>& W, int stage, const double* q,
                  double* out) {
@@ -340,6 +290,7 @@ Geo geo_of(const hteno_solver* s) {
 int fv2d_setup(hteno_solver* s) {
   if (upload_const(c_dev, &g_mask, &g_mu) != cudaSuccess)
     return set_error(s, HTENO_ERR_CUDA, "constant upload failed");
+  if (fv2d_fp64_setup(s) != HTENO_OK) return HTENO_ERR_CUDA;
   const int nx = s->cfg.nx, ny = s->cfg.ny;
   s->work_bytes = s->cfg.precision == HTENO_PREC_MIXED ? work_bytes<float>(nx, ny)
                                                        : work_bytes<double>(nx, ny);
@@ -352,10 +303,12 @@ int fv2d_setup(hteno_solver* s) {
 int fv2d_prepare(hteno_solver* s) {
   const Geo G = geo_of(s);
   const size_t nc = size_t(G.nx) * G.ny;
-  double* prim = s->cfg.precision == HTENO_PREC_MIXED ? carve<float>(s->work, G.nx, G.ny).prim
-                                                      : carve<double>(s->work, G.nx, G.ny).prim;
-  k_prim<<<unsigned((nc + 255) / 256), 256, 0, s->stream>>>(G, s->q, prim, s->dstate, 1);
-  return cuda_error(s, cudaGetLastError(), "k_prim");
+  if (s->cfg.precision == HTENO_PREC_MIXED)
+    k_prim<<<unsigned((nc + 255) / 256), 256, 0, s->stream>>>(G, s->q, carve<float>(s->work, G.nx, G.ny).prim,
+                                                             s->dstate, 1);
+  else
+    fv2d_fp64_prim(s, G, carve<double>(s->work, G.nx, G.ny), s->q, s->dstate, 1);
+  return cuda_error(s, cudaGetLastError(), "primitives");
 }
 
 int fv2d_step_async(hteno_solver* s, int nsteps) {
@@ -366,7 +319,7 @@ int fv2d_step_async(hteno_solver* s, int nsteps) {
       if (s->cfg.precision == HTENO_PREC_MIXED)
         launch_stage(s, G, carve<float>(s->work, G.nx, G.ny), stage, s->q, nullptr);
       else
-        launch_stage(s, G, carve<double>(s->work, G.nx, G.ny), stage, s->q, nullptr);
+        fv2d_fp64_stage(s, G, carve<double>(s->work, G.nx, G.ny), stage, s->q, nullptr);
     }
     k_end_step<<<1, 1, 0, s->stream>>>(s->dstate);
   }
@@ -382,8 +335,8 @@ int fv2d_residual(hteno_solver* s, const double* q, double* rhs) {
     launch_stage(s, G, W, 0, q, rhs);
   } else {
     Work<double> W = carve<double>(s->work, G.nx, G.ny);
-    k_prim<<<unsigned((nc + 255) / 256), 256, 0, s->stream>>>(G, q, W.prim, s->dstate, 0);
-    launch_stage(s, G, W, 0, q, rhs);
+    fv2d_fp64_prim(s, G, W, q, nullptr, 0);
+    fv2d_fp64_stage(s, G, W, 0, q, rhs);
   }
   return cuda_error(s, cudaGetLastError(), "fv2d residual launch");
 }

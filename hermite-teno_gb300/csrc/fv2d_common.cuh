@@ -1,0 +1,68 @@
+// Layout and launch constants shared by the FV 2D translation units (fv2d.cu: mixed FP32 path
+// and host dispatch; fv2d_fp64.cu: bit-reproducible FP64 path).
+#pragma once
+
+#include "hteno_internal.h"
+
+namespace hteno {
+
+struct Geo {
+  int nx, ny, bc, recon, flux;
+  double dx, dy, area, gamma, g1;
+};
+
+// Work buffer: primitives (double) and per-face intermediates (compute type T).
+template <typename T>
+struct Work {
+  double* prim;  // [4][ncell]: u, v, h, sqrt|rho|
+  T* xc;         // [8][ny][nx+1]  characteristic face values (l0..l3, r0..r3), face basis
+  T* xroe;       // [7][ny][nx+1]  vxm, vym, hm, qm, cm, rcm, b1
+  T* yc;         // [8][ny+1][nx]
+  T* yroe;       // [7][ny+1][nx]
+  T* fx;         // [4][ny][nx+1]  face fluxes (Gauss-Legendre quadrature of the face)
+  T* fy;         // [4][ny+1][nx]
+};
+
+template <typename T>
+inline size_t work_bytes(int nx, int ny) {
+  const size_t nc = size_t(nx) * ny, nxf = size_t(nx + 1) * ny, nyf = size_t(ny + 1) * nx;
+  return 4 * nc * sizeof(double) + (8 + 7 + 4) * (nxf + nyf) * sizeof(T) + 256 * 8;
+}
+
+template <typename T>
+inline Work<T> carve(void* base, int nx, int ny) {
+  const size_t nc = size_t(nx) * ny, nxf = size_t(nx + 1) * ny, nyf = size_t(ny + 1) * nx;
+  char* p = static_cast<char*>(base);
+  auto take = [&](size_t bytes) {
+    char* r = p;
+    p += (bytes + 255) & ~size_t(255);
+    return r;
+  };
+  Work<T> w;
+  w.prim = reinterpret_cast<double*>(take(4 * nc * sizeof(double)));
+  w.xc = reinterpret_cast<T*>(take(8 * nxf * sizeof(T)));
+  w.xroe = reinterpret_cast<T*>(take(7 * nxf * sizeof(T)));
+  w.yc = reinterpret_cast<T*>(take(8 * nyf * sizeof(T)));
+  w.yroe = reinterpret_cast<T*>(take(7 * nyf * sizeof(T)));
+  w.fx = reinterpret_cast<T*>(take(4 * nxf * sizeof(T)));
+  w.fy = reinterpret_cast<T*>(take(4 * nyf * sizeof(T)));
+  return w;
+}
+
+// Algorithmic flops of the reference per face / per cell of one stage, op-counted on the oracle
+// build (oracle/opcount.cpp): +, -, *, /, sqrt count one each, pow one per call.
+constexpr double kFacesFlops = 1131.0;        // Roe average, 6 projections, TENO5 x 4 fields
+constexpr double kFluxFlopsHllc = 1603.07;    // GL3 x 8, 6 back-projections, 3 HLLC, quadrature
+constexpr double kFluxFlopsRusanov = 1628.0;  // the same with characteristic Rusanov
+constexpr double kUpdateFlops = 52.0;         // primitives, flux difference, RK stage
+
+constexpr int kFaceThreads = 128;
+
+// Bit-reproducible FP64 path (fv2d_fp64.cu)
+int fv2d_fp64_setup(hteno_solver* s);
+void fv2d_fp64_prim(hteno_solver* s, const Geo& G, const Work<double>& W, const double* q,
+                    StepState* st, int do_max);
+void fv2d_fp64_stage(hteno_solver* s, const Geo& G, const Work<double>& W, int stage,
+                     const double* q, double* out);
+
+}  // namespace hteno

@@ -1,0 +1,261 @@
+// Plain FP64 path of FV::System2D, bit-reproducible against the reference's arithmetic
+// (see parity_math.cuh).  This translation unit is compiled with --fmad=false.
+//
+// Per stage (FV_System2D.cpp:363-573): faces<X>, faces<Y> (Roe average, characteristic
+// projection of the 6-cell stencil, TENO5 on the 4 fields), flux<X>, flux<Y> (GL3 along the face
+// over the face values of the 5 neighbouring faces, each in its own basis as in the reference;
+// back-projection with the face's R; HLLC or Rusanov at the 3 Gauss points; quadrature), update
+// (flux difference, SSP-RK3 stage, primitives of the new state, max wave speed on stage 3).
+#include "fv2d_common.cuh"
+#include "parity_math.cuh"
+
+namespace hteno {
+namespace {
+
+__constant__ DevConst c_dev;
+unsigned long long g_mask = 0;
+std::mutex g_mu;
+
+#include "common_kernels.cuh"
+
+// primitives: calcPrimitiveVariable (FV_System2D.cpp:226-263)
+__device__ __forceinline__ void cell_prim(double g1, const double* q, double* w, double& h,
+                                          double& sr) {
+  par::primitive(g1, q, w);
+  sr = sqrt(fabs(w[0]));
+  h = (q[3] + w[3]) / w[0];
+}
+
+__global__ void kp_prim(Geo G, const double* __restrict__ q, double* __restrict__ prim,
+                        StepState* st, int do_max) {
+  const size_t nc = size_t(G.nx) * G.ny;
+  const size_t k = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+  double ms = 0.0;
+  if (k < nc) {
+    double qq[4] = {q[k], q[nc + k], q[2 * nc + k], q[3 * nc + k]}, w[4], h, sr;
+    cell_prim(G.g1, qq, w, h, sr);
+    prim[k] = w[1];
+    prim[nc + k] = w[2];
+    prim[2 * nc + k] = h;
+    prim[3 * nc + k] = sr;
+    ms = par::max_speed2(G.gamma, w);
+  }
+  if (do_max) block_max_to(ms, &st->maxbits);
+}
+
+template <int DIR>
+__global__ void __launch_bounds__(kFaceThreads) kp_faces(Geo G, const double* __restrict__ q,
+                                                         const double* __restrict__ prim,
+                                                         double* __restrict__ fc,
+                                                         double* __restrict__ froe,
+                                                         const StepState* st) {
+  if (st && st->done) return;
+  const int nf = DIR == 1 ? G.nx + 1 : G.ny + 1;
+  const int nt = DIR == 1 ? G.ny : G.nx;
+  const long idx = blockIdx.x * long(blockDim.x) + threadIdx.x;
+  if (idx >= long(nf) * nt) return;
+  int f, t;
+  if (DIR == 1) { f = int(idx % nf); t = int(idx / nf); }
+  else { t = int(idx % nt); f = int(idx / nt); }
+  const size_t nc = size_t(G.nx) * G.ny;
+  const int ns = DIR == 1 ? G.nx : G.ny;
+  auto cell = [&](int s) -> size_t {
+    const int m = bmap(s, ns, G.bc);
+    return DIR == 1 ? size_t(t) * G.nx + m : size_t(m) * G.nx + t;
+  };
+  const size_t ca = cell(f - 1), cb = cell(f);
+  const par::Eig E = par::eig(G.g1, DIR, prim[3 * nc + ca], prim[ca], prim[nc + ca],
+                              prim[2 * nc + ca], prim[3 * nc + cb], prim[cb], prim[nc + cb],
+                              prim[2 * nc + cb]);
+  double ch[4][6];
+#pragma unroll
+  for (int m = 0; m < 6; ++m) {
+    const size_t c = cell(f - 3 + m);
+    const double qq[4] = {q[c], q[nc + c], q[2 * nc + c], q[3 * nc + c]};
+    double cc[4];
+    par::left(E, DIR, qq, cc);
+#pragma unroll
+    for (int r = 0; r < 4; ++r) ch[r][m] = cc[r];
+  }
+  const size_t nface = size_t(nf) * nt;
+  const size_t o = DIR == 1 ? size_t(t) * nf + f : size_t(f) * nt + t;
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    double a, b;
+    par::lagrange_recon(c_dev, G.recon, ch[r], a, b);
+    fc[r * nface + o] = a;
+    fc[(4 + r) * nface + o] = b;
+  }
+  froe[0 * nface + o] = E.vxm;
+  froe[1 * nface + o] = E.vym;
+  froe[2 * nface + o] = E.hm;
+  froe[3 * nface + o] = E.qm;
+  froe[4 * nface + o] = E.cm;
+  froe[5 * nface + o] = E.rcm;
+  froe[6 * nface + o] = E.b1;
+}
+
+template <int DIR>
+__global__ void __launch_bounds__(kFaceThreads) kp_flux(Geo G, const double* __restrict__ fc,
+                                                        const double* __restrict__ froe,
+                                                        double* __restrict__ F,
+                                                        const StepState* st) {
+  if (st && st->done) return;
+  const int nf = DIR == 1 ? G.nx + 1 : G.ny + 1;
+  const int nt = DIR == 1 ? G.ny : G.nx;
+  const long idx = blockIdx.x * long(blockDim.x) + threadIdx.x;
+  if (idx >= long(nf) * nt) return;
+  int f, t;
+  if (DIR == 1) { f = int(idx % nf); t = int(idx / nf); }
+  else { t = int(idx % nt); f = int(idx / nt); }
+  const size_t nface = size_t(nf) * nt;
+  size_t nb[5];
+#pragma unroll
+  for (int m = 0; m < 5; ++m) {
+    const int mm = bmap(t - 2 + m, nt, G.bc);
+    nb[m] = DIR == 1 ? size_t(mm) * nf + f : size_t(f) * nt + mm;
+  }
+  double g[8][3];
+#pragma unroll
+  for (int r = 0; r < 8; ++r) {
+    double u5[5];
+#pragma unroll
+    for (int m = 0; m < 5; ++m) u5[m] = fc[r * nface + nb[m]];
+    par::gl3(c_dev, u5, g[r]);
+  }
+  const size_t o = nb[2];
+  par::Eig E;
+  E.vxm = froe[o];
+  E.vym = froe[nface + o];
+  E.hm = froe[2 * nface + o];
+  E.qm = froe[3 * nface + o];
+  E.cm = froe[4 * nface + o];
+  E.rcm = froe[5 * nface + o];
+  E.b1 = froe[6 * nface + o];
+  const double vn = DIR == 1 ? E.vxm : E.vym;  // derived scalars, recomputed bit-identically
+  E.t0r = vn * E.cm;
+  E.b2 = E.qm * E.b1;
+  E.s0 = vn * E.rcm;
+  E.s1 = E.b1 * vn;
+  E.t2 = 0.5 * E.b1;
+  double Fm[3][4];
+#pragma unroll
+  for (int m = 0; m < 3; ++m) {
+    const double cl[4] = {g[0][m], g[1][m], g[2][m], g[3][m]};
+    const double cr[4] = {g[4][m], g[5][m], g[6][m], g[7][m]};
+    double ql[4], qr[4], Fl[4];
+    par::right(E, DIR, cl, ql);
+    par::right(E, DIR, cr, qr);
+    if (G.flux == HTENO_FLUX_HLLC) par::hllc(G.g1, DIR, ql, qr, Fl);
+    else par::rusanov(G.gamma, G.g1, DIR, E, ql, qr, Fl);
+#pragma unroll
+    for (int v = 0; v < 4; ++v) Fm[m][v] = c_dev.gl3w[m] * Fl[v];
+  }
+#pragma unroll
+  for (int v = 0; v < 4; ++v) F[v * nface + o] = (Fm[0][v] + Fm[1][v]) + Fm[2][v];
+}
+
+// rhs (FV_System2D.cpp:562-572) + RungeKutta3 (:575-612); stage 0 writes the residual
+__global__ void kp_update(Geo G, int stage, const double* __restrict__ fx,
+                          const double* __restrict__ fy, double* __restrict__ q,
+                          double* __restrict__ q0, double* __restrict__ prim,
+                          double* __restrict__ out, StepState* st) {
+  if (st && st->done) return;
+  const size_t nc = size_t(G.nx) * G.ny;
+  const size_t k = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+  double ms = 0.0;
+  int bad = 0;
+  if (k < nc) {
+    const int i = int(k % G.nx), j = int(k / G.nx);
+    const size_t nxf = size_t(G.nx + 1) * G.ny, nyf = size_t(G.ny + 1) * G.nx;
+    const size_t ox = size_t(j) * (G.nx + 1) + i, oy = size_t(j) * G.nx + i;
+    double rhs[4];
+#pragma unroll
+    for (int v = 0; v < 4; ++v)
+      rhs[v] = ((fx[v * nxf + ox] - fx[v * nxf + ox + 1]) * G.dy +
+                (fy[v * nyf + oy] - fy[v * nyf + oy + G.nx]) * G.dx) / G.area + 0.0;
+    if (stage == 0) {
+#pragma unroll
+      for (int v = 0; v < 4; ++v) out[v * nc + k] = rhs[v];
+    } else {
+      const double dt = st->dt;
+      double qn[4];
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        const double cur = q[v * nc + k];
+        double base;
+        if (stage == 1) {
+          q0[v * nc + k] = cur;
+          base = cur;
+        } else {
+          base = q0[v * nc + k];
+        }
+        qn[v] = ssprk3(base, cur, rhs[v], dt, stage);
+        q[v * nc + k] = qn[v];
+      }
+      double w[4], h, sr;
+      cell_prim(G.g1, qn, w, h, sr);
+      prim[k] = w[1];
+      prim[nc + k] = w[2];
+      prim[2 * nc + k] = h;
+      prim[3 * nc + k] = sr;
+      if (stage == 3) ms = par::max_speed2(G.gamma, w);
+      bad = (isnan(qn[0]) || isnan(qn[1]) || isnan(qn[2]) || isnan(qn[3])) ? 1 : 0;
+      bad |= (qn[0] <= 0.0 || w[3] <= 0.0) ? 2 : 0;
+    }
+  }
+  if (stage == 3) block_max_to(ms, &st->maxbits);
+  if (bad && st) atomicOr(&st->status, bad);
+}
+
+}  // namespace
+
+int fv2d_fp64_setup(hteno_solver* s) {
+  if (upload_const(c_dev, &g_mask, &g_mu) != cudaSuccess)
+    return set_error(s, HTENO_ERR_CUDA, "constant upload failed");
+  return HTENO_OK;
+}
+
+void fv2d_fp64_prim(hteno_solver* s, const Geo& G, const Work<double>& W, const double* q,
+                    StepState* st, int do_max) {
+  const size_t nc = size_t(G.nx) * G.ny;
+  kp_prim<<<unsigned((nc + 255) / 256), 256, 0, s->stream>>>(G, q, W.prim, st, do_max);
+}
+
+void fv2d_fp64_stage(hteno_solver* s, const Geo& G, const Work<double>& W, int stage,
+                     const double* q, double* out) {
+  cudaStream_t cs = s->stream;
+  const int nx = G.nx, ny = G.ny;
+  const long nxf = long(nx + 1) * ny, nyf = long(ny + 1) * nx;
+  const double ncd = double(nx) * ny;
+  StepState* st = stage == 0 ? nullptr : s->dstate;
+  const double fluxf = G.flux == HTENO_FLUX_HLLC ? kFluxFlopsHllc : kFluxFlopsRusanov;
+  const int kf_x = trace_kind(s, "faces_x", ncd * 64 + double(nxf) * 15 * 8, kFacesFlops * nxf);
+  const int kf_y = trace_kind(s, "faces_y", ncd * 64 + double(nyf) * 15 * 8, kFacesFlops * nyf);
+  const int kx = trace_kind(s, "flux_x", double(nxf) * 19 * 8, fluxf * nxf);
+  const int ky = trace_kind(s, "flux_y", double(nyf) * 19 * 8, fluxf * nyf);
+  const int ku = trace_kind(s, "update", ncd * 128 + double(nxf + nyf) * 4 * 8, kUpdateFlops * ncd);
+  trace_begin(s, kf_x);
+  kp_faces<1><<<unsigned((nxf + kFaceThreads - 1) / kFaceThreads), kFaceThreads, 0, cs>>>(
+      G, q, W.prim, W.xc, W.xroe, st);
+  trace_end(s);
+  trace_begin(s, kf_y);
+  kp_faces<2><<<unsigned((nyf + kFaceThreads - 1) / kFaceThreads), kFaceThreads, 0, cs>>>(
+      G, q, W.prim, W.yc, W.yroe, st);
+  trace_end(s);
+  trace_begin(s, kx);
+  kp_flux<1><<<unsigned((nxf + kFaceThreads - 1) / kFaceThreads), kFaceThreads, 0, cs>>>(
+      G, W.xc, W.xroe, W.fx, st);
+  trace_end(s);
+  trace_begin(s, ky);
+  kp_flux<2><<<unsigned((nyf + kFaceThreads - 1) / kFaceThreads), kFaceThreads, 0, cs>>>(
+      G, W.yc, W.yroe, W.fy, st);
+  trace_end(s);
+  const size_t nc = size_t(nx) * ny;
+  trace_begin(s, ku);
+  kp_update<<<unsigned((nc + 255) / 256), 256, 0, cs>>>(G, stage, W.fx, W.fy, s->q, s->q0,
+                                                       W.prim, out, st);
+  trace_end(s);
+}
+
+}  // namespace hteno

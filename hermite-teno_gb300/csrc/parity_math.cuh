@@ -1,0 +1,464 @@
+// Bit-reproducible FP64 numerics of the plain path.
+//
+// Why: TENO's cut-off is a discontinuous decision.  In the tails of waves the data vary by
+// ~1e-10 relative to their magnitude, so a rounding difference in the characteristic values
+// (1e-16 absolute) can move a weight across the cut-off; the flip then changes the solution by
+// ~1e-10.  Agreement with the reference to 1e-12 over hundreds of steps therefore needs the same
+// rounding, not just the same formulas.  Every function here performs exactly the IEEE
+// operations, in exactly the order, of the reference's expressions (reductions left to right),
+// and this header is only compiled in translation units built with --fmad=false so that no
+// multiply-add is fused.  Divisions and square roots are IEEE correctly rounded, as on the CPU.
+//
+// The one deliberate difference: the TENO cut-off weights (1 + tau/(SI+eps))^6 / sum only select
+// one of 8 cut-off patterns, so they are evaluated with reciprocals and a multiply chain; when a
+// weight lies within a relative 1e-10 of the threshold, the decision is recomputed with the
+// reference's divisions and pow.  The reconstructed values use the pattern's weights from a table
+// built with the reference's own normalisation, so they are bit-identical.
+#pragma once
+
+#include "device_math.cuh"
+
+namespace hteno {
+namespace par {
+
+__device__ __forceinline__ double catchnan(double x) { return isnan(x) ? 1e-15 : x; }
+
+// dot of a 3-vector of coefficients with u[0..2], left to right (Eigen .dot in the reference)
+__device__ __forceinline__ double dot3(double c0, double c1, double c2, const double* u) {
+  double s = c0 * u[0];
+  s = s + c1 * u[1];
+  s = s + c2 * u[2];
+  return s;
+}
+__device__ __forceinline__ double dot3v(const double* p, const double* w) {
+  double s = p[0] * w[0];
+  s = s + p[1] * w[1];
+  s = s + p[2] * w[2];
+  return s;
+}
+
+// ---- Schemes::Lagrange ----------------------------------------------------------------------
+
+// smoothnessMeasure (Schemes_Lagrange.cpp:1013-1026)
+__device__ __forceinline__ void lagrange_si(const double* v, double* SI) {
+  double c[3], b[3];
+  c[0] = v[2] - 2.0 * v[3] + v[4];
+  b[0] = 3.0 * v[2] - 4.0 * v[3] + v[4];
+  c[1] = v[1] - 2.0 * v[2] + v[3];
+  b[1] = v[1] - v[3];
+  c[2] = v[0] - 2.0 * v[1] + v[2];
+  b[2] = v[0] - 4.0 * v[1] + 3.0 * v[2];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) b[k] = b[k] / 2.0;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) SI[k] = b[k] * b[k] + (13.0 / 12.0) * c[k] * c[k];
+}
+// fullpointsSmootness (:1029-1034)
+__device__ __forceinline__ double lagrange_b35(const double* v) {
+  double r = v[4] * (6908.0 * v[4] - 51001.0 * v[3] + 67923.0 * v[2] - 38947.0 * v[1] +
+                     8209.0 * v[0]) +
+             v[3] * (104963.0 * v[3] - 299076.0 * v[2] + 179098.0 * v[1] - 38947.0 * v[0]) +
+             v[2] * (231153.0 * v[2] - 299076.0 * v[1] + 67923.0 * v[0]) +
+             v[1] * (104963.0 * v[1] - 51001.0 * v[0]) + 6908.0 * v[0] * v[0];
+  return r / 5040.0;
+}
+
+// Cut-off pattern of the reference's cutOff() (:1141-1149) given SI and tau.  Fast path with a
+// guard band; inside the band the reference's arithmetic decides.
+__device__ __forceinline__ int cutoff_pattern(const double* SI, double tau, double epsz, double ct) {
+  double r[3], a[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) r[k] = 1.0 + tau * __drcp_rn(SI[k] + epsz);
+  const double rm = fmax(fmax(r[0], r[1]), r[2]);
+  const double inv = __drcp_rn(rm);
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    double x = r[k] * inv;
+    x = x * x;
+    a[k] = x * x * x;
+  }
+  const double S = (a[0] + a[1]) + a[2];
+  const double lim = ct * S;
+  int pat = 0;
+  bool near = false;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    pat |= (a[k] < lim ? 0 : 1) << k;
+    near |= fabs(a[k] - lim) <= 1e-10 * lim;
+  }
+  if (near) {  // reference arithmetic: w_k = pow(1 + tau/(SI_k + epsz), 6) / sum
+    double w[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) w[k] = pow(1.0 + tau / (SI[k] + epsz), 6.0);
+    const double s = (w[0] + w[1]) + w[2];
+    pat = 0;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) pat |= ((w[k] / s) < ct ? 0 : 1) << k;
+  }
+  return pat;
+}
+
+// One side of teno5 (:481-511) / teno5i (:1235-1263) given the candidates p and stencil v.
+__device__ __forceinline__ double teno_side(const DevConst& C, const double* p, const double* v,
+                                            int side, bool improved) {
+  double SI[3];
+  lagrange_si(v, SI);
+  double tau;
+  if (!improved) {
+    const double b35 = lagrange_b35(v);
+    tau = fabs(b35 - (SI[0] + SI[2] + 4.0 * SI[1]) / 6.0);
+  } else {
+    tau = SI[0];
+    tau = (tau < SI[1]) ? SI[1] : tau;
+    tau = (tau < SI[2]) ? SI[2] : tau;
+  }
+  const int pat = cutoff_pattern(SI, tau, HTENO_LAG_EPSZ, HTENO_LAG_CT);
+  const double* w = side ? C.wtab_p[pat] : C.wtab_m[pat];
+  return catchnan(dot3v(p, w));
+}
+
+// kind 0 teno5, 1 teno5i, 2 linear (:1219-1233)
+__device__ __forceinline__ void lagrange_recon(const DevConst& C, int kind, const double* u,
+                                               double& outm, double& outp) {
+  double p[3];
+  p[0] = dot3(C.crj[0][1], C.crj[1][1], C.crj[2][1], u + 2);
+  p[1] = dot3(C.crj[0][2], C.crj[1][2], C.crj[2][2], u + 1);
+  p[2] = dot3(C.crj[0][3], C.crj[1][3], C.crj[2][3], u + 0);
+  outm = kind == 2 ? dot3v(p, C.dkm) : teno_side(C, p, u, 0, kind == 1);
+  p[0] = dot3(C.crj[0][0], C.crj[1][0], C.crj[2][0], u + 3);
+  p[1] = dot3(C.crj[0][1], C.crj[1][1], C.crj[2][1], u + 2);
+  p[2] = dot3(C.crj[0][2], C.crj[1][2], C.crj[2][2], u + 1);
+  outp = kind == 2 ? dot3v(p, C.dkp) : teno_side(C, p, u + 1, 1, kind == 1);
+}
+
+// weno5JS3PointsQuadrature (Schemes_Lagrange.cpp:1155-1217)
+__device__ __forceinline__ void gl3(const DevConst& C, const double* u, double* out) {
+  double bg[3], cg[3], s2[3];
+  bg[0] = u[0] - 4.0 * u[1] + 3.0 * u[2];
+  cg[0] = u[0] - 2.0 * u[1] + u[2];
+  bg[1] = u[1] - u[3];
+  cg[1] = u[1] - 2.0 * u[2] + u[3];
+  bg[2] = 3.0 * u[2] - 4.0 * u[3] + u[4];
+  cg[2] = u[2] - 2.0 * u[3] + u[4];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const double si = 0.25 * (bg[k] * bg[k]) + (13.0 / 12.0) * (cg[k] * cg[k]);
+    const double e = 1e-6 + si;
+    s2[k] = e * e;  // pow(eps + SI, 2)
+  }
+  double p[3], w[3];
+  auto weighted = [&](const double* lw) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) w[k] = lw[k] / s2[k];
+    const double s = (w[0] + w[1]) + w[2];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) w[k] = w[k] / s;
+    return dot3v(p, w);
+  };
+  p[0] = dot3(C.gp[0][0], C.gp[1][0], C.gp[2][0], u + 0);
+  p[1] = dot3(C.gp[0][1], C.gp[1][1], C.gp[2][1], u + 1);
+  p[2] = dot3(C.gp[0][2], C.gp[1][2], C.gp[2][2], u + 2);
+  out[0] = weighted(C.linwp);
+  p[0] = (-u[0] + 2.0 * u[1] + 23.0 * u[2]) / 24.0;
+  p[1] = (-u[1] + 26.0 * u[2] - u[3]) / 24.0;
+  p[2] = (23.0 * u[2] + 2.0 * u[3] - u[4]) / 24.0;
+  double c = C.sumw0p * weighted(C.linw0p);
+  c = c - C.sumw0m * weighted(C.linw0m);
+  out[1] = c;
+  p[0] = dot3(C.gm[0][0], C.gm[1][0], C.gm[2][0], u + 0);
+  p[1] = dot3(C.gm[0][1], C.gm[1][1], C.gm[2][1], u + 1);
+  p[2] = dot3(C.gm[0][2], C.gm[1][2], C.gm[2][2], u + 2);
+  out[2] = weighted(C.linwm);
+#pragma unroll
+  for (int k = 0; k < 3; ++k) out[k] = catchnan(out[k]);
+}
+
+// ---- Equations::Euler2D ---------------------------------------------------------------------
+
+__device__ __forceinline__ void primitive(double g1, const double* q, double* w) {  // :20-26
+  w[0] = q[0];
+  w[1] = q[1] / q[0];
+  w[2] = q[2] / q[0];
+  w[3] = (q[3] - 0.5 * (q[1] * w[1] + q[2] * w[2])) * g1;
+}
+
+__device__ __forceinline__ void flux(int dir, const double* q, const double* w, double* f) {
+  if (dir == 1) {
+    f[0] = q[1];
+    f[1] = q[1] * w[1] + w[3];
+    f[2] = q[1] * w[2];
+    f[3] = w[1] * (q[3] + w[3]);
+  } else {
+    f[0] = q[2];
+    f[1] = q[2] * w[1];
+    f[2] = q[2] * w[2] + w[3];
+    f[3] = w[2] * (q[3] + w[3]);
+  }
+}
+
+// Face eigensystem (eigen2DEuler, FV_System2D.cpp:265-361): the entries of R and L are kept as
+// the scalars the reference's matrices are built from.
+struct Eig {
+  double vxm, vym, hm, qm, cm, t0r;  // t0r = vn * cm (right eigenvectors)
+  double rcm, b1, b2, s0, s1, t2;    // left eigenvectors
+};
+
+__device__ __forceinline__ Eig eig(double g1, int dir, double sra, double ua, double va, double ha,
+                                   double srb, double ub, double vb, double hb) {
+  Eig e;
+  double t0 = sra / (sra + srb);
+  const double t1 = 1.0 - t0;
+  e.vxm = t0 * ua + t1 * ub;
+  e.vym = t0 * va + t1 * vb;
+  e.hm = t0 * ha + t1 * hb;
+  e.qm = 0.5 * (e.vxm * e.vxm + e.vym * e.vym);
+  e.cm = sqrt(fabs(g1 * (e.hm - e.qm)));
+  const double vn = dir == 1 ? e.vxm : e.vym;
+  e.t0r = vn * e.cm;
+  e.rcm = 1.0 / e.cm;
+  e.b1 = g1 * e.rcm * e.rcm;
+  e.b2 = e.qm * e.b1;
+  e.s0 = vn * e.rcm;
+  e.s1 = e.b1 * vn;
+  e.t2 = 0.5 * e.b1;
+  return e;
+}
+
+// L * q with the reference's left-to-right row sums (leftEigenVectorx/y, :133-205).  Zero entries
+// of L add exact zeros in the reference and are skipped; unit entries multiply exactly.
+__device__ __forceinline__ void left(const Eig& e, int dir, const double* q, double* c) {
+  const double l00 = 0.5 * (e.b2 + e.s0), l0n = -0.5 * (e.s1 + e.rcm);
+  const double l30 = 0.5 * (e.b2 - e.s0), l3n = -0.5 * (e.s1 - e.rcm);
+  const double l20 = 1.0 - e.b2;
+  if (dir == 1) {
+    const double lt = -e.t2 * e.vym, l2t = e.b1 * e.vym;
+    double s = l00 * q[0]; s = s + l0n * q[1]; s = s + lt * q[2]; s = s + e.t2 * q[3]; c[0] = s;
+    s = -e.vym * q[0]; s = s + q[2]; c[1] = s;
+    s = l20 * q[0]; s = s + e.s1 * q[1]; s = s + l2t * q[2]; s = s + (-e.b1) * q[3]; c[2] = s;
+    s = l30 * q[0]; s = s + l3n * q[1]; s = s + lt * q[2]; s = s + e.t2 * q[3]; c[3] = s;
+  } else {
+    const double lt = -e.t2 * e.vxm, l2t = e.b1 * e.vxm;
+    double s = l00 * q[0]; s = s + lt * q[1]; s = s + l0n * q[2]; s = s + e.t2 * q[3]; c[0] = s;
+    s = -e.vxm * q[0]; s = s + q[1]; c[1] = s;
+    s = l20 * q[0]; s = s + l2t * q[1]; s = s + e.s1 * q[2]; s = s + (-e.b1) * q[3]; c[2] = s;
+    s = l30 * q[0]; s = s + lt * q[1]; s = s + l3n * q[2]; s = s + e.t2 * q[3]; c[3] = s;
+  }
+}
+
+// R * c (rightEigenVectorx/y, :100-131, 169-180)
+__device__ __forceinline__ void right(const Eig& e, int dir, const double* c, double* q) {
+  double s = c[0]; s = s + c[2]; s = s + c[3]; q[0] = s;
+  if (dir == 1) {
+    s = (e.vxm - e.cm) * c[0]; s = s + e.vxm * c[2]; s = s + (e.vxm + e.cm) * c[3]; q[1] = s;
+    s = e.vym * c[0]; s = s + c[1]; s = s + e.vym * c[2]; s = s + e.vym * c[3]; q[2] = s;
+    s = (e.hm - e.t0r) * c[0]; s = s + e.vym * c[1]; s = s + e.qm * c[2]; s = s + (e.hm + e.t0r) * c[3]; q[3] = s;
+  } else {
+    s = e.vxm * c[0]; s = s + c[1]; s = s + e.vxm * c[2]; s = s + e.vxm * c[3]; q[1] = s;
+    s = (e.vym - e.cm) * c[0]; s = s + e.vym * c[2]; s = s + (e.vym + e.cm) * c[3]; q[2] = s;
+    s = (e.hm - e.t0r) * c[0]; s = s + e.vxm * c[1]; s = s + e.qm * c[2]; s = s + (e.hm + e.t0r) * c[3]; q[3] = s;
+  }
+}
+
+// HLLC (Equations_Euler2D.cpp:372-428)
+__device__ __forceinline__ void hllc(double g1, int dir, const double* ql, const double* qr,
+                                     double* F) {
+  const int d1 = dir - 1;
+  double wl[4], wr[4], fl[4], fr[4], qs[4];
+  primitive(g1, ql, wl);
+  primitive(g1, qr, wr);
+  const double hl = (ql[3] + wl[3]) / wl[0];
+  const double hr = (qr[3] + wr[3]) / wr[0];
+  const double rr = sqrt(fabs(wr[0] / wl[0]));
+  const double rrr = 1.0 / (1.0 + rr);
+  double vm[2];
+  vm[0] = (wl[1] + wr[1] * rr) * rrr;
+  vm[1] = (wl[2] + wr[2] * rr) * rrr;
+  const double qm = 0.5 * (vm[0] * vm[0] + vm[1] * vm[1]);
+  const double hm = (hl + hr * rr) * rrr;
+  const double cm = sqrt(fabs(g1 * (hm - qm)));
+  const double cl = sqrt(fabs(wl[3] / wl[0]));
+  const double cr = sqrt(fabs(wr[3] / wr[0]));
+  const double sl = fmin(wl[dir] - cl, vm[d1] - cm);
+  const double sr = fmax(wr[dir] + cr, vm[d1] + cm);
+  const double sm = (qr[dir] * (sr - wr[dir]) - ql[dir] * (sl - wl[dir]) + wl[3] - wr[3]) /
+                    (wr[0] * (sr - wr[dir]) - wl[0] * (sl - wl[dir]));
+  const double ps = wl[3] + wl[0] * (wl[dir] - sl) * (wl[dir] - sm);
+  if (sl > 0.0) {
+    flux(dir, ql, wl, F);
+  } else if (sl <= 0.0 && sm > 0.0) {
+    flux(dir, ql, wl, fl);
+    const double nom = sl - wl[dir], den = sl - sm;
+    qs[0] = wl[0] * nom / den;
+    qs[1] = dir == 1 ? (nom * ql[1] + ps - wl[3]) / den : nom * ql[1] / den;
+    qs[2] = dir == 2 ? (nom * ql[2] + ps - wl[3]) / den : nom * ql[2] / den;
+    qs[3] = (nom * ql[3] - wl[3] * wl[dir] + ps * sm) / den;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) F[k] = fl[k] + sl * (qs[k] - ql[k]);
+  } else if (sm <= 0.0 && sr >= 0.0) {
+    flux(dir, qr, wr, fr);
+    const double nom = sr - wr[dir], den = sr - sm;
+    qs[0] = wr[0] * nom / den;
+    qs[1] = dir == 1 ? (nom * qr[1] + ps - wr[3]) / den : nom * qr[1] / den;
+    qs[2] = dir == 2 ? (nom * qr[2] + ps - wr[3]) / den : nom * qr[2] / den;
+    qs[3] = (nom * qr[3] - wl[3] * wr[dir] + ps * sm) / den;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) F[k] = fr[k] + sr * (qs[k] - qr[k]);
+  } else {
+    flux(dir, qr, wr, F);
+  }
+}
+
+// characteristic Rusanov (:310-330) with maxLocalWaveSpeed (:221-246)
+__device__ __forceinline__ void rusanov(double g, double g1, int dir, const Eig& e,
+                                        const double* ql, const double* qr, double* F) {
+  double wl[4], wr[4], a[4], fl[4], fr[4], d[4], m[4], rm[4];
+  primitive(g1, ql, wl);
+  primitive(g1, qr, wr);
+  const double cl = sqrt(fabs(g * wl[3] / wl[0]));
+  const double cr = sqrt(fabs(g * wr[3] / wr[0]));
+  const double vl = wl[dir], vr = wr[dir];
+  a[0] = fmax(fabs(vl - cl), fabs(vr - cr));
+  a[1] = fmax(fabs(vl), fabs(vr));
+  a[2] = a[1];
+  a[3] = fmax(fabs(vl + cl), fabs(vr + cr));
+  flux(dir, ql, wl, fl);
+  flux(dir, qr, wr, fr);
+#pragma unroll
+  for (int k = 0; k < 4; ++k) d[k] = qr[k] - ql[k];
+  left(e, dir, d, m);
+#pragma unroll
+  for (int k = 0; k < 4; ++k) m[k] = a[k] * m[k];
+  right(e, dir, m, rm);
+#pragma unroll
+  for (int k = 0; k < 4; ++k) F[k] = 0.5 * (fl[k] + fr[k] - rm[k]);
+}
+
+// maxSpeed over both directions (Equations_Euler2D.cpp:207-219)
+__device__ __forceinline__ double max_speed2(double g, const double* w) {
+  const double c = sqrt(fabs(g * w[3] / w[0]));
+  return fmax(fmax(w[1] - c, fabs(w[1] + c)), fmax(w[2] - c, fabs(w[2] + c)));
+}
+
+// ---- Equations::Euler1D (Equations_Euler1D.cpp) --------------------------------------------
+
+__device__ __forceinline__ void primitive1(double g1, const double* q, double* w) {  // :18-23
+  w[0] = q[0];
+  w[1] = q[1] / q[0];
+  w[2] = (q[2] - 0.5 * q[1] * w[1]) * g1;
+}
+
+// eigen1DEuler (FV_System1D.cpp:121-156), eigenvectors :55-89 as full row-major 3x3 matrices
+__device__ __forceinline__ void eig1(double g1, double sra, double ua, double ha, double srb,
+                                     double ub, double hb, double* R, double* L) {
+  double t0 = sra / (sra + srb);
+  const double t1 = 1.0 - t0;
+  const double vxm = t0 * ua + t1 * ub;
+  const double hm = t0 * ha + t1 * hb;
+  const double qm = 0.5 * vxm * vxm;
+  const double cm = sqrt(fabs(g1 * (hm - qm)));
+  t0 = vxm * cm;
+  R[0] = 1.0; R[1] = 1.0; R[2] = 1.0;
+  R[3] = vxm - cm; R[4] = vxm; R[5] = vxm + cm;
+  R[6] = hm - t0; R[7] = qm; R[8] = hm + t0;
+  const double rcm = 1.0 / cm;
+  const double b1 = g1 * rcm * rcm;
+  const double b2 = qm * b1;
+  const double s0 = vxm * rcm;
+  const double s1 = b1 * vxm;
+  const double t2 = 0.5 * b1;
+  L[0] = 0.5 * (b2 + s0); L[1] = -0.5 * (s1 + rcm); L[2] = t2;
+  L[3] = 1.0 - b2; L[4] = s1; L[5] = -b1;
+  L[6] = 0.5 * (b2 - s0); L[7] = -0.5 * (s1 - rcm); L[8] = t2;
+}
+
+__device__ __forceinline__ void mv3(const double* M, const double* x, double* y) {
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    double s = M[3 * i] * x[0];
+    s = s + M[3 * i + 1] * x[1];
+    s = s + M[3 * i + 2] * x[2];
+    y[i] = s;
+  }
+}
+
+__device__ __forceinline__ void flux1(const double* q, const double* w, double* f) {
+  f[0] = q[1];
+  f[1] = q[1] * w[1] + w[2];
+  f[2] = w[1] * (q[2] + w[2]);
+}
+
+// Rusanov (Equations_Euler1D.cpp:129-135) with maxLocalWaveSpeed (:96-107)
+__device__ __forceinline__ void rusanov1(double g, double g1, const double* L, const double* R,
+                                         const double* ql, const double* qr, double* F) {
+  double wl[3], wr[3], a[3], fl[3], fr[3], d[3], m[3], rm[3];
+  primitive1(g1, ql, wl);
+  primitive1(g1, qr, wr);
+  const double cl = sqrt(fabs(g * wl[2] / wl[0]));
+  const double cr = sqrt(fabs(g * wr[2] / wr[0]));
+  a[0] = fmax(fabs(wl[1] - cl), fabs(wr[1] - cr));
+  a[1] = fmax(fabs(wl[1]), fabs(wr[1]));
+  a[2] = fmax(fabs(wl[1] + cl), fabs(wr[1] + cr));
+  flux1(ql, wl, fl);
+  flux1(qr, wr, fr);
+#pragma unroll
+  for (int k = 0; k < 3; ++k) d[k] = qr[k] - ql[k];
+  mv3(L, d, m);
+#pragma unroll
+  for (int k = 0; k < 3; ++k) m[k] = a[k] * m[k];
+  mv3(R, m, rm);
+#pragma unroll
+  for (int k = 0; k < 3; ++k) F[k] = 0.5 * (fl[k] + fr[k] - rm[k]);
+}
+
+// HLLC (Equations_Euler1D.cpp:156-210)
+__device__ __forceinline__ void hllc1(double g1, const double* ql, const double* qr, double* F) {
+  double wl[3], wr[3], fl[3], fr[3], qs[3];
+  primitive1(g1, ql, wl);
+  primitive1(g1, qr, wr);
+  const double hl = (ql[2] + wl[2]) / wl[0];
+  const double hr = (qr[2] + wr[2]) / wr[0];
+  const double rr = sqrt(fabs(wr[0] / wl[0]));
+  const double rrr = 1.0 / (1.0 + rr);
+  const double vm = (wl[1] + wr[1] * rr) * rrr;
+  const double qm = 0.5 * vm * vm;
+  const double hm = (hl + hr * rr) * rrr;
+  const double cm = sqrt(fabs(g1 * (hm - qm)));
+  const double cl = sqrt(fabs(wl[2] / wl[0]));
+  const double cr = sqrt(fabs(wr[2] / wr[0]));
+  const double sl = fmin(wl[1] - cl, vm - cm);
+  const double sr = fmax(wr[1] + cr, vm + cm);
+  const double sm = (qr[1] * (sr - wr[1]) - ql[1] * (sl - wl[1]) + wl[2] - wr[2]) /
+                    (wr[0] * (sr - wr[1]) - wl[0] * (sl - wl[1]));
+  const double ps = wl[2] + wl[0] * (wl[1] - sl) * (wl[1] - sm);
+  flux1(ql, wl, fl);
+  flux1(qr, wr, fr);
+  if (sl > 0.0) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) F[k] = fl[k];
+  } else if (sl <= 0.0 && sm > 0.0) {
+    const double nom = sl - wl[1], den = sl - sm;
+    qs[0] = wl[0] * nom / den;
+    qs[1] = (nom * ql[1] + ps - wl[2]) / den;
+    qs[2] = (nom * ql[2] - wl[2] * wl[1] + ps * sm) / den;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) F[k] = fl[k] + sl * (qs[k] - ql[k]);
+  } else if (sm <= 0.0 && sr >= 0.0) {
+    const double nom = sr - wr[1], den = sr - sm;
+    qs[0] = wr[0] * nom / den;
+    qs[1] = (nom * qr[1] + ps - wr[2]) / den;
+    qs[2] = (nom * qr[2] - wl[2] * wr[1] + ps * sm) / den;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) F[k] = fr[k] + sr * (qs[k] - qr[k]);
+  } else {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) F[k] = fr[k];
+  }
+}
+
+__device__ __forceinline__ double max_speed1(double g, const double* w) {  // :91-94
+  const double c = sqrt(fabs(g * w[2] / w[0]));
+  return fmax(fabs(w[1] - c), fabs(w[1] + c));
+}
+
+}  // namespace par
+}  // namespace hteno

@@ -1,10 +1,15 @@
 // Pointwise batch kernels: one reference function per entry point (see include/hteno.h).
-// They exist so that each building block of the fused solver kernels can be checked against the
-// oracle in isolation; the solver kernels call the same device functions.
+// They exist so that each building block of the solver kernels can be checked against the
+// oracle in isolation; the solver kernels call the same device functions: the bit-reproducible
+// ones (parity_math.cuh) in double, the fast ones (device_math.cuh) in float.  Compiled with
+// --fmad=false.
 #include <cstdio>
+
+#include <type_traits>
 
 #include "hermite_math.cuh"
 #include "hteno_internal.h"
+#include "parity_math.cuh"
 
 namespace hteno {
 namespace {
@@ -30,7 +35,8 @@ __global__ void k_lagrange(int kind, const double* __restrict__ u, double* __res
   T v[6];
   for (int m = 0; m < 6; ++m) v[m] = static_cast<T>(u[6 * k + m]);
   T a, b;
-  lagrange_recon(c_dev, kind, v, a, b);
+  if constexpr (std::is_same<T, double>::value) par::lagrange_recon(c_dev, kind, v, a, b);
+  else lagrange_recon(c_dev, kind, v, a, b);
   out[2 * k] = a;
   out[2 * k + 1] = b;
 }
@@ -42,7 +48,13 @@ __global__ void k_gl3(const double* __restrict__ u, double* __restrict__ out, lo
   T v[5];
   for (int m = 0; m < 5; ++m) v[m] = static_cast<T>(u[5 * k + m]);
   T a, b, c;
-  gl3(c_dev, v, a, b, c);
+  if constexpr (std::is_same<T, double>::value) {
+    double o[3];
+    par::gl3(c_dev, v, o);
+    a = o[0]; b = o[1]; c = o[2];
+  } else {
+    gl3(c_dev, v, a, b, c);
+  }
   out[3 * k] = a;
   out[3 * k + 1] = b;
   out[3 * k + 2] = c;
@@ -85,7 +97,8 @@ __global__ void k_hllc2(T g1, int dir, const double* __restrict__ ql, const doub
     a[m] = static_cast<T>(ql[4 * k + m]);
     b[m] = static_cast<T>(qr[4 * k + m]);
   }
-  hllc2(g1, dir, a, b, F);
+  if constexpr (std::is_same<T, double>::value) par::hllc(g1, dir, a, b, F);
+  else hllc2(g1, dir, a, b, F);
   for (int m = 0; m < 4; ++m) out[4 * k + m] = F[m];
 }
 
@@ -99,7 +112,8 @@ __global__ void k_hllc1(T g1, const double* __restrict__ ql, const double* __res
     a[m] = static_cast<T>(ql[3 * k + m]);
     b[m] = static_cast<T>(qr[3 * k + m]);
   }
-  hllc1(g1, a, b, F);
+  if constexpr (std::is_same<T, double>::value) par::hllc1(g1, a, b, F);
+  else hllc1(g1, a, b, F);
   for (int m = 0; m < 3; ++m) out[3 * k + m] = F[m];
 }
 
@@ -120,13 +134,22 @@ __global__ void k_rusanov2(T g, T g1, int dir, const double* __restrict__ qa,
                            const double* __restrict__ qr, double* __restrict__ out, long n) {
   long k = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (k >= n) return;
-  Roe2<T> s = roe_of_pair(g1, qa + 4 * k, qb + 4 * k);
   T a[4], b[4], F[4];
   for (int m = 0; m < 4; ++m) {
     a[m] = static_cast<T>(ql[4 * k + m]);
     b[m] = static_cast<T>(qr[4 * k + m]);
   }
-  rusanov2(g, g1, dir, s, a, b, F);
+  if constexpr (std::is_same<T, double>::value) {
+    double wa[4], wb[4];
+    par::primitive(g1, qa + 4 * k, wa);
+    par::primitive(g1, qb + 4 * k, wb);
+    const par::Eig E = par::eig(g1, dir, sqrt(fabs(wa[0])), wa[1], wa[2], (qa[4 * k + 3] + wa[3]) / wa[0],
+                                sqrt(fabs(wb[0])), wb[1], wb[2], (qb[4 * k + 3] + wb[3]) / wb[0]);
+    par::rusanov(g, g1, dir, E, a, b, F);
+  } else {
+    Roe2<T> s = roe_of_pair(g1, qa + 4 * k, qb + 4 * k);
+    rusanov2(g, g1, dir, s, a, b, F);
+  }
   for (int m = 0; m < 4; ++m) out[4 * k + m] = F[m];
 }
 

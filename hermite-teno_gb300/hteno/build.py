@@ -24,6 +24,8 @@ ORACLE_DIR = REPO_DIR / "oracle"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
               "-Xcompiler", "-ffp-contract=off", "--expt-relaxed-constexpr"]
+# Translation units holding the bit-reproducible FP64 path: no fused multiply-adds.
+NO_FMAD = {"fv2d_fp64.cu", "fv1d.cu", "pointwise.cu", "hermite2d_fp64.cu", "hermite1d.cu"}
 
 
 def _cuda_home() -> Path:
@@ -66,7 +68,8 @@ def build_library(force: bool = False, jobs: int | None = None, verbose: bool = 
         o = BUILD / (u.stem + ".o")
         objs.append(o)
         if force or _stale(o, [u] + headers):
-            jobs_todo.append([nvcc, *ARCH, *NVCC_FLAGS, "-I", str(REPO_DIR / "include"),
+            extra = ["--fmad=false"] if u.name in NO_FMAD else []
+            jobs_todo.append([nvcc, *ARCH, *NVCC_FLAGS, *extra, "-I", str(REPO_DIR / "include"),
                               "-c", str(u), "-o", str(o)])
     for u in host_units:
         o = BUILD / (u.stem + ".host.o")
