@@ -7,9 +7,13 @@
 // the limiter (:259-273) runs once per rhs over the padded range when any flag is set, updating
 // the moments in place (a Gauss-Seidel sweep that also limits the left ghost first).  Both are
 // one thread per conserved field walking the line; faces and updates are one thread per face /
-// cell.
+// cell.  In double the bit-reproducible functions (parity_math.cuh) are used; compiled with
+// --fmad=false.
+#include <type_traits>
+
 #include "hermite_math.cuh"
 #include "hteno_internal.h"
+#include "parity_math.cuh"
 
 namespace hteno {
 namespace {
@@ -25,7 +29,7 @@ constexpr int kS = 1;      // s (:25)
 
 struct GeoH1 {
   int nx, nxx;
-  double dx, area, gamma, g1;
+  double dx, area, gamma, g1, g3;  // g3 = gamma - 3 as the reference computes it
 };
 
 template <typename T>
@@ -81,7 +85,7 @@ __global__ void kh1_init(GeoH1 G, const double* __restrict__ q, StepState* st) {
   if (i < G.nx) {
     double qq[3] = {q[i], q[G.nx + i], q[2 * G.nx + i]}, w[3], h, sr;
     prim1(G.g1, qq, w, h, sr);
-    ms = max_speed1(G.gamma, w);
+    ms = par::max_speed1(G.gamma, w);
   }
   block_max_to(ms, &st->maxbits);
 }
@@ -129,7 +133,8 @@ __global__ void kh1_sensor(GeoH1 G, HermiteK<T> K, const double* __restrict__ q,
   for (int i = kGhost - 1; i < nxx - kGhost + 1; ++i) {
     T uu[3] = {T(u[wrap(i - 1, n)]), T(u[wrap(i, n)]), T(u[wrap(i + 1, n)])};
     T dd[3] = {T(vp[i - 1]), T(vp[i]), T(vp[i + 1])};
-    vp[i] = double(hermite_limiter(K, uu, dd));
+    if constexpr (std::is_same<T, double>::value) vp[i] = par::hermite_limiter(K, uu, dd);
+    else vp[i] = double(hermite_limiter(K, uu, dd));
   }
   for (int i = 0; i < n; ++i) v[size_t(e) * n + i] = vp[i + kGhost];
 }
@@ -151,31 +156,58 @@ __global__ void kh1_faces(GeoH1 G, HermiteK<T> K, const double* __restrict__ q,
   }
   prim1(G.g1, qa, wa, ha, sa);
   prim1(G.g1, qb, wb, hb, sb);
-  const Roe1<T> R = roe1<T>(T(G.g1), T(sa), T(wa[1]), T(ha), T(sb), T(wb[1]), T(hb));
-  T A[3][4], B[3][4];
-  for (int m = 0; m < 4; ++m) {
-    const int c = wrap(ip - 1 + m, n);
-    T a3[3] = {T(q[c]), T(q[n + c]), T(q[2 * n + c])};
-    T b3[3] = {T(v[c]), T(v[n + c]), T(v[2 * n + c])};
-    T ca3[3], cb3[3];
-    roe1_left(R, a3, ca3);
-    roe1_left(R, b3, cb3);
-    for (int r = 0; r < 3; ++r) {
-      A[r][m] = ca3[r];
-      B[r][m] = cb3[r];
-    }
-  }
-  T cl[4][3];
-  for (int r = 0; r < 3; ++r) {
-    T o[4];
-    hermite_recon(c_dev, K, W.flags[3 * ip + r] ? 1 : 2, A[r], B[r], o);
-    for (int a = 0; a < 4; ++a) cl[a][r] = o[a];
-  }
-  T X[4][3];
-  for (int a = 0; a < 4; ++a) roe1_right(R, cl[a], X[a]);
   T fu[3], fv[3];
-  rusanov1(T(G.gamma), T(G.g1), R, X[0], X[1], fu);
-  drusanov1(T(G.gamma), T(G.g1), R, X[0], X[1], X[2], X[3], fv);
+  if constexpr (std::is_same<T, double>::value) {
+    double R[9], L[9], A[3][4], B[3][4];
+    par::eig1(G.g1, sa, wa[1], ha, sb, wb[1], hb, R, L);
+    for (int m = 0; m < 4; ++m) {
+      const int c = wrap(ip - 1 + m, n);
+      const double a3[3] = {q[c], q[n + c], q[2 * n + c]};
+      const double b3[3] = {v[c], v[n + c], v[2 * n + c]};
+      double ca3[3], cb3[3];
+      par::mv3(L, a3, ca3);
+      par::mv3(L, b3, cb3);
+      for (int r = 0; r < 3; ++r) {
+        A[r][m] = ca3[r];
+        B[r][m] = cb3[r];
+      }
+    }
+    double cl[4][3];
+    for (int r = 0; r < 3; ++r) {
+      double o[4];
+      par::hermite_recon(c_dev, K, W.flags[3 * ip + r] ? 1 : 2, A[r], B[r], o);
+      for (int a = 0; a < 4; ++a) cl[a][r] = o[a];
+    }
+    double X[4][3];
+    for (int a = 0; a < 4; ++a) par::mv3(R, cl[a], X[a]);
+    par::rusanov1(G.gamma, G.g1, L, R, X[0], X[1], fu);
+    par::drusanov1(G.gamma, G.g1, G.g3, L, R, X[0], X[1], X[2], X[3], fv);
+  } else {
+    const Roe1<T> R = roe1<T>(T(G.g1), T(sa), T(wa[1]), T(ha), T(sb), T(wb[1]), T(hb));
+    T A[3][4], B[3][4];
+    for (int m = 0; m < 4; ++m) {
+      const int c = wrap(ip - 1 + m, n);
+      T a3[3] = {T(q[c]), T(q[n + c]), T(q[2 * n + c])};
+      T b3[3] = {T(v[c]), T(v[n + c]), T(v[2 * n + c])};
+      T ca3[3], cb3[3];
+      roe1_left(R, a3, ca3);
+      roe1_left(R, b3, cb3);
+      for (int r = 0; r < 3; ++r) {
+        A[r][m] = ca3[r];
+        B[r][m] = cb3[r];
+      }
+    }
+    T cl[4][3];
+    for (int r = 0; r < 3; ++r) {
+      T o[4];
+      hermite_recon(c_dev, K, W.flags[3 * ip + r] ? 1 : 2, A[r], B[r], o);
+      for (int a = 0; a < 4; ++a) cl[a][r] = o[a];
+    }
+    T X[4][3];
+    for (int a = 0; a < 4; ++a) roe1_right(R, cl[a], X[a]);
+    rusanov1(T(G.gamma), T(G.g1), R, X[0], X[1], fu);
+    drusanov1(T(G.gamma), T(G.g1), R, X[0], X[1], X[2], X[3], fv);
+  }
   for (int c = 0; c < 3; ++c) {
     W.Fu[c * (n + 1) + f] = fu[c];
     W.Fv[c * (n + 1) + f] = fv[c];
@@ -215,7 +247,7 @@ __global__ void kh1_update(GeoH1 G, int stage, WorkH1<T> W, double* __restrict__
     }
     double w[3], h, sr;
     prim1(G.g1, qn, w, h, sr);
-    if (stage == 3) ms = max_speed1(G.gamma, w);
+    if (stage == 3) ms = par::max_speed1(G.gamma, w);
     bad = (isnan(qn[0]) || isnan(qn[1]) || isnan(qn[2])) ? 1 : 0;
     bad |= (qn[0] <= 0.0 || w[2] <= 0.0) ? 2 : 0;
   }
@@ -231,6 +263,7 @@ GeoH1 geo_of(const hteno_solver* s) {
   G.area = s->dx;
   G.gamma = s->cfg.gamma;
   G.g1 = s->cfg.gamma - 1.0;
+  G.g3 = s->cfg.gamma - 3.0;
   return G;
 }
 

@@ -68,6 +68,7 @@ struct hteno_solver {
   hteno::StepState* hstate = nullptr;  // pinned host mirror
 
   int launches_per_step = 0;
+  bool strict = false;
   std::string err;
 
   // per-kernel event timing (hteno_enable_kernel_timing)

@@ -17,6 +17,7 @@
 #pragma once
 
 #include "device_math.cuh"
+#include "hermite_math.cuh"
 
 namespace hteno {
 namespace par {
@@ -458,6 +459,233 @@ __device__ __forceinline__ void hllc1(double g1, const double* ql, const double*
 __device__ __forceinline__ double max_speed1(double g, const double* w) {  // :91-94
   const double c = sqrt(fabs(g * w[2] / w[0]));
   return fmax(fabs(w[1] - c), fabs(w[1] + c));
+}
+
+// ---- Schemes::Hermite (Schemes_Hermite.cpp) -------------------------------------------------
+
+// smoothnessMeasure (:515-526)
+__device__ __forceinline__ void hermite_si(const double* u, const double* v, double* SI) {
+  double b[3], c[3];
+  b[0] = -2.0 * (u[0] - u[1]) - v[0];
+  c[0] = -2.0 * (u[0] - u[1] + v[0]);
+  b[1] = -2.0 * (u[1] - u[2]) - v[2];
+  c[1] = 2.0 * (u[1] - u[2]) + 2.0 * v[2];
+  b[2] = (-u[0] + u[2]) / 2.0;
+  c[2] = u[0] - 2.0 * u[1] + u[2];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) SI[k] = (13.0 / 12.0) * (c[k] * c[k]) + b[k] * b[k];
+}
+// smoothnessMeasureDerivative (:528-541)
+__device__ __forceinline__ void hermite_sid(const double* u, const double* d, double* SI) {
+  double b[3], c[3];
+  b[0] = 6.0 * (u[0] - u[1]) + (2.0 * d[0] + 4.0 * d[1]);
+  c[0] = 12.0 * (u[0] - u[1]) + 6.0 * (d[0] + d[1]);
+  b[1] = 6.0 * (u[2] - u[1]) - (4.0 * d[1] + 2.0 * d[2]);
+  c[1] = 12.0 * (u[1] - u[2]) + 6.0 * (d[1] + d[2]);
+  b[2] = u[0] - 2.0 * u[1] + u[2];
+  c[2] = 3.0 * (u[2] - u[0]) - 6.0 * d[1];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) SI[k] = (13.0 / 12.0) * (c[k] * c[k]) + b[k] * b[k];
+}
+// fullPointsSI (:597-603)
+__device__ __forceinline__ double hermite_brk(const double* u, const double* d) {
+  return fabs((1029270.0 * u[2] - 2129184.0 * u[1] + 1099914.0 * u[0] + 281121.0 * d[0] -
+               494958.0 * d[2]) * d[0] +
+              (-1029270.0 * u[0] + 2129184.0 * u[1] - 1099914.0 * u[2] + 281121.0 * d[2]) * d[2] +
+              (1099445.0 * u[2] - 4317056.0 * u[1] + 2118166.0 * u[0]) * u[2] +
+              4317056.0 * (u[1] - u[0]) * u[1] + 1099445.0 * u[0] * u[0]) /
+         6720.0;
+}
+// fullPointsSId (:605-612)
+__device__ __forceinline__ double hermite_brkd(const double* u, const double* d) {
+  return fabs((3156862.0 * d[2] + 13189240.0 * d[1] + 1710479.0 * d[0] - 9617754.0 * u[2] -
+               531552.0 * u[1] + 10149306.0 * u[0]) * d[0] +
+              (13189240.0 * d[2] + 26511200.0 * d[1] - 39700440.0 * u[2] + 39700440.0 * u[0]) * d[1] +
+              (1710479.0 * d[2] - 10149306.0 * u[2] + 531552.0 * u[1] + 9617754.0 * u[0]) * d[2] +
+              (15136011.0 * u[2] - 1076544.0 * u[1] - 29195478.0 * u[0]) * u[2] +
+              1076544.0 * (u[1] - u[0]) * u[1] + 15136011.0 * u[0] * u[0]) /
+         1680.0;
+}
+__device__ __forceinline__ double maxof3(const double* s) {
+  double t = s[0];
+  t = (t < s[1]) ? s[1] : t;
+  t = (t < s[2]) ? s[2] : t;
+  return t;
+}
+// one hteno/htenoi output: cut-off (cutOff/cutOffd, :614-628) and the table weights
+__device__ __forceinline__ double hermite_weighted(const DevConst& C, int which, const double* p,
+                                                   const double* SI, double tau) {
+  const int pat = cutoff_pattern(SI, tau, 1e-40, 1e-3);
+  const double* w = which == 0 ? C.hwtab_m[pat] : which == 1 ? C.hwtab_p[pat]
+                  : which == 2 ? C.hwtab_md[pat] : C.hwtab_pd[pat];
+  return catchnan(dot3v(p, w));
+}
+
+// kind 0 hteno (:295-379), 1 htenoi (:670-758), 2 linear (:760-812);
+// out = {u^-, u^+, d^-, d^+} at x_{i+1/2}
+__device__ __forceinline__ void hermite_recon(const DevConst& C, const HermiteK<double>& K,
+                                              int kind, const double* u, const double* d,
+                                              double* out) {
+  if (kind == 2) {
+    out[0] = dot3(K.crjlin[0][0], K.crjlin[1][0], K.crjlin[2][0], u) + K.crjlin[3][0] * d[0] +
+             K.crjlin[4][0] * d[2];
+    out[1] = dot3(K.crjlin[0][1], K.crjlin[1][1], K.crjlin[2][1], u + 1) + K.crjlin[3][1] * d[1] +
+             K.crjlin[4][1] * d[3];
+    out[2] = dot3(K.crjlind[0][0], K.crjlind[1][0], K.crjlind[2][0], u) +
+             dot3(K.crjlind[3][0], K.crjlind[4][0], K.crjlind[5][0], d);
+    out[3] = dot3(K.crjlind[0][1], K.crjlind[1][1], K.crjlind[2][1], u + 1) +
+             dot3(K.crjlind[3][1], K.crjlind[4][1], K.crjlind[5][1], d + 1);
+    return;
+  }
+  const bool imp = kind == 1;
+  double ud[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) ud[k] = d[k] * K.dif;
+  double p[3], SI[3], tau;
+  p[0] = K.crj[0][0] * u[0] + K.crj[1][0] * u[1] + K.crj[2][0] * d[0];
+  p[1] = K.crj[0][1] * u[1] + K.crj[1][1] * u[2] + K.crj[2][1] * d[2];
+  p[2] = K.crj[0][2] * u[0] + K.crj[1][2] * u[1] + K.crj[2][2] * u[2];
+  hermite_si(u, ud, SI);
+  tau = imp ? maxof3(SI) : fabs(hermite_brk(u, ud) - 0.25 * (SI[0] + SI[1] + 2.0 * SI[2]));
+  out[0] = hermite_weighted(C, 0, p, SI, tau);
+
+  p[0] = K.crjd[0][0] * u[0] + K.crjd[1][0] * u[1] + K.crjd[2][0] * d[0] + K.crjd[3][0] * d[1];
+  p[1] = K.crjd[0][1] * u[1] + K.crjd[1][1] * u[2] + K.crjd[2][1] * d[1] + K.crjd[3][1] * d[2];
+  p[2] = K.crjd[0][2] * u[0] + K.crjd[1][2] * u[1] + K.crjd[2][2] * u[2] + K.crjd[3][2] * d[1];
+  hermite_sid(u, ud, SI);
+  tau = imp ? maxof3(SI) : fabs(hermite_brkd(u, ud) - 0.25 * (SI[0] + SI[1] + 2.0 * SI[2]));
+  out[2] = hermite_weighted(C, 2, p, SI, tau);
+
+  p[0] = K.crj[1][1] * u[1] + K.crj[0][1] * u[2] - K.crj[2][1] * d[1];
+  p[1] = K.crj[1][0] * u[2] + K.crj[0][0] * u[3] - K.crj[2][0] * d[3];
+  p[2] = K.crj[2][2] * u[1] + K.crj[1][2] * u[2] + K.crj[0][2] * u[3];
+  hermite_si(u + 1, ud + 1, SI);
+  tau = imp ? maxof3(SI) : fabs(hermite_brk(u + 1, ud + 1) - 0.25 * (SI[0] + SI[1] + 2.0 * SI[2]));
+  out[1] = hermite_weighted(C, 1, p, SI, tau);
+
+  p[0] = K.crjd[0][1] * u[1] + K.crjd[1][1] * u[2] + K.crjd[3][1] * d[1] + K.crjd[2][1] * d[2];
+  p[1] = K.crjd[0][0] * u[2] + K.crjd[1][0] * u[3] + K.crjd[3][0] * d[2] + K.crjd[2][0] * d[3];
+  p[2] = -(K.crjd[2][2] * u[1] + K.crjd[1][2] * u[2] + K.crjd[0][2] * u[3]) + K.crjd[3][2] * d[2];
+  hermite_sid(u + 1, ud + 1, SI);
+  tau = imp ? maxof3(SI) : fabs(hermite_brkd(u + 1, ud + 1) - 0.25 * (SI[0] + SI[1] + 2.0 * SI[2]));
+  out[3] = hermite_weighted(C, 3, p, SI, tau);
+}
+
+// hermiteLimiter (Schemes_Hermite.cpp:634-662)
+__device__ __forceinline__ double hermite_limiter(const HermiteK<double>& K, const double* u,
+                                                  const double* d) {
+  double p[3];
+  p[0] = 0.75 * (u[2] - u[0]) / K.dif - 0.25 * (d[0] + d[2]);
+  p[1] = (u[1] - u[0]) / K.dif;
+  p[2] = (u[2] - u[1]) / K.dif;
+  const double lw[3] = {1.0 - 2E-5, 1E-5, 1E-5};
+  const double ud[3] = {d[0] * K.dif, d[1] * K.dif, d[2] * K.dif};
+  double sm[3];
+  sm[0] = hermite_brk(u, ud);
+  sm[1] = (u[0] - u[1]) * (u[0] - u[1]);
+  sm[2] = (u[1] - u[2]) * (u[1] - u[2]);
+  const double ta = fabs(sm[0] - sm[1]) + fabs(sm[0] - sm[2]);
+  const double tau = ta * ta / 4.0;
+  double w[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) w[k] = lw[k] * (1.0 + tau / (sm[k] + 1e-6));
+  const double s = (w[0] + w[1]) + w[2];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) w[k] = w[k] / s;
+  const double r1 = lw[1] / lw[0], r2 = lw[2] / lw[0];
+  double inner = r1 * p[1];
+  inner = inner + r2 * p[2];
+  double w12 = w[1] * p[1];
+  w12 = w12 + w[2] * p[2];
+  return w[0] * (p[0] / lw[0] - inner) + w12;
+}
+
+// A(q) * x with the Jacobians dfluxx / dfluxy (Equations_Euler2D.cpp:52-98), row sums left to
+// right; zero and unit entries as in the reference's matrices.
+__device__ __forceinline__ void dflux_apply(double g, double g1, double g3, int dir, const double* q,
+                                            const double* w, const double* x, double* y) {
+  if (dir == 1) {
+    const double sv = w[1] * w[1];
+    const double dv = 0.5 * g1 * (sv + w[2] * w[2]);
+    const double h = (q[3] + w[3]) / w[0];
+    y[0] = x[1];
+    double s = (dv - sv) * x[0]; s = s + (-g3 * w[1]) * x[1]; s = s + (-g1 * w[2]) * x[2]; s = s + g1 * x[3]; y[1] = s;
+    s = (-w[1] * w[2]) * x[0]; s = s + w[2] * x[1]; s = s + w[1] * x[2]; y[2] = s;
+    s = ((dv - h) * w[1]) * x[0]; s = s + (h - g1 * sv) * x[1]; s = s + (-g1 * w[1] * w[2]) * x[2];
+    s = s + (g * w[1]) * x[3]; y[3] = s;
+  } else {
+    const double sv = w[2] * w[2];
+    const double dv = 0.5 * g1 * (sv + w[1] * w[1]);
+    const double h = (q[3] + w[3]) / w[0];
+    y[0] = x[2];
+    double s = (-w[1] * w[2]) * x[0]; s = s + w[2] * x[1]; s = s + w[1] * x[2]; y[1] = s;
+    s = (dv - sv) * x[0]; s = s + (-g1 * w[1]) * x[1]; s = s + (-g3 * w[2]) * x[2]; s = s + g1 * x[3]; y[2] = s;
+    s = ((dv - h) * w[2]) * x[0]; s = s + (-g1 * w[1] * w[2]) * x[1]; s = s + (h - g1 * sv) * x[2];
+    s = s + (g * w[2]) * x[3]; y[3] = s;
+  }
+}
+
+// dRusanov (Equations_Euler2D.cpp:352-360) as called in FVHermite_System2D.cpp:553-589
+__device__ __forceinline__ void drusanov(double g, double g1, double g3, int dir, const Eig& e,
+                                         const double* ql, const double* qr, const double* dql,
+                                         const double* dqr, double* F) {
+  double wl[4], wr[4], a[4], d[4], m[4], al[4], ar[4], rm[4];
+  primitive(g1, ql, wl);
+  primitive(g1, qr, wr);
+  dflux_apply(g, g1, g3, dir, ql, wl, dql, al);
+  dflux_apply(g, g1, g3, dir, qr, wr, dqr, ar);
+  const double cl = sqrt(fabs(g * wl[3] / wl[0]));
+  const double cr = sqrt(fabs(g * wr[3] / wr[0]));
+  const double vl = wl[dir], vr = wr[dir];
+  a[0] = fmax(fabs(vl - cl), fabs(vr - cr));
+  a[1] = fmax(fabs(vl), fabs(vr));
+  a[2] = a[1];
+  a[3] = fmax(fabs(vl + cl), fabs(vr + cr));
+#pragma unroll
+  for (int k = 0; k < 4; ++k) d[k] = dqr[k] - dql[k];
+  left(e, dir, d, m);
+#pragma unroll
+  for (int k = 0; k < 4; ++k) m[k] = a[k] * m[k];
+  right(e, dir, m, rm);
+#pragma unroll
+  for (int k = 0; k < 4; ++k) F[k] = 0.5 * (al[k] + ar[k] - rm[k]);
+}
+
+// dflux 1D (Equations_Euler1D.cpp:39-53) applied to x; dRusanov 1D (:212-220)
+__device__ __forceinline__ void drusanov1(double g, double g1, double g3, const double* L,
+                                          const double* R, const double* ql, const double* qr,
+                                          const double* dql, const double* dqr, double* F) {
+  double wl[3], wr[3], a[3], d[3], m[3], rm[3], al[3], ar[3];
+  primitive1(g1, ql, wl);
+  primitive1(g1, qr, wr);
+  auto apply = [&](const double* q, const double* w, const double* x, double* y) {
+    double A[9];
+    A[0] = 0.0; A[1] = 1.0; A[2] = 0.0;
+    A[3] = 0.5 * g3 * w[1] * w[1];
+    A[4] = -g3 * w[1];
+    A[5] = g1;
+    A[6] = (g1 * (w[1] * w[1]) - g * q[2] / w[0]) * w[1];
+    A[7] = g * q[2] / w[0] - 1.5 * g1 * w[1] * w[1];
+    A[8] = g * w[1];
+    y[0] = x[1];
+    double s = A[3] * x[0]; s = s + A[4] * x[1]; s = s + A[5] * x[2]; y[1] = s;
+    s = A[6] * x[0]; s = s + A[7] * x[1]; s = s + A[8] * x[2]; y[2] = s;
+  };
+  apply(ql, wl, dql, al);
+  apply(qr, wr, dqr, ar);
+  const double cl = sqrt(fabs(g * wl[2] / wl[0]));
+  const double cr = sqrt(fabs(g * wr[2] / wr[0]));
+  a[0] = fmax(fabs(wl[1] - cl), fabs(wr[1] - cr));
+  a[1] = fmax(fabs(wl[1]), fabs(wr[1]));
+  a[2] = fmax(fabs(wl[1] + cl), fabs(wr[1] + cr));
+#pragma unroll
+  for (int k = 0; k < 3; ++k) d[k] = dqr[k] - dql[k];
+  mv3(L, d, m);
+#pragma unroll
+  for (int k = 0; k < 3; ++k) m[k] = a[k] * m[k];
+  mv3(R, m, rm);
+#pragma unroll
+  for (int k = 0; k < 3; ++k) F[k] = 0.5 * (al[k] + ar[k] - rm[k]);
 }
 
 }  // namespace par

@@ -70,7 +70,8 @@ __global__ void k_hermite(int kind, HermiteK<T> K, const double* __restrict__ u,
     uu[m] = static_cast<T>(u[4 * k + m]);
     dd[m] = static_cast<T>(d[4 * k + m]);
   }
-  hermite_recon(c_dev, K, kind, uu, dd, o);
+  if constexpr (std::is_same<T, double>::value) par::hermite_recon(c_dev, K, kind, uu, dd, o);
+  else hermite_recon(c_dev, K, kind, uu, dd, o);
   for (int m = 0; m < 4; ++m) out[4 * k + m] = o[m];
 }
 
@@ -84,7 +85,8 @@ __global__ void k_hlimiter(HermiteK<T> K, const double* __restrict__ u, const do
     uu[m] = static_cast<T>(u[3 * k + m]);
     dd[m] = static_cast<T>(d[3 * k + m]);
   }
-  out[k] = hermite_limiter(K, uu, dd);
+  if constexpr (std::is_same<T, double>::value) out[k] = par::hermite_limiter(K, uu, dd);
+  else out[k] = hermite_limiter(K, uu, dd);
 }
 
 template <typename T>
@@ -154,13 +156,12 @@ __global__ void k_rusanov2(T g, T g1, int dir, const double* __restrict__ qa,
 }
 
 template <typename T>
-__global__ void k_drusanov2(T g, T g1, int dir, const double* __restrict__ qa,
+__global__ void k_drusanov2(T g, T g1, T g3, int dir, const double* __restrict__ qa,
                             const double* __restrict__ qb, const double* __restrict__ ql,
                             const double* __restrict__ qr, const double* __restrict__ dql,
                             const double* __restrict__ dqr, double* __restrict__ out, long n) {
   long k = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (k >= n) return;
-  Roe2<T> s = roe_of_pair(g1, qa + 4 * k, qb + 4 * k);
   T a[4], b[4], da[4], db[4], F[4];
   for (int m = 0; m < 4; ++m) {
     a[m] = static_cast<T>(ql[4 * k + m]);
@@ -168,7 +169,17 @@ __global__ void k_drusanov2(T g, T g1, int dir, const double* __restrict__ qa,
     da[m] = static_cast<T>(dql[4 * k + m]);
     db[m] = static_cast<T>(dqr[4 * k + m]);
   }
-  drusanov2(g, g1, dir, s, a, b, da, db, F);
+  if constexpr (std::is_same<T, double>::value) {
+    double wa[4], wb[4];
+    par::primitive(g1, qa + 4 * k, wa);
+    par::primitive(g1, qb + 4 * k, wb);
+    const par::Eig E = par::eig(g1, dir, sqrt(fabs(wa[0])), wa[1], wa[2], (qa[4 * k + 3] + wa[3]) / wa[0],
+                                sqrt(fabs(wb[0])), wb[1], wb[2], (qb[4 * k + 3] + wb[3]) / wb[0]);
+    par::drusanov(g, g1, g3, dir, E, a, b, da, db, F);
+  } else {
+    Roe2<T> s = roe_of_pair(g1, qa + 4 * k, qb + 4 * k);
+    drusanov2(g, g1, dir, s, a, b, da, db, F);
+  }
   for (int m = 0; m < 4; ++m) out[4 * k + m] = F[m];
 }
 
@@ -286,11 +297,12 @@ int hteno_drusanov2d_batch(int precision, double gamma, int dir, const double* q
   cudaStream_t st;
   if (prep(stream, &st)) return HTENO_ERR_CUDA;
   if (precision == HTENO_PREC_MIXED)
-    k_drusanov2<float><<<grid_for(n, 256), 256, 0, st>>>(float(gamma), float(gamma - 1.0), dir, qa,
-                                                          qb, ql, qr, dql, dqr, out, n);
+    k_drusanov2<float><<<grid_for(n, 256), 256, 0, st>>>(float(gamma), float(gamma - 1.0),
+                                                          float(gamma - 3.0), dir, qa, qb, ql, qr,
+                                                          dql, dqr, out, n);
   else
-    k_drusanov2<double><<<grid_for(n, 256), 256, 0, st>>>(gamma, gamma - 1.0, dir, qa, qb, ql, qr,
-                                                           dql, dqr, out, n);
+    k_drusanov2<double><<<grid_for(n, 256), 256, 0, st>>>(gamma, gamma - 1.0, gamma - 3.0, dir, qa,
+                                                           qb, ql, qr, dql, dqr, out, n);
   return finish();
 }
 

@@ -298,8 +298,9 @@ int hteno_sync(hteno_solver* s) {
                                   s->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
   if (e != cudaSuccess) return cuda_error(s, e, "sync");
-  if (s->hstate->status & 1) return set_error(s, HTENO_ERR_NAN, "NaN in the conserved state");
-  if (s->hstate->status & 2)
+  if (s->strict && (s->hstate->status & 1))
+    return set_error(s, HTENO_ERR_NAN, "NaN in the conserved state");
+  if (s->strict && (s->hstate->status & 2))
     return set_error(s, HTENO_ERR_NONPHYSICAL, "non-positive density or pressure in the state");
   return HTENO_OK;
 }
@@ -319,6 +320,22 @@ int hteno_get_time(hteno_solver* s, double* t, long* steps, double* last_dt) {
   if (t) *t = s->hstate->t;
   if (steps) *steps = static_cast<long>(s->hstate->steps);
   if (last_dt) *last_dt = s->hstate->dt;
+  return HTENO_OK;
+}
+
+int hteno_get_status(hteno_solver* s, int* flags) {
+  if (!s || !flags) return HTENO_ERR_INVALID_ARG;
+  cudaError_t e = cudaMemcpyAsync(s->hstate, s->dstate, sizeof(StepState), cudaMemcpyDeviceToHost,
+                                  s->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+  if (e != cudaSuccess) return cuda_error(s, e, "get_status");
+  *flags = s->hstate->status;
+  return HTENO_OK;
+}
+
+int hteno_set_strict(hteno_solver* s, int on) {
+  if (!s) return HTENO_ERR_INVALID_ARG;
+  s->strict = on != 0;
   return HTENO_OK;
 }
 

@@ -92,6 +92,8 @@ def lib() -> ctypes.CDLL:
         L.hteno_enable_kernel_timing.argtypes = [vp, i]
         L.hteno_kernel_timing.argtypes = [vp, ctypes.POINTER(KernelTime), i, ctypes.POINTER(i)]
         L.hteno_measure_fma_peak.argtypes = [i, _D]
+        L.hteno_get_status.argtypes = [vp, ctypes.POINTER(i)]
+        L.hteno_set_strict.argtypes = [vp, i]
         _lib = L
     return _lib
 
@@ -185,6 +187,15 @@ class Solver:
         t, n, dt = ctypes.c_double(), ctypes.c_long(), ctypes.c_double()
         _check(lib().hteno_get_time(self.h, ctypes.byref(t), ctypes.byref(n), ctypes.byref(dt)), self.h)
         return t.value, n.value, dt.value
+
+    def status(self) -> int:
+        """Sticky health flags: bit 0 NaN seen, bit 1 non-positive density/pressure seen."""
+        f = ctypes.c_int()
+        _check(lib().hteno_get_status(self.h, ctypes.byref(f)), self.h)
+        return f.value
+
+    def set_strict(self, on: bool = True) -> None:
+        _check(lib().hteno_set_strict(self.h, int(bool(on))), self.h)
 
     def launches_per_step(self) -> int:
         n = ctypes.c_int()

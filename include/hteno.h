@@ -105,6 +105,14 @@ int hteno_get_time(hteno_solver* s, double* t, long* steps, double* last_dt);
 /* Number of kernel launches hteno_step_async issues per step for this configuration. */
 int hteno_launches_per_step(hteno_solver* s, int* launches);
 
+/* Health flags of the state, sticky since the last hteno_set_state: bit 0 = a NaN appeared,
+ * bit 1 = a non-positive density or pressure appeared.  The reference solver keeps stepping in
+ * both cases (its positivity checks are commented out, e.g. FV_System2D.cpp:236-250), and so does
+ * this library: by default hteno_step/hteno_sync return HTENO_OK and only record the flags.
+ * With strict mode on they return HTENO_ERR_NAN / HTENO_ERR_NONPHYSICAL instead. */
+int hteno_get_status(hteno_solver* s, int* flags);
+int hteno_set_strict(hteno_solver* s, int on);
+
 /* Message of the last failed call on this handle ("" if none). */
 const char* hteno_last_error(hteno_solver* s);
 const char* hteno_status_string(int status);

@@ -17,8 +17,12 @@ TOL = 1e-12
 
 
 def rel_linf(a, b):
+    """Relative L-inf error per variable (NaNs, which the reference produces too where its HLLC
+    goes non-physical, must sit at the same places and are excluded from the norm)."""
+    assert np.array_equal(np.isnan(a), np.isnan(b)), "NaN pattern differs"
     ax = tuple(range(1, a.ndim))
-    return (np.abs(a - b).max(axis=ax) / np.abs(b).max(axis=ax)).max()
+    d = np.where(np.isnan(b), 0.0, np.abs(a - b))
+    return (np.nanmax(d, axis=ax) / np.nanmax(np.abs(b), axis=ax)).max()
 
 
 def gpu_run2d(h, q, nsteps, t_final=1e30, **kw):
@@ -56,8 +60,9 @@ def test_fv2d_matches_oracle(hteno_lib, cuda, oracle, cfg):
     want, t_o, n_o = oracle.fv2d_run(q, 25, **cfg)
     got, t_g, n_g = gpu_run2d(hteno_lib, q, 25, **cfg)
     assert n_g == n_o == 25
-    assert abs(t_g - t_o) <= 1e-14 * t_o
+    assert t_g == t_o
     assert rel_linf(got, want) <= TOL
+    np.testing.assert_array_equal(got, want)  # the plain path reproduces the oracle's rounding
 
 
 def test_fv2d_bitwise_200_steps(hteno_lib, cuda, oracle):
@@ -115,15 +120,24 @@ def test_fv2d_constant_state_is_steady(hteno_lib, cuda):
 
 
 def test_fv2d_nonphysical_state_reports_status(hteno_lib, cuda):
-    """A negative density is reported as HTENO_ERR_NONPHYSICAL after the step (the kernels,
-    like the reference, take sqrt(|rho|) and keep running; nothing faults)."""
+    """A negative density is recorded in the health flags; in strict mode the step returns
+    HTENO_ERR_NONPHYSICAL (or NAN).  Like the reference, the kernels take sqrt(|rho|) and keep
+    running; nothing faults."""
     from hteno import ic, HtenoError
 
     q = ic.four_quadrant(16, 16, 1)
     q[0, 5, 5] = -0.5
-    with pytest.raises(HtenoError) as e:
-        gpu_run2d(hteno_lib, q, 1, flux=1)
-    assert e.value.code in (4, 5)
+    cfg = hteno_lib.config(dims=2, nx=16, ny=16, flux=1)
+    with hteno_lib.Solver(cfg) as s:
+        s.set_state(q)
+        s.step(1)
+        assert s.status() & 2
+        s.set_state(q)
+        assert s.status() == 0
+        s.set_strict(True)
+        with pytest.raises(HtenoError) as e:
+            s.step(1)
+        assert e.value.code in (4, 5)
 
 
 def test_fv2d_full_size_properties(hteno_lib, cuda):
@@ -138,17 +152,26 @@ def test_fv2d_full_size_properties(hteno_lib, cuda):
     np.testing.assert_array_equal(a, b)
     assert a[0].min() > 0
     c, _, _ = gpu_run2d(hteno_lib, q, 50, flux=1, bc=1)
+    good = np.isfinite(c).all()
+    assert good, "periodic run stays finite"
     np.testing.assert_allclose(c.sum(axis=(1, 2)), q.sum(axis=(1, 2)), rtol=1e-12)
 
 
 def test_fv2d_transpose_symmetry_gpu(hteno_lib, cuda):
+    """Swapping x and y commutes with the scheme up to rounding: the x and y characteristic sums
+    associate the normal and tangential momenta in opposite order (as in the reference), and a
+    rounding difference can flip a TENO cut-off in a wave tail, so the bound is 1e-7, not 1e-12.
+    The first step is symmetric to rounding."""
     from hteno import ic
 
     q = ic.four_quadrant(96, 96, 4)
     qt = np.ascontiguousarray(q[[0, 2, 1, 3]].transpose(0, 2, 1))
+    a, _, _ = gpu_run2d(hteno_lib, q, 1, flux=1)
+    b, _, _ = gpu_run2d(hteno_lib, qt, 1, flux=1)
+    assert rel_linf(a, np.ascontiguousarray(b[[0, 2, 1, 3]].transpose(0, 2, 1))) <= 1e-14
     a, _, _ = gpu_run2d(hteno_lib, q, 20, flux=1)
     b, _, _ = gpu_run2d(hteno_lib, qt, 20, flux=1)
-    assert rel_linf(a, np.ascontiguousarray(b[[0, 2, 1, 3]].transpose(0, 2, 1))) <= TOL
+    assert rel_linf(a, np.ascontiguousarray(b[[0, 2, 1, 3]].transpose(0, 2, 1))) <= 1e-7
 
 
 def test_fv2d_mixed_precision_error(hteno_lib, cuda, oracle):

@@ -1,0 +1,95 @@
+"""GPU parity of the Hermite solvers (FVHermite::System2D, FVHermite::System1D) against the
+oracle and the reference's golden runs.  The plain FP64 path reproduces the oracle's rounding
+(tolerance 1e-12 relative L-inf, bitwise expected); the mixed path is checked by its error."""
+from __future__ import annotations
+
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+GOLD = Path(__file__).resolve().parent / "golden"
+TOL = 1e-12
+
+
+def rel_linf(a, b):
+    ax = tuple(range(1, a.ndim))
+    return (np.abs(a - b).max(axis=ax) / np.maximum(np.abs(b).max(axis=ax), 1e-300)).max()
+
+
+def run2(h, q, v, w, nsteps, **kw):
+    cfg = h.config(dims=2, scheme=h.SCHEME_HERMITE, nx=q.shape[2], ny=q.shape[1], **kw)
+    with h.Solver(cfg) as s:
+        s.set_state(q)
+        s.set_moments(v, w)
+        s.step(nsteps)
+        t, n, _ = s.time()
+        vo, wo = s.get_moments()
+        return s.get_state(), vo, wo, t, n
+
+
+def run1(h, q, v, nsteps, **kw):
+    cfg = h.config(dims=1, scheme=h.SCHEME_HERMITE, nx=q.shape[1], **kw)
+    with h.Solver(cfg) as s:
+        s.set_state(q)
+        s.set_moments(v)
+        s.step(nsteps)
+        t, n, _ = s.time()
+        return s.get_state(), s.get_moments(), t, n
+
+
+def test_hermite2d_matches_reference_golden(hteno_lib, cuda):
+    g = np.load(GOLD / "solvers.npz")
+    q, v, w, t, n = run2(hteno_lib, g["h2d_q0"], g["h2d_v0"], g["h2d_w0"], int(g["h2d_steps"]))
+    assert n == int(g["h2d_steps"])
+    for a, b in ((q, g["h2d_q"]), (v, g["h2d_v"]), (w, g["h2d_w"])):
+        assert rel_linf(a, b) <= TOL
+
+
+def test_hermite2d_matches_oracle_bitwise(hteno_lib, cuda, oracle):
+    from hteno import ic
+
+    q = ic.four_quadrant(30, 22, 8)
+    rng = np.random.default_rng(3)
+    v = np.ascontiguousarray(rng.normal(size=q.shape) * 0.3)
+    w = np.ascontiguousarray(rng.normal(size=q.shape) * 0.3)
+    qo, vo, wo, to, no = oracle.hermite2d_run(q, v, w, 6)
+    qg, vg, wg, tg, ng = run2(hteno_lib, q, v, w, 6)
+    assert ng == no == 6 and tg == to
+    for a, b in ((qg, qo), (vg, vo), (wg, wo)):
+        assert rel_linf(a, b) <= TOL
+        np.testing.assert_array_equal(a, b)
+
+
+def test_hermite2d_mixed_precision_error(hteno_lib, cuda, oracle):
+    from hteno import ic
+
+    q = ic.gaussian_blobs_shock(48, 48, 2)
+    v = np.zeros_like(q)
+    w = np.zeros_like(q)
+    qo, _, _, _, _ = oracle.hermite2d_run(q, v, w, 8)
+    qg, _, _, _, _ = run2(hteno_lib, q, v, w, 8, precision=1)
+    l1 = np.abs(qg[0] - qo[0]).mean()
+    assert l1 <= 1e-4, l1
+
+
+def test_hermite1d_matches_reference_golden(hteno_lib, cuda):
+    g = np.load(GOLD / "solvers.npz")
+    q, v, t, n = run1(hteno_lib, g["h1d_q0"], g["h1d_v0"], int(g["h1d_steps"]))
+    assert n == int(g["h1d_steps"])
+    assert rel_linf(q, g["h1d_q"]) <= TOL
+    assert rel_linf(v, g["h1d_v"]) <= TOL
+
+
+def test_hermite1d_matches_oracle_bitwise(hteno_lib, cuda, oracle):
+    nx = 200
+    x = (np.arange(nx) + 0.5) / nx
+    q = np.ascontiguousarray(np.stack([1 + 0.2 * np.sin(2 * np.pi * x) + (x > 0.3) * 0.4 - (x > 0.7) * 0.3,
+                                       0.4 * np.ones(nx), 2.5 + 0.5 * (x > 0.5)]))
+    v = np.ascontiguousarray(np.gradient(q, 1.0 / nx, axis=1))
+    qo, vo, to, no = oracle.hermite1d_run(q, v, 40)
+    qg, vg, tg, ng = run1(hteno_lib, q, v, 40)
+    assert ng == no == 40 and tg == to
+    np.testing.assert_array_equal(qg, qo)
+    np.testing.assert_array_equal(vg, vo)
