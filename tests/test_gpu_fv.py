@@ -102,15 +102,30 @@ def test_fv2d_residual_matches_oracle(hteno_lib, cuda, oracle):
 
 
 def test_fv2d_edge_sizes_and_time_clipping(hteno_lib, cuda, oracle):
+    """Smallest accepted grid and non-square grids, stopping on t_final mid-run, with both fluxes.
+    The reference's HLLC (sound speeds without gamma) drives the 64 x 9 case to negative pressure
+    at step 10 and to NaN later; past that point neither side's numbers mean anything, so that
+    case is compared bit for bit over its first 9 steps and the GPU must flag it."""
     from hteno import ic
 
-    # smallest accepted grid, non-square, stop on t_final mid-run
-    for nx, ny in ((6, 6), (7, 13), (64, 9)):
-        q = ic.four_quadrant(nx, ny, nx * 100 + ny)
-        want, t_o, n_o = oracle.fv2d_run(q, 1000, t_final=0.05, flux=1)
-        got, t_g, n_g = gpu_run2d(hteno_lib, q, 1000, t_final=0.05, flux=1)
-        assert n_g == n_o and t_g == pytest.approx(0.05, abs=0) and t_o == pytest.approx(0.05, abs=0)
-        assert rel_linf(got, want) <= TOL
+    for flux in (0, 1):
+        for nx, ny in ((6, 6), (7, 13), (64, 9)):
+            q = ic.four_quadrant(nx, ny, nx * 100 + ny)
+            if flux == 1 and (nx, ny) == (64, 9):
+                want, t_o, n_o = oracle.fv2d_run(q, 9, t_final=0.05, flux=flux)
+                got, t_g, n_g = gpu_run2d(hteno_lib, q, 9, t_final=0.05, flux=flux)
+                assert n_g == n_o == 9 and t_g == t_o
+                np.testing.assert_array_equal(got, want)
+                with hteno_lib.Solver(hteno_lib.config(dims=2, nx=nx, ny=ny, flux=flux)) as s:
+                    s.set_state(q)
+                    s.step(1000, 0.05)
+                    assert s.status() != 0
+                continue
+            want, t_o, n_o = oracle.fv2d_run(q, 1000, t_final=0.05, flux=flux)
+            got, t_g, n_g = gpu_run2d(hteno_lib, q, 1000, t_final=0.05, flux=flux)
+            assert n_g == n_o and t_g == pytest.approx(0.05, abs=0) and t_o == pytest.approx(0.05, abs=0)
+            assert rel_linf(got, want) <= TOL
+            np.testing.assert_array_equal(got, want)
 
 
 def test_fv2d_constant_state_is_steady(hteno_lib, cuda):
@@ -140,9 +155,21 @@ def test_fv2d_nonphysical_state_reports_status(hteno_lib, cuda):
         assert e.value.code in (4, 5)
 
 
+def periodic_box(nx, ny):
+    """A dense, high-pressure square advected diagonally through periodic boundaries: contacts
+    and shocks that stay physical (the random four-quadrant data do not under periodic wrap)."""
+    from hteno import ic
+
+    x = (np.arange(nx) + 0.5) / nx
+    y = (np.arange(ny) + 0.5) / ny
+    X, Y = np.meshgrid(x, y)
+    inside = (np.abs(X - 0.5) < 0.25) & (np.abs(Y - 0.5) < 0.25)
+    return np.ascontiguousarray(ic.conservative2(1.0 + inside, 0.5 + 0 * X, -0.3 + 0 * X, 1.0 + 1.5 * inside))
+
+
 def test_fv2d_full_size_properties(hteno_lib, cuda):
-    """The 1024^2 benchmark configuration (HLLC, 200 steps): deterministic, positive, and with
-    periodic boundaries conservative to rounding."""
+    """The 1024^2 benchmark configuration (HLLC, 200 steps): deterministic and positive; with
+    periodic boundaries the totals are conserved to rounding."""
     from hteno import ic
 
     q = ic.four_quadrant(1024, 1024, 0)
@@ -151,10 +178,12 @@ def test_fv2d_full_size_properties(hteno_lib, cuda):
     assert n1 == 200 and t1 == t2
     np.testing.assert_array_equal(a, b)
     assert a[0].min() > 0
-    c, _, _ = gpu_run2d(hteno_lib, q, 50, flux=1, bc=1)
-    good = np.isfinite(c).all()
-    assert good, "periodic run stays finite"
-    np.testing.assert_allclose(c.sum(axis=(1, 2)), q.sum(axis=(1, 2)), rtol=1e-12)
+    p = periodic_box(1024, 1024)
+    c, _, _ = gpu_run2d(hteno_lib, p, 50, flux=1, bc=1)
+    assert np.isfinite(c).all() and c[0].min() > 0
+    tot0, tot = p.sum(axis=(1, 2)), c.sum(axis=(1, 2))
+    scale = np.abs(p).sum(axis=(1, 2))
+    assert (np.abs(tot - tot0) <= 1e-12 * scale).all(), (tot - tot0) / scale
 
 
 def test_fv2d_transpose_symmetry_gpu(hteno_lib, cuda):
