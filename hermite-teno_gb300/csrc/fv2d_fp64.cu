@@ -258,4 +258,89 @@ void fv2d_fp64_stage(hteno_solver* s, const Geo& G, const Work<double>& W, int s
   trace_end(s);
 }
 
+// ---- Residual without any device allocation --------------------------------------------------
+// Some callers cannot allocate device memory: code running inside another framework's stream
+// capture or memory pool, or a host that must keep its device footprint fixed after start-up.
+// hteno_residual_noalloc serves them with the FP64 residual above, its work buffers taken from
+// the fixed-size array below instead of cudaMalloc.  The array is part of the loaded module: every
+// GPU that loads the library holds it until the process exits.  All calls share it, so two calls
+// that overlap on the GPU race; it keeps the last call's contents, and nothing in it has to start
+// at zero because each launch writes every element it later reads.
+namespace {
+
+constexpr int kNoAllocMaxCells = HTENO_NOALLOC_MAX_CELLS;
+constexpr int kNoAllocMaxEdge = HTENO_NOALLOC_MAX_EDGE;  // bound on nx + ny
+constexpr size_t kNoAllocBytes =
+    4 * size_t(kNoAllocMaxCells) * sizeof(double) +
+    19 * (2 * size_t(kNoAllocMaxCells) + size_t(kNoAllocMaxEdge)) * sizeof(double) + 256 * 8;
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+void* g_noalloc_ptr[64] = {nullptr};
+unsigned long long g_noalloc_const = 0;
+std::mutex g_noalloc_mu;
+
+}  // namespace
+
 }  // namespace hteno
+
+using namespace hteno;
+
+extern "C" int hteno_residual_noalloc(const hteno_config* cfg, const double* q, double* rhs,
+                                      void* stream) {
+  if (!cfg || !q || !rhs) return HTENO_ERR_INVALID_ARG;
+  const hteno_config& c = *cfg;
+  if (c.dims != 2 || c.scheme != HTENO_SCHEME_FV || c.precision != HTENO_PREC_FP64)
+    return HTENO_ERR_UNSUPPORTED;
+  if (c.nx < 6 || c.ny < 6 || !(c.xr > c.xl) || !(c.yt > c.yb) || !(c.gamma > 1.0) ||
+      c.recon < 0 || c.recon > 2 || c.flux < 0 || c.flux > 1 || c.bc < 0 || c.bc > 1)
+    return HTENO_ERR_INVALID_ARG;
+  // size limit of the fixed scratch array
+  if ((long long)c.nx * c.ny > kNoAllocMaxCells || c.nx + c.ny > kNoAllocMaxEdge)
+    return HTENO_ERR_INVALID_ARG;
+  if (work_bytes<double>(c.nx, c.ny) > kNoAllocBytes) return HTENO_ERR_INVALID_ARG;
+
+  // one-time set-up per device, with that device current: the scratch address (a host-side
+  // stand-in is not a device address) and this file's constant block
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return HTENO_ERR_CUDA;
+  void* scratch = nullptr;
+  {
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+      void* ptr = nullptr;
+      if (cudaGetSymbolAddress(&ptr, g_noalloc_scratch) != cudaSuccess || !ptr) return HTENO_ERR_CUDA;
+      g_noalloc_ptr[dev] = ptr;
+    }
+    scratch = g_noalloc_ptr[dev];
+  }
+  if (upload_const(c_dev, &g_noalloc_const, &g_mu) != cudaSuccess) return HTENO_ERR_CUDA;
+
+  Geo G;
+  G.nx = c.nx;
+  G.ny = c.ny;
+  G.bc = c.bc;
+  G.recon = c.recon;
+  G.flux = c.flux;
+  G.dx = (c.xr - c.xl) / c.nx;
+  G.dy = (c.yt - c.yb) / c.ny;
+  G.area = G.dx * G.dy;
+  G.gamma = c.gamma;
+  G.g1 = c.gamma - 1.0;
+  const Work<double> W = carve<double>(scratch, c.nx, c.ny);
+  cudaStream_t cs = static_cast<cudaStream_t>(stream);
+  const long nxf = long(c.nx + 1) * c.ny, nyf = long(c.ny + 1) * c.nx;
+  const size_t nc = size_t(c.nx) * c.ny;
+  kp_prim<<<unsigned((nc + 255) / 256), 256, 0, cs>>>(G, q, W.prim, nullptr, 0);
+  kp_faces<1><<<unsigned((nxf + kFaceThreads - 1) / kFaceThreads), kFaceThreads, 0, cs>>>(
+      G, q, W.prim, W.xc, W.xroe, nullptr);
+  kp_faces<2><<<unsigned((nyf + kFaceThreads - 1) / kFaceThreads), kFaceThreads, 0, cs>>>(
+      G, q, W.prim, W.yc, W.yroe, nullptr);
+  kp_flux<1><<<unsigned((nxf + kFaceThreads - 1) / kFaceThreads), kFaceThreads, 0, cs>>>(
+      G, W.xc, W.xroe, W.fx, nullptr);
+  kp_flux<2><<<unsigned((nyf + kFaceThreads - 1) / kFaceThreads), kFaceThreads, 0, cs>>>(
+      G, W.yc, W.yroe, W.fy, nullptr);
+  kp_update<<<unsigned((nc + 255) / 256), 256, 0, cs>>>(G, 0, W.fx, W.fy, nullptr, nullptr,
+                                                       W.prim, rhs, nullptr);
+  return cudaGetLastError() == cudaSuccess ? HTENO_OK : HTENO_ERR_CUDA;
+}

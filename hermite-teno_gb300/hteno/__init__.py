@@ -94,6 +94,7 @@ def lib() -> ctypes.CDLL:
         L.hteno_measure_fma_peak.argtypes = [i, _D]
         L.hteno_get_status.argtypes = [vp, ctypes.POINTER(i)]
         L.hteno_set_strict.argtypes = [vp, i]
+        L.hteno_residual_noalloc.argtypes = [ctypes.POINTER(Config), vp, vp, vp]
         _lib = L
     return _lib
 

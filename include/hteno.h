@@ -182,6 +182,25 @@ int hteno_kernel_timing(hteno_solver* s, hteno_kernel_time* out, int max, int* c
  * kind 0 = FP64 FMA, 1 = FP32 FMA; result in TFLOP/s (2 flops per FMA). */
 int hteno_measure_fma_peak(int kind, double* tflops);
 
+/* ---- Residual without device allocation -------------------------------------------------- */
+
+/* Same computation as hteno_residual (one evaluation of FV::System2D::rhs in FP64) without a
+ * solver handle and without allocating device memory, for callers that cannot call cudaMalloc:
+ * code inside another framework's stream capture or memory pool, or hosts whose device footprint
+ * must stay fixed after start-up.  No reference counterpart: the reference has no device and no
+ * allocation constraints.
+ *   cfg: dims 2, scheme FV, precision FP64; q, rhs: DEVICE pointers [4][ny][nx]; stream may be
+ *   NULL.  Asynchronous.
+ * Limits: nx * ny <= HTENO_NOALLOC_MAX_CELLS and nx + ny <= HTENO_NOALLOC_MAX_EDGE; larger grids
+ * return HTENO_ERR_INVALID_ARG.  Its work buffers live in one fixed array (about 6 MB) inside
+ * the library, held by every GPU that loads the library until the process exits.
+ * The first call on each device looks up that array's address (cudaGetSymbolAddress) and
+ * uploads constants; make that first call before any stream capture.  All calls share the array,
+ * so calls that overlap on the GPU race with each other. */
+#define HTENO_NOALLOC_MAX_CELLS 16384
+#define HTENO_NOALLOC_MAX_EDGE 4096
+int hteno_residual_noalloc(const hteno_config* cfg, const double* q, double* rhs, void* stream);
+
 /* Version string of the library build. */
 const char* hteno_version(void);
 
