@@ -48,6 +48,11 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-mixed", action="store_true")
+    ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--no-hermite", action="store_true")
+    ap.add_argument("--hermite-steps", type=int, default=10)
+    ap.add_argument("--batch-steps", type=int, default=100)
     return ap.parse_args()
 
 
@@ -197,6 +202,121 @@ def run_reference(args):
 
 
 # ---- GB300 arm -------------------------------------------------------------------------------
+def batch_path(hteno, torch, stream, steps, world):
+    """256 independent grids with sides drawn from {64, ..., 512} (seeded, non-square allowed),
+    seeded four-quadrant data each, TENO5 + HLLC, mixed precision, per-instance dt; `steps`
+    steps of every instance timed with CUDA events (one graph replay per step)."""
+    from hteno import ic
+
+    rng = np.random.default_rng(4)
+    sides = rng.integers(64, 513, size=(256, 2))
+    cfgs = [hteno.config(dims=2, nx=int(nx), ny=int(ny), flux=hteno.FLUX_HLLC, recon=hteno.RECON_TENO5,
+                         precision=hteno.PREC_MIXED) for nx, ny in sides]
+    cells = int(sum(int(nx) * int(ny) for nx, ny in sides))
+    with hteno.Batch(cfgs) as b:
+        b.set_stream(stream.cuda_stream)
+        for k, (nx, ny) in enumerate(sides):
+            b.set_state(k, ic.four_quadrant(int(nx), int(ny), 1000 + k))
+        tile = b.tile()
+        b.step(3)  # warm-up (graph capture, first replays)
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        b.step_async(steps)
+        ev1.record(stream)
+        ev1.synchronize()
+        b.sync()
+        ms = ev0.elapsed_time(ev1)
+        done = [b.time(k)[1] for k in range(len(cfgs))]
+        status = [b.time(k)[2] for k in range(len(cfgs))]
+    return {"value": cells * steps * world / (ms / 1e3) / 1e6, "unit": UNIT, "ms_per_step": ms / steps,
+            "instances": len(cfgs), "cells": cells, "steps": steps, "tile": list(tile),
+            "min_steps_done": min(done), "unhealthy_instances": int(sum(1 for s in status if s)),
+            "note": "one persistent launch per RK stage over all instances' tiles, a step replayed "
+                    "as one CUDA graph; FP32 reconstruction/fluxes, FP64 state"}
+
+
+def hermite_path(hteno, torch, stream, steps, ref_steps, world, n=2048):
+    """Hermite-WENO 2D (FVHermite::System2D) on n x n: 32 seeded Gaussian density blobs on
+    rho = 1, p = 1, a Mach-2 shock entering from x = 0, moments by face differences; mixed
+    precision timed over `steps` steps; density error against the plain FP64 run advanced
+    `ref_steps` steps, the mixed run stopping at the same time."""
+    from hteno import ic
+
+    f = ic.blobs_shock_fn(5)
+    x = (np.arange(n) + 0.5) / n
+    X, Y = np.meshgrid(x, x)
+    q = np.ascontiguousarray(f(X, Y))
+    v, w = ic.face_difference_moments(f, n, n, 0.0, 1.0, 0.0, 1.0)
+    out = {}
+    ref = None
+    for prec in (hteno.PREC_FP64, hteno.PREC_MIXED):
+        cfg = hteno.config(dims=2, scheme=hteno.SCHEME_HERMITE, nx=n, ny=n, flux=hteno.FLUX_RUSANOV,
+                           precision=prec)
+        with hteno.Solver(cfg) as s:
+            s.set_stream(stream.cuda_stream)
+            s.set_state(q)
+            s.set_moments(v, w)
+            k = ref_steps if prec == hteno.PREC_FP64 else steps
+            ev0 = torch.cuda.Event(enable_timing=True)
+            ev1 = torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            ev0.record(stream)
+            s.step_async(k)
+            ev1.record(stream)
+            ev1.synchronize()
+            s.sync()
+            ms = ev0.elapsed_time(ev1)
+            name = "fp64" if prec == hteno.PREC_FP64 else "fp32_mixed"
+            out[name] = {"value": n * n * k * world / (ms / 1e3) / 1e6, "unit": UNIT,
+                         "ms_per_step": ms / k, "steps": k}
+            if prec == hteno.PREC_FP64:
+                ref = (s.time()[0], s.get_state())
+            else:
+                s.set_state(q)
+                s.set_moments(v, w)
+                s.step(1 << 20, ref[0])
+                l1, linf = density_errors(s.get_state(), ref[1])
+                out[name].update({"l1_rho_vs_fp64": l1, "linf_rho_vs_fp64": linf, "t": ref[0]})
+    out["speedup_mixed_vs_fp64"] = out["fp64"]["ms_per_step"] / out["fp32_mixed"]["ms_per_step"]
+    out["workload"] = f"hermite2d_blobs_mach2_{n}x{n}_rusanov_ssprk3"
+    return out
+
+
+def density_errors(a, b):
+    d = np.abs(a[0] - b[0])
+    return float(d.mean()), float(d.max())
+
+
+def mixed_path(hteno, torch, q, stream, args, t_end, ref_state, ms_plain, world):
+    """Times K steps of the mixed path after W warm-up steps (the same counts as the plain run),
+    then finishes the run at the plain run's end time and reports the density error."""
+    cfg = hteno.config(dims=2, nx=NX, ny=NY, flux=hteno.FLUX_HLLC, recon=hteno.RECON_TENO5,
+                       precision=hteno.PREC_MIXED)
+    with hteno.Solver(cfg) as s:
+        s.set_stream(stream.cuda_stream)
+        s.set_state(q)
+        s.step_async(args.warmup)
+        s.sync()
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        s.step_async(args.steps)
+        ev1.record(stream)
+        ev1.synchronize()
+        ms = ev0.elapsed_time(ev1)
+        s.step(1 << 20, t_end)
+        t, n, _ = s.time()
+        l1, linf = density_errors(s.get_state(), ref_state)
+    return {"value": NX * NY * args.steps * world / (ms / 1e3) / 1e6, "unit": UNIT,
+            "ms_per_step": ms / args.steps, "speedup_vs_fp64": ms_plain / ms,
+            "l1_rho_vs_fp64": l1, "linf_rho_vs_fp64": linf, "t": t, "steps_to_t": n,
+            "note": "FP32 reconstruction/fluxes, FP64 state and SSP-RK3; error against the plain "
+                    "FP64 GPU state at the same time (bit-identical to the CPU oracle)"}
+
+
 def run_gpu(args):
     import torch
 
@@ -237,6 +357,8 @@ def run_gpu(args):
     barrier(torch, world)
     solver.sync()
     ms = ev0.elapsed_time(ev1)
+    t_plain, _, _ = solver.time()
+    ref_state = solver.get_state()
     ms_max = allreduce_max(torch, world, ms)
     value = ncell * args.steps * world / (ms_max / 1e3) / 1e6
 
@@ -292,11 +414,22 @@ def run_gpu(args):
         e2e = {"value": ncell * e2e_steps * world / el / 1e6, "unit": UNIT,
                "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes}
 
+    # the mixed path (FP32 reconstruction and fluxes, FP64 state and RK accumulation) on the same
+    # workload, advanced to the same time as the plain path; density error against the plain
+    # FP64 state, which is bit-identical to the CPU oracle
+    paths = {}
+    if not args.no_mixed:
+        paths["fp32_mixed"] = mixed_path(hteno, torch, q, stream, args, t_plain, ref_state, ms_max, world)
+    if not args.no_hermite:
+        paths["hermite_2048"] = hermite_path(hteno, torch, stream, args.hermite_steps, 3, world)
+    if not args.no_batch:
+        paths["batch_256_mixed"] = batch_path(hteno, torch, stream, args.batch_steps, world)
+
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": config_block(args, world), "gpu_launches": launches * args.steps,
-            "clocks": clocks.summary(), "roofline": roofline, "e2e": e2e}
+            "clocks": clocks.summary(), "roofline": roofline, "e2e": e2e, "paths": paths}
     if rank == 0 and world == 1 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline_sample(os.cpu_count() or 1)
     solver.close()

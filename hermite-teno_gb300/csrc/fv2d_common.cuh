@@ -58,6 +58,29 @@ constexpr double kUpdateFlops = 52.0;         // primitives, flux difference, RK
 
 constexpr int kFaceThreads = 128;
 
+inline Geo geo_of(const hteno_solver* s) {
+  Geo G;
+  G.nx = s->cfg.nx;
+  G.ny = s->cfg.ny;
+  G.bc = s->cfg.bc;
+  G.recon = s->cfg.recon;
+  G.flux = s->cfg.flux;
+  G.dx = s->dx;
+  G.dy = s->dy;
+  G.area = s->dx * s->dy;
+  G.gamma = s->cfg.gamma;
+  G.g1 = s->cfg.gamma - 1.0;
+  return G;
+}
+
+// Mixed path, one fused launch per stage (fv2d_fused.cu).  Work buffer: one extra state.
+size_t fv2d_fused_work_bytes(int nx, int ny);
+int fv2d_fused_setup(hteno_solver* s);
+int fv2d_fused_prepare(hteno_solver* s, const Geo& G, double* scratch);
+void fv2d_fused_step(hteno_solver* s, const Geo& G, double* qc);
+void fv2d_fused_residual(hteno_solver* s, const Geo& G, const double* q, double* rhs);
+const char* fv2d_fused_variant_name(int v);
+
 // Bit-reproducible FP64 path (fv2d_fp64.cu)
 int fv2d_fp64_setup(hteno_solver* s);
 void fv2d_fp64_prim(hteno_solver* s, const Geo& G, const Work<double>& W, const double* q,

@@ -1,0 +1,304 @@
+// Fused mixed-precision stage of FV::System2D (FV_System2D.cpp:363-612) for one tile of cells:
+// residual of both directions and the SSP-RK3 stage combination in one pass, so a stage reads
+// the conserved state once and writes it once.
+//
+//   A  load the tile plus a 3-cell halo of q (double) into shared memory as float, with the
+//      primitives u, v, H, sqrt|rho| of every loaded cell (calcPrimitiveVariable, :226-263)
+//   B  x faces of rows -2 .. TY+1: Roe average, L projection of the 6-cell stencil, TENO5 (or
+//      teno5i / linear) for 4 fields on both sides -> 8 characteristic values per face
+//   C  x faces of rows 0 .. TY-1: GL3 across rows r-2 .. r+2 (each face in its own basis, as
+//      the reference), R back-projection with the face's Roe state, HLLC or Rusanov at the 3
+//      Gauss points, quadrature (:432-497)
+//   D, E the same for the y faces
+//   F  flux difference in double, SSP-RK3 in double (Schemes_SSPRK.cpp:3-15); on the last
+//      stage the pressure (double, refined reciprocal), the health flags and the max wave
+//      speed that sets the next dt (timeStepping, :622-633)
+//
+// Reconstruction, smoothness indicators and fluxes run in float; the state, the RK accumulation
+// and the pressure check stay double.  Stage buffers: a stage reads its input state with halos
+// from `qin` (never written during the stage), the step-start state pointwise from `qbase`
+// and writes `qout`; stage 3 writes in place over the step-start state, which only the owning
+// thread reads.  Included by the translation units that launch it (single-grid and batched).
+#pragma once
+
+#include "fv2d_common.cuh"
+
+namespace hteno {
+namespace fused {
+
+// Cell index with the boundary condition applied for any offset (tiles may run past the edge
+// of small grids): zero-gradient clamps, periodic wraps.
+__device__ __forceinline__ int cmap(int i, int n, int bc) {
+  if (bc == HTENO_BC_PERIODIC) {
+    i %= n;
+    return i < 0 ? i + n : i;
+  }
+  return min(max(i, 0), n - 1);
+}
+
+template <int TX, int TY>
+struct Shape {
+  static constexpr int W = TX + 6, H = TY + 6;   // loaded cells, halo 3
+  static constexpr int XF = TX + 1, XR = TY + 4;  // x faces: columns 0..TX, rows -2..TY+1
+  static constexpr int YF = TY + 1, YC = TX + 4;  // y faces: rows 0..TY, columns -2..TX+1
+  static constexpr int XN = XF * XR, YN = YF * YC;
+  static constexpr int FN = XN > YN ? XN : YN;
+};
+
+template <int TX, int TY>
+struct Smem {
+  float q[4][TY + 6][TX + 6];
+  float p[4][TY + 6][TX + 6];  // u, v, H, sqrt|rho|
+  float c[8][Shape<TX, TY>::FN];
+  float fx[4][TY][TX + 1];
+  float fy[4][TY + 1][TX];
+  float wtab[2][8][3];  // TENO weights per cut-off pattern, minus and plus side
+};
+
+template <int TX, int TY>
+constexpr size_t smem_bytes() {
+  return sizeof(Smem<TX, TY>);
+}
+
+// One side of teno5 / teno5i with the weight table in shared memory (a per-thread pattern
+// would serialise constant-memory reads).
+__device__ __forceinline__ float teno_side_s(float p0, float p1, float p2, const float* v,
+                                             const float (*tab)[3], bool improved) {
+  float SI0, SI1, SI2;
+  lagrange_si(v, SI0, SI1, SI2);
+  float tau;
+  if (!improved) tau = fabsf(lagrange_b35(v) - (SI0 + SI2 + 4.0f * SI1) * (1.0f / 6.0f));
+  else tau = fmaxf(fmaxf(SI0, SI1), SI2);
+  const float ez = HTENO_F32_EPSZ;
+  const float r0 = 1.0f + tau * __frcp_rn(SI0 + ez);
+  const float r1 = 1.0f + tau * __frcp_rn(SI1 + ez);
+  const float r2 = 1.0f + tau * __frcp_rn(SI2 + ez);
+  const float* w = tab[teno_pattern(r0, r1, r2, float(HTENO_LAG_CT))];
+  return catchnan(p0 * w[0] + p1 * w[1] + p2 * w[2]);
+}
+
+// teno5 (Schemes_Lagrange.cpp:481-511), teno5i (:1235-1263) or linear (:1219-1233):
+// u[0..5] -> (u^-_{i+1/2}, u^+_{i+1/2}).
+__device__ __forceinline__ void recon_s(const DevConst& C, int kind, const float (*tab)[8][3],
+                                        const float* u, float& outm, float& outp) {
+  float p0 = C.f_crj[0][1] * u[2] + C.f_crj[1][1] * u[3] + C.f_crj[2][1] * u[4];
+  float p1 = C.f_crj[0][2] * u[1] + C.f_crj[1][2] * u[2] + C.f_crj[2][2] * u[3];
+  float p2 = C.f_crj[0][3] * u[0] + C.f_crj[1][3] * u[1] + C.f_crj[2][3] * u[2];
+  if (kind == 2) outm = p0 * tab[0][7][0] + p1 * tab[0][7][1] + p2 * tab[0][7][2];
+  else outm = teno_side_s(p0, p1, p2, u, tab[0], kind == 1);
+  p0 = C.f_crj[0][0] * u[3] + C.f_crj[1][0] * u[4] + C.f_crj[2][0] * u[5];
+  p1 = C.f_crj[0][1] * u[2] + C.f_crj[1][1] * u[3] + C.f_crj[2][1] * u[4];
+  p2 = C.f_crj[0][2] * u[1] + C.f_crj[1][2] * u[2] + C.f_crj[2][2] * u[3];
+  if (kind == 2) outp = p0 * tab[1][7][0] + p1 * tab[1][7][1] + p2 * tab[1][7][2];
+  else outp = teno_side_s(p0, p1, p2, u + 1, tab[1], kind == 1);
+}
+
+// Pointers of one stage of one grid.
+struct StageArgs {
+  const double* qin;    // input state of the stage (halo reads)
+  const double* qbase;  // step-start state (stages 2, 3), read pointwise
+  double* qout;         // output state (stages 1-3) or residual (stage 0)
+  StepState* st;        // dt, health flags, max wave speed; null for stage 0
+};
+
+// The tile at (i0, j0) of grid G.  Every thread of the block must call it (barriers inside).
+// Returns this thread's max wave speed over the cells it updated (stage 3) and ORs health flags
+// into *bad.
+template <int TX, int TY, int NT>
+__device__ __forceinline__ double tile_stage(const DevConst& C, const Geo& G, int i0, int j0,
+                                             int stage, const StageArgs& a, Smem<TX, TY>& S,
+                                             int& bad) {
+  typedef Shape<TX, TY> Sh;
+  const size_t nc = size_t(G.nx) * G.ny;
+  const float g1 = float(G.g1);
+  const int tid = threadIdx.x;
+
+  if (tid < 48) {
+    const int side = tid / 24, pat = (tid % 24) / 3, k = tid % 3;
+    S.wtab[side][pat][k] = side ? C.f_wtab_p[pat][k] : C.f_wtab_m[pat][k];
+  }
+  // A: state and primitives of the tile and its halo
+  for (int it = tid; it < Sh::W * Sh::H; it += NT) {
+    const int y = it / Sh::W, x = it - y * Sh::W;
+    const int gi = cmap(i0 - 3 + x, G.nx, G.bc), gj = cmap(j0 - 3 + y, G.ny, G.bc);
+    const size_t k = size_t(gj) * G.nx + gi;
+    const float r = float(__ldg(a.qin + k)), mx = float(__ldg(a.qin + nc + k));
+    const float my = float(__ldg(a.qin + 2 * nc + k)), e = float(__ldg(a.qin + 3 * nc + k));
+    S.q[0][y][x] = r;
+    S.q[1][y][x] = mx;
+    S.q[2][y][x] = my;
+    S.q[3][y][x] = e;
+    const float ir = __frcp_rn(r);
+    const float u = mx * ir, v = my * ir;
+    const float p = (e - 0.5f * (mx * u + my * v)) * g1;
+    S.p[0][y][x] = u;
+    S.p[1][y][x] = v;
+    S.p[2][y][x] = (e + p) * ir;
+    S.p[3][y][x] = sqrtf(fabsf(r));
+  }
+  __syncthreads();
+
+  // B: x faces, characteristic reconstruction
+  for (int it = tid; it < Sh::XN; it += NT) {
+    const int rr = it / Sh::XF, f = it - rr * Sh::XF;
+    const int y = rr + 1;
+    const int xa = f + 2, xb = f + 3;
+    const Roe2<float> R = roe2<float>(g1, S.p[3][y][xa], S.p[0][y][xa], S.p[1][y][xa],
+                                      S.p[2][y][xa], S.p[3][y][xb], S.p[0][y][xb],
+                                      S.p[1][y][xb], S.p[2][y][xb]);
+    float ch[4][6];
+#pragma unroll
+    for (int m = 0; m < 6; ++m) {
+      const float qq[4] = {S.q[0][y][f + m], S.q[1][y][f + m], S.q[2][y][f + m], S.q[3][y][f + m]};
+      float cc[4];
+      roe_left(R, 1, qq, cc);
+#pragma unroll
+      for (int r = 0; r < 4; ++r) ch[r][m] = cc[r];
+    }
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      float lo, hi;
+      recon_s(C, G.recon, S.wtab, ch[r], lo, hi);
+      S.c[r][it] = lo;
+      S.c[4 + r][it] = hi;
+    }
+  }
+  __syncthreads();
+
+  // C: x faces, transverse quadrature and flux
+  for (int it = tid; it < Sh::XF * TY; it += NT) {
+    const int r = it / Sh::XF, f = it - r * Sh::XF;
+    float g[8][3];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      float u5[5];
+#pragma unroll
+      for (int m = 0; m < 5; ++m) u5[m] = S.c[k][(r + m) * Sh::XF + f];
+      gl3(C, u5, g[k][0], g[k][1], g[k][2]);
+    }
+    const int y = r + 3, xa = f + 2, xb = f + 3;
+    const Roe2<float> R = roe2<float>(g1, S.p[3][y][xa], S.p[0][y][xa], S.p[1][y][xa],
+                                      S.p[2][y][xa], S.p[3][y][xb], S.p[0][y][xb],
+                                      S.p[1][y][xb], S.p[2][y][xb]);
+    float acc[4];
+#pragma unroll
+    for (int m = 0; m < 3; ++m) {
+      const float cl[4] = {g[0][m], g[1][m], g[2][m], g[3][m]};
+      const float cr[4] = {g[4][m], g[5][m], g[6][m], g[7][m]};
+      float ql[4], qr[4], Fm[4];
+      roe_right(R, 1, cl, ql);
+      roe_right(R, 1, cr, qr);
+      if (G.flux == HTENO_FLUX_HLLC) hllc2(g1, 1, ql, qr, Fm);
+      else rusanov2(float(G.gamma), g1, 1, R, ql, qr, Fm);
+      const float wm = C.f_gl3w[m];
+#pragma unroll
+      for (int v = 0; v < 4; ++v) acc[v] = m == 0 ? wm * Fm[v] : acc[v] + wm * Fm[v];
+    }
+#pragma unroll
+    for (int v = 0; v < 4; ++v) S.fx[v][r][f] = acc[v];
+  }
+  __syncthreads();
+
+  // D: y faces, characteristic reconstruction
+  for (int it = tid; it < Sh::YN; it += NT) {
+    const int gg = it / Sh::YC, cc = it - gg * Sh::YC;
+    const int x = cc + 1;
+    const int ya = gg + 2, yb = gg + 3;
+    const Roe2<float> R = roe2<float>(g1, S.p[3][ya][x], S.p[0][ya][x], S.p[1][ya][x],
+                                      S.p[2][ya][x], S.p[3][yb][x], S.p[0][yb][x],
+                                      S.p[1][yb][x], S.p[2][yb][x]);
+    float ch[4][6];
+#pragma unroll
+    for (int m = 0; m < 6; ++m) {
+      const float qq[4] = {S.q[0][gg + m][x], S.q[1][gg + m][x], S.q[2][gg + m][x],
+                           S.q[3][gg + m][x]};
+      float cv[4];
+      roe_left(R, 2, qq, cv);
+#pragma unroll
+      for (int r = 0; r < 4; ++r) ch[r][m] = cv[r];
+    }
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      float lo, hi;
+      recon_s(C, G.recon, S.wtab, ch[r], lo, hi);
+      S.c[r][it] = lo;
+      S.c[4 + r][it] = hi;
+    }
+  }
+  __syncthreads();
+
+  // E: y faces, transverse quadrature and flux
+  for (int it = tid; it < Sh::YF * TX; it += NT) {
+    const int gg = it / TX, col = it - gg * TX;
+    float g[8][3];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      float u5[5];
+#pragma unroll
+      for (int m = 0; m < 5; ++m) u5[m] = S.c[k][gg * Sh::YC + col + m];
+      gl3(C, u5, g[k][0], g[k][1], g[k][2]);
+    }
+    const int x = col + 3, ya = gg + 2, yb = gg + 3;
+    const Roe2<float> R = roe2<float>(g1, S.p[3][ya][x], S.p[0][ya][x], S.p[1][ya][x],
+                                      S.p[2][ya][x], S.p[3][yb][x], S.p[0][yb][x],
+                                      S.p[1][yb][x], S.p[2][yb][x]);
+    float acc[4];
+#pragma unroll
+    for (int m = 0; m < 3; ++m) {
+      const float cl[4] = {g[0][m], g[1][m], g[2][m], g[3][m]};
+      const float cr[4] = {g[4][m], g[5][m], g[6][m], g[7][m]};
+      float ql[4], qr[4], Fm[4];
+      roe_right(R, 2, cl, ql);
+      roe_right(R, 2, cr, qr);
+      if (G.flux == HTENO_FLUX_HLLC) hllc2(g1, 2, ql, qr, Fm);
+      else rusanov2(float(G.gamma), g1, 2, R, ql, qr, Fm);
+      const float wm = C.f_gl3w[m];
+#pragma unroll
+      for (int v = 0; v < 4; ++v) acc[v] = m == 0 ? wm * Fm[v] : acc[v] + wm * Fm[v];
+    }
+#pragma unroll
+    for (int v = 0; v < 4; ++v) S.fy[v][gg][col] = acc[v];
+  }
+  __syncthreads();
+
+  // F: residual and SSP-RK3 stage in double
+  double ms = 0.0;
+  const double dt = stage ? a.st->dt : 0.0;
+  for (int it = tid; it < TX * TY; it += NT) {
+    const int y = it / TX, x = it - y * TX;
+    const int gi = i0 + x, gj = j0 + y;
+    if (gi >= G.nx || gj >= G.ny) continue;
+    const size_t k = size_t(gj) * G.nx + gi;
+    double qn[4];
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      const double dfx = double(S.fx[v][y][x]) - double(S.fx[v][y][x + 1]);
+      const double dfy = double(S.fy[v][y][x]) - double(S.fy[v][y + 1][x]);
+      const double rhs = (dfx * G.dy + dfy * G.dx) / G.area;
+      if (stage == 0) {
+        a.qout[v * nc + k] = rhs;
+      } else {
+        const double cur = a.qin[v * nc + k];
+        const double base = stage == 1 ? cur : a.qbase[v * nc + k];
+        qn[v] = ssprk3(base, cur, rhs, dt, stage);
+        a.qout[v * nc + k] = qn[v];
+      }
+    }
+    if (stage == 3) {
+      // pressure in double with a refined float reciprocal of rho (relative error ~1e-14)
+      double ir = double(__frcp_rn(float(qn[0])));
+      ir = fma(ir, fma(-qn[0], ir, 1.0), ir);
+      const double p = (qn[3] - 0.5 * (qn[1] * qn[1] + qn[2] * qn[2]) * ir) * G.g1;
+      if (isnan(p)) bad |= 1;
+      else if (qn[0] <= 0.0 || p <= 0.0) bad |= 2;
+      const float fr = float(qn[0]), fu = float(qn[1] * ir), fv = float(qn[2] * ir);
+      const float c = sqrtf(fabsf(float(G.gamma) * float(p) / fr));
+      const float m = fmaxf(fmaxf(fu - c, fabsf(fu + c)), fmaxf(fv - c, fabsf(fv + c)));
+      ms = fmax(ms, double(m));
+    }
+  }
+  return ms;
+}
+
+}  // namespace fused
+}  // namespace hteno

@@ -68,6 +68,7 @@ struct hteno_solver {
   hteno::StepState* hstate = nullptr;  // pinned host mirror
 
   int launches_per_step = 0;
+  int tile_variant = -1;  // mixed FV 2D: tile shape picked by the tuner (-1: not yet)
   bool strict = false;
   std::string err;
 

@@ -305,10 +305,22 @@ int hteno_sync(hteno_solver* s) {
   return HTENO_OK;
 }
 
+// Synchronous stepping issues the steps in growing chunks and stops issuing once the device
+// state shows t >= t_final, so a large step budget (advance to tmax) costs no idle launches.
 int hteno_step(hteno_solver* s, int nsteps, double t_final) {
-  int rc = hteno_step_async(s, nsteps, t_final);
-  if (rc) return rc;
-  return hteno_sync(s);
+  if (!s || nsteps < 0 || std::isnan(t_final)) return HTENO_ERR_INVALID_ARG;
+  int chunk = 32;
+  for (int left = nsteps; left > 0;) {
+    const int n = left < chunk ? left : chunk;
+    int rc = hteno_step_async(s, n, t_final);
+    if (rc) return rc;
+    rc = hteno_sync(s);
+    if (rc) return rc;
+    left -= n;
+    if (s->hstate->done || !(s->hstate->t < t_final)) break;
+    chunk = chunk < 1024 ? chunk * 2 : 1024;
+  }
+  return HTENO_OK;
 }
 
 int hteno_get_time(hteno_solver* s, double* t, long* steps, double* last_dt) {

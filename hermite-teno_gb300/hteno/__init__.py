@@ -95,6 +95,19 @@ def lib() -> ctypes.CDLL:
         L.hteno_get_status.argtypes = [vp, ctypes.POINTER(i)]
         L.hteno_set_strict.argtypes = [vp, i]
         L.hteno_residual_noalloc.argtypes = [ctypes.POINTER(Config), vp, vp, vp]
+        L.hteno_batch_create.argtypes = [ctypes.POINTER(Config), i, ctypes.POINTER(vp)]
+        L.hteno_batch_destroy.argtypes = [vp]
+        L.hteno_batch_size.argtypes = [vp, ctypes.POINTER(i)]
+        L.hteno_batch_set_stream.argtypes = [vp, vp]
+        L.hteno_batch_set_state.argtypes = [vp, i, vp, i]
+        L.hteno_batch_get_state.argtypes = [vp, i, vp, i]
+        L.hteno_batch_step.argtypes = [vp, i, d]
+        L.hteno_batch_step_async.argtypes = [vp, i, d]
+        L.hteno_batch_sync.argtypes = [vp]
+        L.hteno_batch_get_time.argtypes = [vp, i, _D, ctypes.POINTER(l), ctypes.POINTER(i)]
+        L.hteno_batch_tile.argtypes = [vp, ctypes.POINTER(i), ctypes.POINTER(i), ctypes.POINTER(i)]
+        L.hteno_batch_last_error.restype = ctypes.c_char_p
+        L.hteno_batch_last_error.argtypes = [vp]
         _lib = L
     return _lib
 
@@ -208,6 +221,75 @@ class Solver:
 
     def residual(self, q_dev, rhs_dev) -> None:
         _check(lib().hteno_residual(self.h, _ptr(q_dev)[0], _ptr(rhs_dev)[0]), self.h)
+
+
+class Batch:
+    """Owner of one hteno_batch handle: independent mixed-precision FV 2D grids stepped together."""
+
+    def __init__(self, cfgs):
+        arr = (Config * len(cfgs))(*cfgs)
+        h = ctypes.c_void_p()
+        rc = lib().hteno_batch_create(arr, len(cfgs), ctypes.byref(h))
+        if rc != 0:
+            raise HtenoError(rc, "batch create")
+        self.h = h
+        self.shapes = [(4, c.ny, c.nx) for c in cfgs]
+
+    def _check(self, rc):
+        if rc != 0:
+            raise HtenoError(rc, lib().hteno_batch_last_error(self.h).decode())
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            lib().hteno_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __len__(self):
+        return len(self.shapes)
+
+    def set_stream(self, stream_ptr: int) -> None:
+        self._check(lib().hteno_batch_set_stream(self.h, ctypes.c_void_p(stream_ptr)))
+
+    def set_state(self, i: int, q) -> None:
+        p, where = _ptr(q)
+        self._check(lib().hteno_batch_set_state(self.h, i, p, where))
+
+    def get_state(self, i: int, out=None):
+        out = np.empty(self.shapes[i]) if out is None else out
+        p, where = _ptr(out)
+        self._check(lib().hteno_batch_get_state(self.h, i, p, where))
+        return out
+
+    def step(self, nsteps: int, t_final: float = float("inf")) -> None:
+        self._check(lib().hteno_batch_step(self.h, int(nsteps), float(t_final)))
+
+    def step_async(self, nsteps: int, t_final: float = float("inf")) -> None:
+        self._check(lib().hteno_batch_step_async(self.h, int(nsteps), float(t_final)))
+
+    def sync(self) -> None:
+        self._check(lib().hteno_batch_sync(self.h))
+
+    def time(self, i: int):
+        t, n, st = ctypes.c_double(), ctypes.c_long(), ctypes.c_int()
+        self._check(lib().hteno_batch_get_time(self.h, i, ctypes.byref(t), ctypes.byref(n), ctypes.byref(st)))
+        return t.value, n.value, st.value
+
+    def tile(self):
+        tx, ty, nt = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        self._check(lib().hteno_batch_tile(self.h, ctypes.byref(tx), ctypes.byref(ty), ctypes.byref(nt)))
+        return tx.value, ty.value, nt.value
 
 
 def measure_fma_peak(kind: int) -> float:

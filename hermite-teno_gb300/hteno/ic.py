@@ -54,37 +54,47 @@ def sod(nx: int, xl: float = 0.0, xr: float = 1.0, gamma: float = 1.4):
     return np.ascontiguousarray(np.stack([rho, rho * u, p / (gamma - 1.0) + 0.5 * rho * u * u]))
 
 
-def gaussian_blobs_shock(nx: int, ny: int, seed: int, gamma: float = 1.4, nblob: int = 32,
-                         mach: float = 2.0, x_shock: float = 0.02):
-    """Conserved state [4][ny][nx] on [0,1]^2: rho = 1 + sum_b A_b exp(-|x - x_b|^2 / s_b^2),
-    A ~ U[0.2, 1], s ~ U[0.01, 0.05], centres ~ U[0,1]^2 (drawn in that order per blob),
-    p = 1, u = v = 0; cells with x < x_shock hold the post-shock state of a Mach `mach` shock
-    moving in +x into rho = 1, p = 1."""
+def blobs_shock_fn(seed: int, gamma: float = 1.4, nblob: int = 32, mach: float = 2.0,
+                   x_shock: float = 0.02):
+    """Pointwise conserved state q(X, Y) -> [4, ...] on [0,1]^2: rho = 1 + sum_b A_b
+    exp(-|x - x_b|^2 / s_b^2), A ~ U[0.2, 1], s ~ U[0.01, 0.05], centres ~ U[0,1]^2 (drawn in
+    that order per blob), p = 1, u = v = 0; points with x < x_shock hold the post-shock state of
+    a Mach `mach` shock moving in +x into rho = 1, p = 1 (Rankine-Hugoniot)."""
     rng = np.random.default_rng(seed)
-    x = (np.arange(nx) + 0.5) / nx
-    y = (np.arange(ny) + 0.5) / ny
-    X, Y = np.meshgrid(x, y)
-    rho = np.ones((ny, nx))
+    blobs = []
     for _ in range(nblob):
         a = rng.uniform(0.2, 1.0)
         s = rng.uniform(0.01, 0.05)
         cx, cy = rng.uniform(0.0, 1.0, size=2)
-        rho += a * np.exp(-((X - cx) ** 2 + (Y - cy) ** 2) / s ** 2)
-    p = np.ones((ny, nx))
-    u = np.zeros((ny, nx))
-    v = np.zeros((ny, nx))
-    # Rankine-Hugoniot post-shock state for a shock of Mach M into (rho0, p0, u0 = 0)
+        blobs.append((a, s, cx, cy))
     g, M = gamma, mach
     rho0, p0 = 1.0, 1.0
     c0 = np.sqrt(g * p0 / rho0)
     rho1 = rho0 * (g + 1) * M ** 2 / ((g - 1) * M ** 2 + 2)
     p1 = p0 * (2 * g * M ** 2 - (g - 1)) / (g + 1)
     u1 = M * c0 * (1 - rho0 / rho1)
-    post = X < x_shock
-    rho = np.where(post, rho1, rho)
-    p = np.where(post, p1, p)
-    u = np.where(post, u1, u)
-    return np.ascontiguousarray(conservative2(rho, u, v, p, gamma))
+
+    def q(X, Y):
+        rho = np.ones_like(X)
+        for a, s, cx, cy in blobs:
+            rho = rho + a * np.exp(-((X - cx) ** 2 + (Y - cy) ** 2) / s ** 2)
+        post = X < x_shock
+        rho = np.where(post, rho1, rho)
+        p = np.where(post, p1, 1.0 + 0 * X)
+        u = np.where(post, u1, 0 * X)
+        return conservative2(rho, u, 0 * X, p, gamma)
+
+    return q
+
+
+def gaussian_blobs_shock(nx: int, ny: int, seed: int, gamma: float = 1.4, nblob: int = 32,
+                         mach: float = 2.0, x_shock: float = 0.02):
+    """Cell-centre values [4][ny][nx] of blobs_shock_fn on [0,1]^2."""
+    x = (np.arange(nx) + 0.5) / nx
+    y = (np.arange(ny) + 0.5) / ny
+    X, Y = np.meshgrid(x, y)
+    f = blobs_shock_fn(seed, gamma, nblob, mach, x_shock)
+    return np.ascontiguousarray(f(X, Y))
 
 
 def face_difference_moments(q_fn, nx, ny, xl, xr, yb, yt):

@@ -94,10 +94,11 @@ int hteno_get_moments(hteno_solver* s, double* v, double* w, int where);
 
 /* Advances at most nsteps SSP-RK3 steps, stopping when t reaches t_final (the loop of
  * timeStepping(), FV_System2D.cpp:614-651, with dt = cfl*min(dx,dy)/max wave speed and the
- * last step clipped to t_final).  Launches asynchronously and synchronises at the end. */
+ * last step clipped to t_final).  Issues the steps in chunks, checking the device time
+ * between chunks, so a large nsteps (advance to t_final) launches no idle steps. */
 int hteno_step(hteno_solver* s, int nsteps, double t_final);
-/* Same as hteno_step without the final synchronisation and status check (for timing loops
- * and graph replay); call hteno_sync() before reading results. */
+/* Issues exactly nsteps steps without synchronising (steps after t_final are no-ops on the
+ * device); for timing loops.  Call hteno_sync() before reading results. */
 int hteno_step_async(hteno_solver* s, int nsteps, double t_final);
 int hteno_sync(hteno_solver* s);
 int hteno_get_time(hteno_solver* s, double* t, long* steps, double* last_dt);
@@ -158,6 +159,34 @@ int hteno_ssprk3_batch(const double* q0, const double* qn, const double* rhs, do
 /* One residual evaluation of FV::System2D::rhs (FV_System2D.cpp:363-573) at state q[4][ny][nx]
  * (device) into rhs[4][ny][nx] (device), using the solver's configuration and buffers. */
 int hteno_residual(hteno_solver* s, const double* q, double* rhs);
+
+/* ---- Batches of independent 2D grids (mixed precision FV) --------------------------------- */
+
+/* n independent FV::System2D instances (FV_System2D.h:12-20), each with its own config (dims 2,
+ * scheme FV, precision HTENO_PREC_MIXED; grid sizes may differ and need not be square), advanced
+ * together: each instance keeps its own time, dt and stop test exactly as its own
+ * timeStepping() loop would (FV_System2D.cpp:614-651).  One persistent launch per RK stage
+ * covers the tiles of every instance; a whole step is captured once in a CUDA graph and
+ * replayed; the tile shape is picked by timing the candidates on the batch itself (first step,
+ * or hteno_batch_tile).  No reference counterpart for the batching itself: the reference runs
+ * one grid per process. */
+typedef struct hteno_batch hteno_batch;
+int hteno_batch_create(const hteno_config* cfgs, int n, hteno_batch** out);
+int hteno_batch_destroy(hteno_batch* b);
+int hteno_batch_size(hteno_batch* b, int* n);
+int hteno_batch_set_stream(hteno_batch* b, void* cuda_stream);
+/* State of instance i, SoA [4][ny_i][nx_i]; resets that instance's time to its t_init. */
+int hteno_batch_set_state(hteno_batch* b, int i, const double* q, int where);
+int hteno_batch_get_state(hteno_batch* b, int i, double* q, int where);
+/* Up to nsteps steps of every instance; an instance stops once its time reaches t_final. */
+int hteno_batch_step(hteno_batch* b, int nsteps, double t_final);
+int hteno_batch_step_async(hteno_batch* b, int nsteps, double t_final);
+int hteno_batch_sync(hteno_batch* b);
+/* Time, completed steps and health flags of instance i as of the last hteno_batch_sync. */
+int hteno_batch_get_time(hteno_batch* b, int i, double* t, long* steps, int* status);
+/* Tile shape in use (tunes first if needed). */
+int hteno_batch_tile(hteno_batch* b, int* tx, int* ty, int* threads);
+const char* hteno_batch_last_error(hteno_batch* b);
 
 /* ---- Tracing: per-kernel CUDA-event timing of hteno_step ---------------------------------- */
 

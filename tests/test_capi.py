@@ -7,6 +7,7 @@ import re
 from pathlib import Path
 
 import numpy as np
+import pytest
 
 REPO = Path(__file__).resolve().parent.parent
 
@@ -74,3 +75,14 @@ def test_initial_data_generators():
     assert s.shape == (3, 10) and s[0, 0] == 1.0 and s[0, -1] == 0.125
     b = ic.gaussian_blobs_shock(64, 64, 1)
     assert b.shape == (4, 64, 64) and b[0].max() > 2.0
+
+
+def test_batch_rejects_unsupported_configs(hteno_lib):
+    """Batches hold mixed-precision FV 2D grids only; configs are checked before any device work."""
+    h = hteno_lib
+    with pytest.raises(h.HtenoError):
+        h.Batch([h.config(dims=2, nx=32, ny=32, precision=0)])
+    with pytest.raises(h.HtenoError):
+        h.Batch([h.config(dims=2, nx=4, ny=32, precision=1)])
+    with pytest.raises(h.HtenoError):
+        h.Batch([h.config(dims=1, nx=32, precision=1)])

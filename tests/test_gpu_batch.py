@@ -1,0 +1,94 @@
+"""Batched independent 2D grids (hteno_batch_*): every instance evolves exactly as the same grid
+run alone through the single-grid mixed path (same tiles arithmetic, same per-instance dt), with
+its own time, step count and stop test."""
+from __future__ import annotations
+
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+SIZES = [(64, 64), (130, 70), (48, 200), (96, 33), (250, 128), (6, 9)]
+
+
+def make_batch(h, sizes, seed0=100, **kw):
+    from hteno import ic
+
+    cfgs = [h.config(dims=2, nx=nx, ny=ny, flux=1, precision=1, **kw) for nx, ny in sizes]
+    states = [ic.four_quadrant(nx, ny, seed0 + k) for k, (nx, ny) in enumerate(sizes)]
+    b = h.Batch(cfgs)
+    for k, q in enumerate(states):
+        b.set_state(k, q)
+    return b, cfgs, states
+
+
+def single(h, cfg, q, nsteps, t_final=float("inf")):
+    with h.Solver(cfg) as s:
+        s.set_state(q)
+        s.step(nsteps, t_final)
+        t, n, _ = s.time()
+        return s.get_state(), t, n
+
+
+def test_batch_matches_single_grids(hteno_lib, cuda):
+    b, cfgs, states = make_batch(hteno_lib, SIZES)
+    with b:
+        b.step(15)
+        for k, (cfg, q) in enumerate(zip(cfgs, states)):
+            want, t_w, n_w = single(hteno_lib, cfg, q, 15)
+            t, n, st = b.time(k)
+            assert n == n_w == 15 and t == t_w and st == 0
+            np.testing.assert_array_equal(b.get_state(k), want)
+
+
+def test_batch_per_instance_time_and_stop(hteno_lib, cuda):
+    """Instances stop independently when they reach t_final; their dts differ."""
+    b, cfgs, states = make_batch(hteno_lib, SIZES[:4], seed0=7)
+    with b:
+        b.step(1000, 0.02)
+        counts = set()
+        for k, (cfg, q) in enumerate(zip(cfgs, states)):
+            want, t_w, n_w = single(hteno_lib, cfg, q, 1000, 0.02)
+            t, n, _ = b.time(k)
+            assert n == n_w and t == t_w == pytest.approx(0.02, rel=1e-14, abs=0)
+            counts.add(n)
+            np.testing.assert_array_equal(b.get_state(k), want)
+        assert len(counts) > 1
+
+
+def test_batch_graph_replay_is_resumable(hteno_lib, cuda):
+    b1, _, _ = make_batch(hteno_lib, SIZES[:3], seed0=3)
+    b2, _, _ = make_batch(hteno_lib, SIZES[:3], seed0=3)
+    with b1, b2:
+        b1.step(7)
+        b2.step(3)
+        b2.step(4)
+        for k in range(3):
+            np.testing.assert_array_equal(b1.get_state(k), b2.get_state(k))
+            assert b1.time(k)[:2] == b2.time(k)[:2]
+
+
+def test_batch_tile_shapes_agree(hteno_lib, cuda):
+    outs = []
+    try:
+        for v in range(6):
+            os.environ["HTENO_FV2D_TILE"] = str(v)
+            b, _, _ = make_batch(hteno_lib, SIZES[:3], seed0=9)
+            with b:
+                assert b.tile()[0] > 0
+                b.step(5)
+                outs.append([b.get_state(k) for k in range(3)])
+    finally:
+        os.environ.pop("HTENO_FV2D_TILE", None)
+    for o in outs[1:]:
+        for a, c in zip(o, outs[0]):
+            np.testing.assert_array_equal(a, c)
+
+
+def test_batch_tuner_picks_a_candidate(hteno_lib, cuda):
+    b, _, _ = make_batch(hteno_lib, SIZES[:2])
+    with b:
+        tx, ty, nt = b.tile()
+        assert (tx, ty, nt) in {(32, 16, 256), (32, 8, 256), (16, 16, 256), (64, 8, 256), (32, 32, 512), (16, 8, 128)}

@@ -104,17 +104,17 @@ def test_fv2d_residual_matches_oracle(hteno_lib, cuda, oracle):
 def test_fv2d_edge_sizes_and_time_clipping(hteno_lib, cuda, oracle):
     """Smallest accepted grid and non-square grids, stopping on t_final mid-run, with both fluxes.
     The reference's HLLC (sound speeds without gamma) drives the 64 x 9 case to negative pressure
-    at step 10 and to NaN later; past that point neither side's numbers mean anything, so that
-    case is compared bit for bit over its first 9 steps and the GPU must flag it."""
+    at step 10, to values beyond 1e35 by step 60 and to NaN later; the two sides stay bit-identical
+    through the non-physical steps (compared over 25 steps here) and the GPU must flag them."""
     from hteno import ic
 
     for flux in (0, 1):
         for nx, ny in ((6, 6), (7, 13), (64, 9)):
             q = ic.four_quadrant(nx, ny, nx * 100 + ny)
             if flux == 1 and (nx, ny) == (64, 9):
-                want, t_o, n_o = oracle.fv2d_run(q, 9, t_final=0.05, flux=flux)
-                got, t_g, n_g = gpu_run2d(hteno_lib, q, 9, t_final=0.05, flux=flux)
-                assert n_g == n_o == 9 and t_g == t_o
+                want, t_o, n_o = oracle.fv2d_run(q, 25, t_final=0.05, flux=flux)
+                got, t_g, n_g = gpu_run2d(hteno_lib, q, 25, t_final=0.05, flux=flux)
+                assert n_g == n_o == 25 and t_g == t_o
                 np.testing.assert_array_equal(got, want)
                 with hteno_lib.Solver(hteno_lib.config(dims=2, nx=nx, ny=ny, flux=flux)) as s:
                     s.set_state(q)

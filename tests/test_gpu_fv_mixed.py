@@ -1,0 +1,144 @@
+"""Mixed-precision FV 2D path (float reconstruction and fluxes, double state and SSP-RK3; one
+fused launch per stage): error against the plain FP64 path, which is bit-identical to the CPU
+oracle, at the same simulated time; independence of the tile shape; conservation; health flags."""
+from __future__ import annotations
+
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+L1_TOL = 1e-4  # L1 density error bound of the mixed path against FP64
+
+
+def run(h, q, nsteps, t_final=1e30, **kw):
+    cfg = h.config(dims=2, nx=q.shape[2], ny=q.shape[1], **kw)
+    with h.Solver(cfg) as s:
+        s.set_state(q)
+        s.step(nsteps, t_final)
+        t, n, _ = s.time()
+        return s.get_state(), t, n, s.status()
+
+
+def smooth_periodic(nx, ny):
+    from hteno import ic
+
+    x = (np.arange(nx) + 0.5) / nx
+    y = (np.arange(ny) + 0.5) / ny
+    X, Y = np.meshgrid(x, y)
+    rho = 1 + 0.2 * np.sin(2 * np.pi * (X + Y))
+    return np.ascontiguousarray(ic.conservative2(rho, 0.5 + 0 * X, -0.3 + 0 * X, 1 + 0 * X))
+
+
+def periodic_box(nx, ny):
+    from hteno import ic
+
+    x = (np.arange(nx) + 0.5) / nx
+    y = (np.arange(ny) + 0.5) / ny
+    X, Y = np.meshgrid(x, y)
+    inside = (np.abs(X - 0.5) < 0.25) & (np.abs(Y - 0.5) < 0.25)
+    return np.ascontiguousarray(ic.conservative2(1.0 + inside, 0.5 + 0 * X, -0.3 + 0 * X, 1.0 + 1.5 * inside))
+
+
+CASES = [
+    dict(flux=1, recon=0, bc=0), dict(flux=0, recon=0, bc=0), dict(flux=1, recon=1, bc=0),
+    dict(flux=0, recon=0, bc=1), dict(flux=1, recon=2, bc=1),
+]
+
+
+@pytest.mark.parametrize("cfg", CASES, ids=lambda c: f"flux{c['flux']}-recon{c['recon']}-bc{c['bc']}")
+def test_mixed_error_against_fp64(hteno_lib, cuda, cfg):
+    from hteno import ic
+
+    nx, ny = 96, 80
+    if cfg["recon"] == 2:
+        q = smooth_periodic(nx, ny)
+    elif cfg["bc"] == 1:
+        q = periodic_box(nx, ny)
+    else:
+        q = ic.four_quadrant(nx, ny, 11)
+    ref, t_ref, _, _ = run(hteno_lib, q, 40, **cfg)
+    got, t_got, n_got, st = run(hteno_lib, q, 1000, t_final=t_ref, precision=1, **cfg)
+    assert t_got == pytest.approx(t_ref, rel=1e-14, abs=0) and st == 0
+    l1 = np.abs(got[0] - ref[0]).mean()
+    assert l1 <= L1_TOL, l1
+    # each conserved variable, relative to its range
+    rng = ref.max(axis=(1, 2)) - ref.min(axis=(1, 2)) + 1e-300
+    assert (np.abs(got - ref).mean(axis=(1, 2)) / rng).max() <= 1e-3
+
+
+def test_mixed_smooth_flow_is_accurate(hteno_lib, cuda):
+    """On a smooth periodic flow the mixed path stays within float rounding of FP64."""
+    q = smooth_periodic(64, 64)
+    ref, t_ref, _, _ = run(hteno_lib, q, 30, flux=1, bc=1)
+    got, _, _, _ = run(hteno_lib, q, 1000, t_final=t_ref, flux=1, bc=1, precision=1)
+    assert np.abs(got - ref).max() <= 1e-5
+
+
+def test_mixed_tile_shapes_agree_bitwise(hteno_lib, cuda):
+    """Every tile shape computes each face from the same data with the same arithmetic, so the
+    results are identical; the grid is not a multiple of any tile."""
+    from hteno import ic
+
+    q = ic.four_quadrant(70, 45, 5)
+    outs = []
+    try:
+        for v in range(6):
+            os.environ["HTENO_FV2D_TILE"] = str(v)
+            outs.append(run(hteno_lib, q, 12, flux=1, precision=1)[0])
+    finally:
+        os.environ.pop("HTENO_FV2D_TILE", None)
+    for o in outs[1:]:
+        np.testing.assert_array_equal(o, outs[0])
+
+
+def test_mixed_periodic_conservation(hteno_lib, cuda):
+    q = periodic_box(128, 96)
+    got, _, _, _ = run(hteno_lib, q, 60, flux=1, bc=1, precision=1)
+    tot0, tot = q.sum(axis=(1, 2)), got.sum(axis=(1, 2))
+    assert (np.abs(tot - tot0) <= 1e-12 * np.abs(q).sum(axis=(1, 2))).all(), tot - tot0
+
+
+def test_mixed_residual_close_to_fp64(hteno_lib, cuda):
+    from hteno import ic
+
+    q = ic.four_quadrant(80, 64, 21)
+    out = {}
+    for prec in (0, 1):
+        with hteno_lib.Solver(hteno_lib.config(dims=2, nx=80, ny=64, flux=1, precision=prec)) as s:
+            dq = cuda.from_numpy(q).cuda()
+            r = cuda.empty_like(dq)
+            s.residual(dq, r)
+            cuda.cuda.synchronize()
+            out[prec] = r.cpu().numpy()
+    d = np.abs(out[1] - out[0]).mean(axis=(1, 2)) / np.abs(out[0]).mean(axis=(1, 2))
+    assert (d <= 1e-3).all(), d
+
+
+def test_mixed_edge_sizes(hteno_lib, cuda):
+    from hteno import ic
+
+    for nx, ny in ((6, 6), (7, 13), (64, 9), (200, 6)):
+        q = ic.four_quadrant(nx, ny, nx * 100 + ny)
+        ref, t_ref, _, _ = run(hteno_lib, q, 8, flux=0)
+        got, t_got, _, _ = run(hteno_lib, q, 1000, t_final=t_ref, flux=0, precision=1)
+        assert t_got == pytest.approx(t_ref, rel=1e-14, abs=0) and np.isfinite(got).all()
+        assert np.abs(got[0] - ref[0]).mean() <= 1e-3
+
+
+def test_mixed_constant_state_is_steady(hteno_lib, cuda):
+    q = np.ascontiguousarray(np.broadcast_to(np.array([1.3, 0.2, -0.4, 2.7])[:, None, None], (4, 20, 24)).copy())
+    got, _, _, st = run(hteno_lib, q, 5, flux=1, precision=1)
+    np.testing.assert_allclose(got, q, rtol=1e-6, atol=1e-6)
+    assert st == 0
+
+
+def test_mixed_nonphysical_state_is_flagged(hteno_lib, cuda):
+    from hteno import ic
+
+    q = ic.four_quadrant(32, 32, 1)
+    q[0, 10, 10] = -0.5
+    _, _, _, st = run(hteno_lib, q, 1, flux=1, precision=1)
+    assert st != 0
