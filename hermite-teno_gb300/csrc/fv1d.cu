@@ -8,6 +8,7 @@
 
 #include "hteno_internal.h"
 #include "parity_math.cuh"
+#include "harvest.cuh"
 
 namespace hteno {
 namespace {
@@ -132,6 +133,36 @@ __global__ void k1_update(Geo1 G, int stage, const T* __restrict__ F, double* __
   if (bad) atomicOr(&st->status, bad);
 }
 
+// Training stencils of the learned classifier (harvest.cuh): every face, 3 characteristic
+// fields, both sides, each kept with probability p.
+__global__ void __launch_bounds__(kThreads) k1_harvest(Geo1 G, const double* __restrict__ q, double p,
+                                                       unsigned long long seed, uint16_t* X, uint8_t* Y,
+                                                       long cap, unsigned long long* count) {
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f > G.nx) return;
+  const int n = G.nx;
+  double qa[3], qb[3], wa[3], wb[3], ha, hb, sa, sb;
+  const int ca = bmap(f - 1, n, G.bc), cb = bmap(f, n, G.bc);
+  for (int v = 0; v < 3; ++v) {
+    qa[v] = q[v * n + ca];
+    qb[v] = q[v * n + cb];
+  }
+  cell_prim1(G.g1, qa, wa, ha, sa);
+  cell_prim1(G.g1, qb, wb, hb, sb);
+  double R[9], L[9], ch[3][6];
+  par::eig1(G.g1, sa, wa[1], ha, sb, wb[1], hb, R, L);
+  for (int m = 0; m < 6; ++m) {
+    const int c = bmap(f - 3 + m, n, G.bc);
+    const double qq[3] = {q[c], q[n + c], q[2 * n + c]};
+    double cc[3];
+    par::mv3(L, qq, cc);
+    for (int r = 0; r < 3; ++r) ch[r][m] = cc[r];
+  }
+  for (int r = 0; r < 3; ++r)
+    harvest::emit_both(ch[r], G.recon == HTENO_RECON_TENO5I, seed, (uint64_t(r) << 40) + uint64_t(f),
+                       p, X, Y, cap, count);
+}
+
 Geo1 geo1_of(const hteno_solver* s) {
   Geo1 G;
   G.nx = s->cfg.nx;
@@ -174,6 +205,14 @@ int fv1d_prepare(hteno_solver* s) {
   const Geo1 G = geo1_of(s);
   k1_init<<<unsigned((G.nx + 127) / 128), 128, 0, s->stream>>>(G, s->q, s->dstate);
   return cuda_error(s, cudaGetLastError(), "k1_init");
+}
+
+int fv1d_harvest(hteno_solver* s, double p, unsigned long long seed, uint16_t* X, uint8_t* Y,
+                 long cap, unsigned long long* count) {
+  const Geo1 G = geo1_of(s);
+  k1_harvest<<<unsigned((G.nx + 1 + kThreads - 1) / kThreads), kThreads, 0, s->stream>>>(
+      G, s->q, p, seed, X, Y, cap, count);
+  return cuda_error(s, cudaGetLastError(), "harvest");
 }
 
 int fv1d_step_async(hteno_solver* s, int nsteps) {

@@ -70,4 +70,10 @@ int fv2d_residual(hteno_solver* s, const double* q, double* rhs) {
   return cuda_error(s, cudaGetLastError(), "fv2d residual launch");
 }
 
+int fv2d_harvest_entry(hteno_solver* s, double p, unsigned long long seed, uint16_t* X, uint8_t* Y,
+                       long cap, unsigned long long* count) {
+  const Geo G = geo_of(s);
+  return fv2d_harvest(s, G, carve<double>(s->work, G.nx, G.ny), p, seed, X, Y, cap, count);
+}
+
 }  // namespace hteno

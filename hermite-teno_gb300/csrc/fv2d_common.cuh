@@ -80,6 +80,15 @@ int fv2d_fused_prepare(hteno_solver* s, const Geo& G, double* scratch);
 void fv2d_fused_step(hteno_solver* s, const Geo& G, double* qc);
 void fv2d_fused_residual(hteno_solver* s, const Geo& G, const double* q, double* rhs);
 const char* fv2d_fused_variant_name(int v);
+// Tensor-core classifier (mlp.cu): route masks of a grid from its state; timeout status.
+int mlp_classify(hteno_mlp* m, const Geo& G, const double* q, uint8_t* mx, uint8_t* my, float thr,
+                 cudaStream_t st);
+int mlp_status(hteno_mlp* m, cudaStream_t st);
+
+// Training stencils of the learned classifier from the current FP64 state (fv2d_fp64.cu).
+int fv2d_harvest(hteno_solver* s, const Geo& G, const Work<double>& W, double p,
+                 unsigned long long seed, uint16_t* X, uint8_t* Y, long cap,
+                 unsigned long long* count);
 
 // Bit-reproducible FP64 path (fv2d_fp64.cu)
 int fv2d_fp64_setup(hteno_solver* s);

@@ -8,6 +8,7 @@
 // (flux difference, SSP-RK3 stage, primitives of the new state, max wave speed on stage 3).
 #include "fv2d_common.cuh"
 #include "parity_math.cuh"
+#include "harvest.cuh"
 
 namespace hteno {
 namespace {
@@ -93,6 +94,45 @@ __global__ void __launch_bounds__(kFaceThreads) kp_faces(Geo G, const double* __
   froe[4 * nface + o] = E.cm;
   froe[5 * nface + o] = E.rcm;
   froe[6 * nface + o] = E.b1;
+}
+
+// Training stencils of the learned classifier from the current state (see harvest.cuh): every
+// face of direction DIR, 4 characteristic fields, both sides, each kept with probability p.
+template <int DIR>
+__global__ void __launch_bounds__(kFaceThreads) kp_harvest(Geo G, const double* __restrict__ q,
+                                                           const double* __restrict__ prim, double p,
+                                                           unsigned long long seed, uint16_t* X,
+                                                           uint8_t* Y, long cap,
+                                                           unsigned long long* count) {
+  const int nf = DIR == 1 ? G.nx + 1 : G.ny + 1;
+  const int nt = DIR == 1 ? G.ny : G.nx;
+  const long idx = blockIdx.x * long(blockDim.x) + threadIdx.x;
+  if (idx >= long(nf) * nt) return;
+  int f, t;
+  if (DIR == 1) { f = int(idx % nf); t = int(idx / nf); }
+  else { t = int(idx % nt); f = int(idx / nt); }
+  const size_t nc = size_t(G.nx) * G.ny;
+  const int ns = DIR == 1 ? G.nx : G.ny;
+  auto cell = [&](int s) -> size_t {
+    const int m = bmap(s, ns, G.bc);
+    return DIR == 1 ? size_t(t) * G.nx + m : size_t(m) * G.nx + t;
+  };
+  const size_t ca = cell(f - 1), cb = cell(f);
+  const par::Eig E = par::eig(G.g1, DIR, prim[3 * nc + ca], prim[ca], prim[nc + ca],
+                              prim[2 * nc + ca], prim[3 * nc + cb], prim[cb], prim[nc + cb],
+                              prim[2 * nc + cb]);
+  double ch[4][6];
+  for (int m = 0; m < 6; ++m) {
+    const size_t c = cell(f - 3 + m);
+    const double qq[4] = {q[c], q[nc + c], q[2 * nc + c], q[3 * nc + c]};
+    double cc[4];
+    par::left(E, DIR, qq, cc);
+    for (int r = 0; r < 4; ++r) ch[r][m] = cc[r];
+  }
+  for (int r = 0; r < 4; ++r) {
+    const uint64_t id = ((uint64_t(DIR) * 4 + r) << 40) + uint64_t(idx);
+    harvest::emit_both(ch[r], G.recon == HTENO_RECON_TENO5I, seed, id, p, X, Y, cap, count);
+  }
 }
 
 template <int DIR>
@@ -256,6 +296,17 @@ void fv2d_fp64_stage(hteno_solver* s, const Geo& G, const Work<double>& W, int s
   kp_update<<<unsigned((nc + 255) / 256), 256, 0, cs>>>(G, stage, W.fx, W.fy, s->q, s->q0,
                                                        W.prim, out, st);
   trace_end(s);
+}
+
+int fv2d_harvest(hteno_solver* s, const Geo& G, const Work<double>& W, double p,
+                 unsigned long long seed, uint16_t* X, uint8_t* Y, long cap,
+                 unsigned long long* count) {
+  const long nxf = long(G.nx + 1) * G.ny, nyf = long(G.ny + 1) * G.nx;
+  kp_harvest<1><<<unsigned((nxf + kFaceThreads - 1) / kFaceThreads), kFaceThreads, 0, s->stream>>>(
+      G, s->q, W.prim, p, seed, X, Y, cap, count);
+  kp_harvest<2><<<unsigned((nyf + kFaceThreads - 1) / kFaceThreads), kFaceThreads, 0, s->stream>>>(
+      G, s->q, W.prim, p, seed, X, Y, cap, count);
+  return cuda_error(s, cudaGetLastError(), "harvest");
 }
 
 // ---- Residual without any device allocation --------------------------------------------------

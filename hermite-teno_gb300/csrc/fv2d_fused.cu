@@ -13,14 +13,14 @@ std::mutex g_mu;
 
 #include "common_kernels.cuh"
 
-template <int TX, int TY, int NT>
+template <int TX, int TY, int NT, bool ROUTE>
 __global__ void __launch_bounds__(NT) k_fused(Geo G, int stage, fused::StageArgs a) {
   if (a.st && a.st->done) return;
   extern __shared__ __align__(16) unsigned char smem[];
   auto& S = *reinterpret_cast<fused::Smem<TX, TY>*>(smem);
   int bad = 0;
-  const double ms = fused::tile_stage<TX, TY, NT>(c_dev, G, blockIdx.x * TX, blockIdx.y * TY,
-                                                  stage, a, S, bad);
+  const double ms = fused::tile_stage<TX, TY, NT, ROUTE>(c_dev, G, blockIdx.x * TX, blockIdx.y * TY,
+                                                         stage, a, S, bad);
   if (stage == 3) {
     block_max_to(ms, &a.st->maxbits);
     if (bad) atomicOr(&a.st->status, bad);
@@ -46,23 +46,31 @@ struct Variant {
   size_t smem;
   const char* name;
   void (*launch)(cudaStream_t, const Geo&, int, const fused::StageArgs&);
+  void (*launch_routed)(cudaStream_t, const Geo&, int, const fused::StageArgs&);
   cudaError_t (*prepare)();
 };
 
-template <int TX, int TY, int NT>
+template <int TX, int TY, int NT, bool ROUTE>
 void launch_v(cudaStream_t cs, const Geo& G, int stage, const fused::StageArgs& a) {
   const dim3 grid(unsigned((G.nx + TX - 1) / TX), unsigned((G.ny + TY - 1) / TY));
-  k_fused<TX, TY, NT><<<grid, NT, fused::smem_bytes<TX, TY>(), cs>>>(G, stage, a);
+  k_fused<TX, TY, NT, ROUTE><<<grid, NT, fused::smem_bytes<TX, TY>(), cs>>>(G, stage, a);
 }
 
 template <int TX, int TY, int NT>
 cudaError_t prepare_v() {
-  return cudaFuncSetAttribute(k_fused<TX, TY, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  cudaError_t e = cudaFuncSetAttribute(k_fused<TX, TY, NT, false>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       int(fused::smem_bytes<TX, TY>()));
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(k_fused<TX, TY, NT, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                               int(fused::smem_bytes<TX, TY>()));
 }
 
-#define HTENO_VARIANT(TX, TY, NT) \
-  { TX, TY, NT, fused::smem_bytes<TX, TY>(), "fused_" #TX "x" #TY "_" #NT, launch_v<TX, TY, NT>, prepare_v<TX, TY, NT> }
+#define HTENO_VARIANT(TX, TY, NT)                                                                \
+  {                                                                                              \
+    TX, TY, NT, fused::smem_bytes<TX, TY>(), "fused_" #TX "x" #TY "_" #NT,                       \
+        launch_v<TX, TY, NT, false>, launch_v<TX, TY, NT, true>, prepare_v<TX, TY, NT>           \
+  }
 
 const Variant kVariants[] = {
     HTENO_VARIANT(32, 16, 256), HTENO_VARIANT(32, 8, 256),  HTENO_VARIANT(16, 16, 256),
@@ -90,7 +98,8 @@ void launch_stage(hteno_solver* s, const Geo& G, int stage, const fused::StageAr
   const int kind = trace_kind(s, stage == 2 || stage == 3 ? "fused_s23" : "fused_s1", bytes,
                               (kFacesFlops + fluxf) * nf + kUpdateFlops * nc);
   trace_begin(s, kind);
-  V.launch(s->stream, G, stage, a);
+  if (a.mx) V.launch_routed(s->stream, G, stage, a);
+  else V.launch(s->stream, G, stage, a);
   trace_end(s);
 }
 
@@ -144,10 +153,29 @@ int fv2d_fused_prepare(hteno_solver* s, const Geo& G, double* scratch) {
 }
 
 // One SSP-RK3 step: q -> q0buf (stage 1), q0buf -> qc (stage 2, base q), qc -> q (stage 3).
+// With a router the classifier first writes the route masks from the step-start state; the
+// three stages use them, and every `audit_every` steps the stages also evaluate the plain TENO
+// cut-off of every stencil and count how the routing compares.
 void fv2d_fused_step(hteno_solver* s, const Geo& G, double* qc) {
-  launch_stage(s, G, 1, fused::StageArgs{s->q, nullptr, s->q0, s->dstate});
-  launch_stage(s, G, 2, fused::StageArgs{s->q0, s->q, qc, s->dstate});
-  launch_stage(s, G, 3, fused::StageArgs{qc, s->q, s->q, s->dstate});
+  fused::StageArgs a1{s->q, nullptr, s->q0, s->dstate}, a2{s->q0, s->q, qc, s->dstate},
+      a3{qc, s->q, s->q, s->dstate};
+  if (s->router) {
+    const int kc = trace_kind(s, "classify", 0.0, 0.0);
+    trace_begin(s, kc);
+    mlp_classify(s->router, G, s->q, s->route_x, s->route_y, s->router_thr, s->stream);
+    trace_end(s);
+    const bool aud = s->audit_every > 0 && s->router_steps % s->audit_every == 0;
+    for (fused::StageArgs* a : {&a1, &a2, &a3}) {
+      a->mx = s->route_x;
+      a->my = s->route_y;
+      a->audit = aud ? s->audit : nullptr;
+    }
+    if (aud) ++s->audits;
+    ++s->router_steps;
+  }
+  launch_stage(s, G, 1, a1);
+  launch_stage(s, G, 2, a2);
+  launch_stage(s, G, 3, a3);
 }
 
 void fv2d_fused_residual(hteno_solver* s, const Geo& G, const double* q, double* rhs) {
@@ -159,3 +187,49 @@ const char* fv2d_fused_variant_name(int v) {
 }
 
 }  // namespace hteno
+
+using namespace hteno;
+
+extern "C" {
+
+int hteno_set_router(hteno_solver* s, hteno_mlp* m, float threshold, int audit_every) {
+  if (!s || !(threshold > 0.f && threshold < 1.f) || audit_every < 0) return HTENO_ERR_INVALID_ARG;
+  if (s->cfg.dims != 2 || s->cfg.scheme != HTENO_SCHEME_FV || s->cfg.precision != HTENO_PREC_MIXED)
+    return set_error(s, HTENO_ERR_UNSUPPORTED, "learned routing runs on the mixed FV 2D path");
+  cudaStreamSynchronize(s->stream);
+  if (!m) {
+    s->router = nullptr;
+    s->launches_per_step = 2 + 3;
+    return HTENO_OK;
+  }
+  if (!s->route_x) {
+    const size_t bx = size_t(s->cfg.nx + 1) * s->cfg.ny, by = size_t(s->cfg.ny + 1) * s->cfg.nx;
+    cudaError_t e = cudaMalloc(&s->route_x, bx);
+    if (e == cudaSuccess) e = cudaMalloc(&s->route_y, by);
+    if (e == cudaSuccess) e = cudaMalloc(&s->audit, 4 * sizeof(unsigned long long));
+    if (e != cudaSuccess) return cuda_error(s, e, "route masks");
+  }
+  cudaMemset(s->audit, 0, 4 * sizeof(unsigned long long));
+  s->router = m;
+  s->router_thr = threshold;
+  s->audit_every = audit_every;
+  s->router_steps = 0;
+  s->audits = 0;
+  s->launches_per_step = 2 + 3 + 1;
+  return HTENO_OK;
+}
+
+int hteno_router_stats(hteno_solver* s, long long* stats) {
+  if (!s || !stats) return HTENO_ERR_INVALID_ARG;
+  if (!s->router || !s->audit) return set_error(s, HTENO_ERR_UNSUPPORTED, "no router set");
+  unsigned long long h[4] = {0, 0, 0, 0};
+  cudaError_t e = cudaMemcpyAsync(h, s->audit, sizeof(h), cudaMemcpyDeviceToHost, s->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+  if (e != cudaSuccess) return cuda_error(s, e, "router stats");
+  for (int k = 0; k < 4; ++k) stats[k] = (long long)h[k];
+  stats[4] = s->audits;
+  const int rc = mlp_status(s->router, s->stream);
+  return rc == HTENO_OK ? HTENO_OK : set_error(s, rc, "classifier tensor-core wait timed out");
+}
+
+}  // extern "C"

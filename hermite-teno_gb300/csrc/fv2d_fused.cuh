@@ -36,6 +36,40 @@ __device__ __forceinline__ int cmap(int i, int n, int bc) {
   return min(max(i, 0), n - 1);
 }
 
+// Conversions between double and float on the integer pipes.  On GB300 the FP64 pipe (which
+// also executes the hardware conversions) runs at 1/64 of the FP32 rate and would bound this
+// kernel; these give the same results as the hardware conversions (round to nearest even) for
+// normal numbers, infinities and NaN, and flush subnormal results to signed zero.
+__device__ __forceinline__ float d2f(double d) {
+  const unsigned hi = unsigned(__double2hiint(d)), lo = unsigned(__double2loint(d));
+  const unsigned s = hi & 0x80000000u;
+  const unsigned eb = (hi >> 20) & 0x7ffu;
+  const int e = int(eb) - 896;  // float biased exponent
+  unsigned m = ((hi & 0xfffffu) << 3) | (lo >> 29);
+  const unsigned rest = lo & 0x1fffffffu;
+  m += (rest > 0x10000000u || (rest == 0x10000000u && (m & 1u))) ? 1u : 0u;
+  if (eb == 0x7ffu) return __uint_as_float(s | 0x7f800000u | (((hi & 0xfffffu) | lo) ? 0x400000u : 0u));
+  if (e <= 0) return __uint_as_float(s);
+  if (e >= 255) return __uint_as_float(s | 0x7f800000u);
+  return __uint_as_float(s | ((unsigned(e) << 23) + m));  // a mantissa carry bumps the exponent
+}
+__device__ __forceinline__ double f2d(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned s = u & 0x80000000u, e = (u >> 23) & 0xffu, m = u & 0x7fffffu;
+  if (e == 0) return __hiloint2double(int(s), 0);
+  const unsigned e2 = e == 255u ? 2047u : e + 896u;
+  return __hiloint2double(int(s | (e2 << 20) | (m >> 3)), int(m << 29));
+}
+
+// SSP-RK3 stage (Schemes_SSPRK.cpp:3-15) in double with fused multiply-adds (the mixed path does
+// not need the reference's rounding sequence, only FP64 accumulation).
+__device__ __forceinline__ double rk_stage(double q0, double qn, double rhs, double dt, int stage) {
+  if (stage == 1) return fma(dt, rhs, q0);
+  const double t = fma(dt, rhs, qn);
+  if (stage == 2) return fma(0.25, t, 0.75 * q0);
+  return fma(2.0 / 3.0, t, q0 * (1.0 / 3.0));
+}
+
 template <int TX, int TY>
 struct Shape {
   static constexpr int W = TX + 6, H = TY + 6;   // loaded cells, halo 3
@@ -60,10 +94,8 @@ constexpr size_t smem_bytes() {
   return sizeof(Smem<TX, TY>);
 }
 
-// One side of teno5 / teno5i with the weight table in shared memory (a per-thread pattern
-// would serialise constant-memory reads).
-__device__ __forceinline__ float teno_side_s(float p0, float p1, float p2, const float* v,
-                                             const float (*tab)[3], bool improved) {
+// Cut-off pattern of one side of teno5 / teno5i (float).
+__device__ __forceinline__ int teno_pat_s(const float* v, bool improved) {
   float SI0, SI1, SI2;
   lagrange_si(v, SI0, SI1, SI2);
   float tau;
@@ -73,8 +105,62 @@ __device__ __forceinline__ float teno_side_s(float p0, float p1, float p2, const
   const float r0 = 1.0f + tau * __frcp_rn(SI0 + ez);
   const float r1 = 1.0f + tau * __frcp_rn(SI1 + ez);
   const float r2 = 1.0f + tau * __frcp_rn(SI2 + ez);
-  const float* w = tab[teno_pattern(r0, r1, r2, float(HTENO_LAG_CT))];
+  return teno_pattern(r0, r1, r2, float(HTENO_LAG_CT));
+}
+
+// One side of teno5 / teno5i with the weight table in shared memory (a per-thread pattern
+// would serialise constant-memory reads).
+__device__ __forceinline__ float teno_side_s(float p0, float p1, float p2, const float* v,
+                                             const float (*tab)[3], bool improved) {
+  const float* w = tab[teno_pat_s(v, improved)];
   return catchnan(p0 * w[0] + p1 * w[1] + p2 * w[2]);
+}
+
+// Audit counters of the learned router: stencils seen, routed to the linear weights, routed
+// although the plain TENO cut-off would not have kept all three candidates, all-smooth by TENO.
+struct RouteCount {
+  int seen = 0, routed = 0, misrouted = 0, smooth = 0;
+};
+
+// recon_s with routing: a side whose route bit is set takes the optimal linear weights (the TENO
+// result when all three cut-off bits are on) without evaluating the smoothness indicators; when
+// auditing, the plain cut-off is evaluated as well and compared.
+__device__ __forceinline__ void recon_routed(const DevConst& C, int kind, const float (*tab)[8][3],
+                                             const float* u, int route, bool audit, RouteCount& rc,
+                                             float& outm, float& outp) {
+  const bool impr = kind == 1;
+  float p0 = C.f_crj[0][1] * u[2] + C.f_crj[1][1] * u[3] + C.f_crj[2][1] * u[4];
+  float p1 = C.f_crj[0][2] * u[1] + C.f_crj[1][2] * u[2] + C.f_crj[2][2] * u[3];
+  float p2 = C.f_crj[0][3] * u[0] + C.f_crj[1][3] * u[1] + C.f_crj[2][3] * u[2];
+  if (kind == 2 || ((route & 1) && !audit)) {
+    outm = p0 * tab[0][7][0] + p1 * tab[0][7][1] + p2 * tab[0][7][2];
+  } else {
+    const int pat = teno_pat_s(u, impr);
+    const float* w = (route & 1) ? tab[0][7] : tab[0][pat];
+    outm = catchnan(p0 * w[0] + p1 * w[1] + p2 * w[2]);
+    if (audit) {
+      rc.seen += 1;
+      rc.smooth += pat == 7;
+      rc.routed += route & 1;
+      rc.misrouted += (route & 1) && pat != 7;
+    }
+  }
+  p0 = C.f_crj[0][0] * u[3] + C.f_crj[1][0] * u[4] + C.f_crj[2][0] * u[5];
+  p1 = C.f_crj[0][1] * u[2] + C.f_crj[1][1] * u[3] + C.f_crj[2][1] * u[4];
+  p2 = C.f_crj[0][2] * u[1] + C.f_crj[1][2] * u[2] + C.f_crj[2][2] * u[3];
+  if (kind == 2 || ((route & 2) && !audit)) {
+    outp = p0 * tab[1][7][0] + p1 * tab[1][7][1] + p2 * tab[1][7][2];
+  } else {
+    const int pat = teno_pat_s(u + 1, impr);
+    const float* w = (route & 2) ? tab[1][7] : tab[1][pat];
+    outp = catchnan(p0 * w[0] + p1 * w[1] + p2 * w[2]);
+    if (audit) {
+      rc.seen += 1;
+      rc.smooth += pat == 7;
+      rc.routed += (route >> 1) & 1;
+      rc.misrouted += (route & 2) && pat != 7;
+    }
+  }
 }
 
 // teno5 (Schemes_Lagrange.cpp:481-511), teno5i (:1235-1263) or linear (:1219-1233):
@@ -99,16 +185,23 @@ struct StageArgs {
   const double* qbase;  // step-start state (stages 2, 3), read pointwise
   double* qout;         // output state (stages 1-3) or residual (stage 0)
   StepState* st;        // dt, health flags, max wave speed; null for stage 0
+  // learned routing (ROUTE kernels): per x face [ny][nx+1] and y face [ny+1][nx] one byte, bit
+  // 2r (2r+1) = left (right) side of characteristic field r takes the linear weights
+  const uint8_t* mx = nullptr;
+  const uint8_t* my = nullptr;
+  unsigned long long* audit = nullptr;  // [4] RouteCount sums when auditing this stage
 };
 
 // The tile at (i0, j0) of grid G.  Every thread of the block must call it (barriers inside).
 // Returns this thread's max wave speed over the cells it updated (stage 3) and ORs health flags
 // into *bad.
-template <int TX, int TY, int NT>
+template <int TX, int TY, int NT, bool ROUTE = false>
 __device__ __forceinline__ double tile_stage(const DevConst& C, const Geo& G, int i0, int j0,
                                              int stage, const StageArgs& a, Smem<TX, TY>& S,
                                              int& bad) {
   typedef Shape<TX, TY> Sh;
+  RouteCount rc;
+  const bool audit = ROUTE && a.audit != nullptr;
   const size_t nc = size_t(G.nx) * G.ny;
   const float g1 = float(G.g1);
   const int tid = threadIdx.x;
@@ -122,8 +215,8 @@ __device__ __forceinline__ double tile_stage(const DevConst& C, const Geo& G, in
     const int y = it / Sh::W, x = it - y * Sh::W;
     const int gi = cmap(i0 - 3 + x, G.nx, G.bc), gj = cmap(j0 - 3 + y, G.ny, G.bc);
     const size_t k = size_t(gj) * G.nx + gi;
-    const float r = float(__ldg(a.qin + k)), mx = float(__ldg(a.qin + nc + k));
-    const float my = float(__ldg(a.qin + 2 * nc + k)), e = float(__ldg(a.qin + 3 * nc + k));
+    const float r = d2f(__ldg(a.qin + k)), mx = d2f(__ldg(a.qin + nc + k));
+    const float my = d2f(__ldg(a.qin + 2 * nc + k)), e = d2f(__ldg(a.qin + 3 * nc + k));
     S.q[0][y][x] = r;
     S.q[1][y][x] = mx;
     S.q[2][y][x] = my;
@@ -155,12 +248,26 @@ __device__ __forceinline__ double tile_stage(const DevConst& C, const Geo& G, in
 #pragma unroll
       for (int r = 0; r < 4; ++r) ch[r][m] = cc[r];
     }
+    if constexpr (ROUTE) {
+      const int gface = min(i0 + f, G.nx);
+      const int route = a.mx[size_t(cmap(j0 - 2 + rr, G.ny, G.bc)) * (G.nx + 1) + gface];
+      const bool own = audit && rr >= 2 && rr < TY + 2 && j0 + rr - 2 < G.ny && i0 + f <= G.nx &&
+                       (f < TX || i0 + f == G.nx);
 #pragma unroll
-    for (int r = 0; r < 4; ++r) {
-      float lo, hi;
-      recon_s(C, G.recon, S.wtab, ch[r], lo, hi);
-      S.c[r][it] = lo;
-      S.c[4 + r][it] = hi;
+      for (int r = 0; r < 4; ++r) {
+        float lo, hi;
+        recon_routed(C, G.recon, S.wtab, ch[r], (route >> (2 * r)) & 3, own, rc, lo, hi);
+        S.c[r][it] = lo;
+        S.c[4 + r][it] = hi;
+      }
+    } else {
+#pragma unroll
+      for (int r = 0; r < 4; ++r) {
+        float lo, hi;
+        recon_s(C, G.recon, S.wtab, ch[r], lo, hi);
+        S.c[r][it] = lo;
+        S.c[4 + r][it] = hi;
+      }
     }
   }
   __syncthreads();
@@ -217,12 +324,26 @@ __device__ __forceinline__ double tile_stage(const DevConst& C, const Geo& G, in
 #pragma unroll
       for (int r = 0; r < 4; ++r) ch[r][m] = cv[r];
     }
+    if constexpr (ROUTE) {
+      const int gface = min(j0 + gg, G.ny);
+      const int route = a.my[size_t(gface) * G.nx + cmap(i0 - 2 + cc, G.nx, G.bc)];
+      const bool own = audit && cc >= 2 && cc < TX + 2 && i0 + cc - 2 < G.nx && j0 + gg <= G.ny &&
+                       (gg < TY || j0 + gg == G.ny);
 #pragma unroll
-    for (int r = 0; r < 4; ++r) {
-      float lo, hi;
-      recon_s(C, G.recon, S.wtab, ch[r], lo, hi);
-      S.c[r][it] = lo;
-      S.c[4 + r][it] = hi;
+      for (int r = 0; r < 4; ++r) {
+        float lo, hi;
+        recon_routed(C, G.recon, S.wtab, ch[r], (route >> (2 * r)) & 3, own, rc, lo, hi);
+        S.c[r][it] = lo;
+        S.c[4 + r][it] = hi;
+      }
+    } else {
+#pragma unroll
+      for (int r = 0; r < 4; ++r) {
+        float lo, hi;
+        recon_s(C, G.recon, S.wtab, ch[r], lo, hi);
+        S.c[r][it] = lo;
+        S.c[4 + r][it] = hi;
+      }
     }
   }
   __syncthreads();
@@ -262,8 +383,9 @@ __device__ __forceinline__ double tile_stage(const DevConst& C, const Geo& G, in
   __syncthreads();
 
   // F: residual and SSP-RK3 stage in double
-  double ms = 0.0;
+  float msf = 0.f;
   const double dt = stage ? a.st->dt : 0.0;
+  const double rdx = 1.0 / G.dx, rdy = 1.0 / G.dy;  // (dfx dy + dfy dx) / (dx dy)
   for (int it = tid; it < TX * TY; it += NT) {
     const int y = it / TX, x = it - y * TX;
     const int gi = i0 + x, gj = j0 + y;
@@ -272,32 +394,44 @@ __device__ __forceinline__ double tile_stage(const DevConst& C, const Geo& G, in
     double qn[4];
 #pragma unroll
     for (int v = 0; v < 4; ++v) {
-      const double dfx = double(S.fx[v][y][x]) - double(S.fx[v][y][x + 1]);
-      const double dfy = double(S.fy[v][y][x]) - double(S.fy[v][y + 1][x]);
-      const double rhs = (dfx * G.dy + dfy * G.dx) / G.area;
+      // float flux differences are exact in double, so the update stays conservative
+      const double dfx = f2d(S.fx[v][y][x]) - f2d(S.fx[v][y][x + 1]);
+      const double dfy = f2d(S.fy[v][y][x]) - f2d(S.fy[v][y + 1][x]);
+      const double rhs = fma(dfx, rdx, dfy * rdy);
       if (stage == 0) {
         a.qout[v * nc + k] = rhs;
       } else {
         const double cur = a.qin[v * nc + k];
         const double base = stage == 1 ? cur : a.qbase[v * nc + k];
-        qn[v] = ssprk3(base, cur, rhs, dt, stage);
+        qn[v] = rk_stage(base, cur, rhs, dt, stage);
         a.qout[v * nc + k] = qn[v];
       }
     }
     if (stage == 3) {
       // pressure in double with a refined float reciprocal of rho (relative error ~1e-14)
-      double ir = double(__frcp_rn(float(qn[0])));
+      double ir = f2d(__frcp_rn(d2f(qn[0])));
       ir = fma(ir, fma(-qn[0], ir, 1.0), ir);
       const double p = (qn[3] - 0.5 * (qn[1] * qn[1] + qn[2] * qn[2]) * ir) * G.g1;
       if (isnan(p)) bad |= 1;
       else if (qn[0] <= 0.0 || p <= 0.0) bad |= 2;
-      const float fr = float(qn[0]), fu = float(qn[1] * ir), fv = float(qn[2] * ir);
-      const float c = sqrtf(fabsf(float(G.gamma) * float(p) / fr));
+      const float fr = d2f(qn[0]), fu = d2f(qn[1] * ir), fv = d2f(qn[2] * ir);
+      const float c = sqrtf(fabsf(float(G.gamma) * d2f(p) / fr));
       const float m = fmaxf(fmaxf(fu - c, fabsf(fu + c)), fmaxf(fv - c, fabsf(fv + c)));
-      ms = fmax(ms, double(m));
+      msf = fmaxf(msf, m);
     }
   }
-  return ms;
+  if constexpr (ROUTE) {
+    if (audit) {
+      int v[4] = {rc.seen, rc.routed, rc.misrouted, rc.smooth};
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
+        if ((threadIdx.x & 31) == 0 && v[k]) atomicAdd(a.audit + k, (unsigned long long)v[k]);
+      }
+    }
+  }
+  return f2d(msf);
 }
 
 }  // namespace fused

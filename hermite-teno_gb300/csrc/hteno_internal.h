@@ -69,6 +69,15 @@ struct hteno_solver {
 
   int launches_per_step = 0;
   int tile_variant = -1;  // mixed FV 2D: tile shape picked by the tuner (-1: not yet)
+  // learned routing (mixed FV 2D): classifier, threshold, audit period, masks, audit sums
+  hteno_mlp* router = nullptr;
+  float router_thr = 0.9f;
+  int audit_every = 0;
+  long router_steps = 0;
+  uint8_t* route_x = nullptr;
+  uint8_t* route_y = nullptr;
+  unsigned long long* audit = nullptr;  // [4]: seen, routed, misrouted, smooth
+  long audits = 0;
   bool strict = false;
   std::string err;
 
@@ -105,6 +114,10 @@ int fv2d_residual(hteno_solver* s, const double* q, double* rhs);
 int fv1d_setup(hteno_solver* s);
 int fv1d_prepare(hteno_solver* s);
 int fv1d_step_async(hteno_solver* s, int nsteps);
+int fv1d_harvest(hteno_solver* s, double p, unsigned long long seed, uint16_t* X, uint8_t* Y,
+                 long cap, unsigned long long* count);
+int fv2d_harvest_entry(hteno_solver* s, double p, unsigned long long seed, uint16_t* X, uint8_t* Y,
+                       long cap, unsigned long long* count);
 
 int hermite2d_setup(hteno_solver* s);
 int hermite2d_prepare(hteno_solver* s);

@@ -1,0 +1,799 @@
+// Learned stencil classifier: a 6 -> 32 -> 32 -> 3 MLP (ReLU, sigmoid outputs) that predicts the
+// three TENO5 cut-off bits of a normalised 6-cell characteristic stencil (cutOff,
+// Schemes_Lagrange.cpp:1141-1149, on the left-biased side; the right side is the mirrored
+// stencil).  BF16 operands, FP32 accumulation, on the tcgen05 tensor cores:
+//
+//   forward   D1 = X W1^T, H1 = relu(D1 + b1); D2 = H1 W2^T, H2 = relu(D2 + b2);
+//             D3 = H2 W3^T, p = sigmoid(D3 + b3)
+//   backward  dZ3 = (p - y) / n;  dH2 = dZ3 W3;  dZ2 = dH2 * [H2 > 0];  dH1 = dZ2 W2;
+//             dZ1 = dH1 * [H1 > 0];  dW3 += dZ3^T H2, dW2 += dZ2^T H1, dW1 += dZ1^T X
+//
+// One CTA of 128 threads owns a 128-row tile (thread = row = tensor-memory lane); weight
+// gradients accumulate in tensor memory across the CTA's tiles and are added to the global
+// gradient at the end.  Adam runs on FP32 master weights; the kernels read BF16 images of them.
+// No reference counterpart: the reference has no learned component (its precedent is the LMPE
+// troubled-cell sensor of FVHermite_System1D.cpp:239-290).
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <random>
+#include <vector>
+
+#include "fv2d_fused.cuh"
+#include "hteno_internal.h"
+#include "mlp_internal.cuh"
+
+struct hteno_mlp;
+
+namespace hteno {
+namespace mlp {
+namespace {
+
+constexpr uint32_t kWaitLimit = 1u << 22;  // polls of an mbarrier before giving up
+
+struct Smem {
+  alignas(128) unsigned char at[128 * 128 * 2];  // A operand of the weight gradients (rows = outputs)
+  alignas(128) unsigned char x[128 * 16 * 2];
+  alignas(128) unsigned char xt[16 * 128 * 2];
+  alignas(128) unsigned char h1[128 * 32 * 2];
+  alignas(128) unsigned char h1t[32 * 128 * 2];
+  alignas(128) unsigned char h2[128 * 32 * 2];
+  alignas(128) unsigned char h2t[32 * 128 * 2];
+  alignas(128) unsigned char dz3[128 * 16 * 2];
+  alignas(128) unsigned char dz2[128 * 32 * 2];
+  alignas(128) unsigned char w1[32 * 16 * 2];
+  alignas(128) unsigned char w2[32 * 32 * 2];
+  alignas(128) unsigned char w3[16 * 32 * 2];
+  alignas(128) unsigned char w3t[32 * 16 * 2];
+  alignas(128) unsigned char w2t[32 * 32 * 2];
+  float b1[32], b2[32], b3[16];
+  float gb1[32], gb2[32], gb3[16];
+  float loss;
+  float stage[16][24];  // classifier: the 6 cells x 4 conserved values of 16 faces
+  alignas(8) uint64_t mbar;
+  uint32_t tmem;
+};
+
+// tensor-memory columns
+constexpr uint32_t C_D1 = 0, C_D2 = 32, C_D3 = 64, C_DH2 = 80, C_DH1 = 112;
+constexpr uint32_t C_GW3 = 144, C_GW2 = 176, C_GW1 = 208, kCols = 256;
+
+__device__ __forceinline__ uint64_t desc_k(const unsigned char* base, int K, int kstep) {
+  return tc::sdesc(tc::smem_u32(base) + uint32_t(kstep) * 256u, 128u, uint32_t(K / 8) * 128u);
+}
+
+// Copies the BF16 weight images into the operand layouts and the FP32 biases.
+__device__ void load_weights(Smem& S, const Weights& W) {
+  const __nv_bfloat16* w1 = reinterpret_cast<const __nv_bfloat16*>(W.w1);
+  for (int e = threadIdx.x; e < 32 * 16; e += blockDim.x) {
+    const int r = e / 16, k = e % 16;
+    *reinterpret_cast<__nv_bfloat16*>(S.w1 + tc::kmaj(r, k, 16)) = w1[e];
+    *reinterpret_cast<__nv_bfloat16*>(S.w3t + tc::kmaj(r, k, 16)) =
+        reinterpret_cast<const __nv_bfloat16*>(W.w3t)[e];
+  }
+  for (int e = threadIdx.x; e < 32 * 32; e += blockDim.x) {
+    const int r = e / 32, k = e % 32;
+    *reinterpret_cast<__nv_bfloat16*>(S.w2 + tc::kmaj(r, k, 32)) =
+        reinterpret_cast<const __nv_bfloat16*>(W.w2)[e];
+    *reinterpret_cast<__nv_bfloat16*>(S.w2t + tc::kmaj(r, k, 32)) =
+        reinterpret_cast<const __nv_bfloat16*>(W.w2t)[e];
+  }
+  for (int e = threadIdx.x; e < 16 * 32; e += blockDim.x) {
+    const int r = e / 32, k = e % 32;
+    *reinterpret_cast<__nv_bfloat16*>(S.w3 + tc::kmaj(r, k, 32)) =
+        reinterpret_cast<const __nv_bfloat16*>(W.w3)[e];
+  }
+  for (int e = threadIdx.x; e < 32; e += blockDim.x) {
+    S.b1[e] = W.b1[e];
+    S.b2[e] = W.b2[e];
+    if (e < 16) S.b3[e] = W.b3[e];
+  }
+}
+
+// Issue (thread 0) after a barrier; every thread then waits for completion.  Returns false on
+// timeout (uniform over the block).
+__device__ __forceinline__ bool wait_mma(Smem& S, uint32_t& phase) {
+  const bool ok = !__syncthreads_or(!tc::mbar_wait(&S.mbar, phase, kWaitLimit));
+  if (ok) phase ^= 1u;  // on timeout `phase` stays the pending one
+  tc::fence_after();
+  return ok;
+}
+
+__device__ __forceinline__ void before_issue() {
+  tc::fence_proxy_async();
+  tc::fence_before();
+  __syncthreads();
+}
+
+__device__ __forceinline__ float rbf(float v) { return __bfloat162float(__float2bfloat16_rn(v)); }
+
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Forward pass of the tile whose inputs are in S.x / S.xt; leaves z1..z3 per thread.
+// keep_t: also store H1^T / H2^T (needed by the weight gradients).
+__device__ __forceinline__ bool forward(Smem& S, uint32_t tbase, uint32_t& phase, float* h1,
+                                        float* h2, float* z3, bool keep_t) {
+  const int row = threadIdx.x;
+  const uint32_t lane_addr = tbase + (uint32_t(threadIdx.x & ~31) << 16);
+  before_issue();
+  if (threadIdx.x == 0) {
+    tc::fence_after();
+    tc::mma_bf16(tbase + C_D1, desc_k(S.x, 16, 0), desc_k(S.w1, 16, 0), tc::idesc_bf16(128, 32), 0);
+    tc::commit(&S.mbar);
+  }
+  if (!wait_mma(S, phase)) return false;
+  tc::tmem_ld16(lane_addr + C_D1, h1);
+  tc::tmem_ld16(lane_addr + C_D1 + 16, h1 + 16);
+#pragma unroll
+  for (int c = 0; c < 32; ++c) {
+    h1[c] = fmaxf(h1[c] + S.b1[c], 0.0f);
+    tc::st_bf16(S.h1, tc::kmaj(row, c, 32), h1[c]);
+    if (keep_t) tc::st_bf16(S.h1t, tc::kmaj(c, row, 128), h1[c]);
+  }
+  before_issue();
+  if (threadIdx.x == 0) {
+    tc::fence_after();
+    for (int s = 0; s < 2; ++s)
+      tc::mma_bf16(tbase + C_D2, desc_k(S.h1, 32, s), desc_k(S.w2, 32, s), tc::idesc_bf16(128, 32), s);
+    tc::commit(&S.mbar);
+  }
+  if (!wait_mma(S, phase)) return false;
+  tc::tmem_ld16(lane_addr + C_D2, h2);
+  tc::tmem_ld16(lane_addr + C_D2 + 16, h2 + 16);
+#pragma unroll
+  for (int c = 0; c < 32; ++c) {
+    h2[c] = fmaxf(h2[c] + S.b2[c], 0.0f);
+    tc::st_bf16(S.h2, tc::kmaj(row, c, 32), h2[c]);
+    if (keep_t) tc::st_bf16(S.h2t, tc::kmaj(c, row, 128), h2[c]);
+  }
+  before_issue();
+  if (threadIdx.x == 0) {
+    tc::fence_after();
+    for (int s = 0; s < 2; ++s)
+      tc::mma_bf16(tbase + C_D3, desc_k(S.h2, 32, s), desc_k(S.w3, 32, s), tc::idesc_bf16(128, 16), s);
+    tc::commit(&S.mbar);
+  }
+  if (!wait_mma(S, phase)) return false;
+  float d3[16];
+  tc::tmem_ld16(lane_addr + C_D3, d3);
+#pragma unroll
+  for (int k = 0; k < 3; ++k) z3[k] = d3[k] + S.b3[k];
+  return true;
+}
+
+// Writes one input row (6 features, bf16 bits) into S.x and S.xt.
+__device__ __forceinline__ void put_input(Smem& S, int row, const uint16_t* f) {
+#pragma unroll
+  for (int k = 0; k < 16; ++k) {
+    const uint16_t bits = k < 6 ? f[k] : uint16_t(0);
+    *reinterpret_cast<uint16_t*>(S.x + tc::kmaj(row, k, 16)) = bits;
+    *reinterpret_cast<uint16_t*>(S.xt + tc::kmaj(k, row, 128)) = bits;
+  }
+}
+
+__device__ void setup(Smem& S, const Weights& W) {
+  for (int e = threadIdx.x; e < int(sizeof(S.at) / 16); e += blockDim.x)
+    reinterpret_cast<uint4*>(S.at)[e] = make_uint4(0, 0, 0, 0);
+  load_weights(S, W);
+  if (threadIdx.x < 32) {
+    S.gb1[threadIdx.x] = 0.f;
+    S.gb2[threadIdx.x] = 0.f;
+    if (threadIdx.x < 16) S.gb3[threadIdx.x] = 0.f;
+  }
+  if (threadIdx.x == 0) {
+    S.loss = 0.f;
+    tc::mbar_init(&S.mbar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (threadIdx.x < 32) tc::tmem_alloc(&S.tmem, kCols);
+  tc::fence_before();
+  __syncthreads();
+  tc::fence_after();
+}
+
+__device__ void teardown(Smem& S, uint32_t tbase) {
+  tc::fence_before();
+  __syncthreads();
+  tc::fence_after();
+  if (threadIdx.x < 32) tc::tmem_dealloc(tbase, kCols);
+}
+
+// Gradient of the mean BCE loss over `n_total` rows, accumulated into G (padded layout).
+__global__ void __launch_bounds__(128) k_train(Weights W, const uint16_t* __restrict__ X,
+                                               const uint8_t* __restrict__ Y, long n, long n_total,
+                                               float* __restrict__ G, float* __restrict__ loss,
+                                               int* __restrict__ err) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  Smem& S = *reinterpret_cast<Smem*>(smem_raw);
+  setup(S, W);
+  const uint32_t tbase = S.tmem;
+  const uint32_t lane_addr = tbase + (uint32_t(threadIdx.x & ~31) << 16);
+  const int row = threadIdx.x, lane = threadIdx.x & 31;
+  const float inv_n = 1.0f / float(n_total);
+  uint32_t phase = 0;
+  bool ok = true;
+  int tiles_done = 0;
+  const long ntiles = (n + 127) / 128;
+  for (long t = blockIdx.x; t < ntiles && ok; t += gridDim.x, ++tiles_done) {
+    const long r = t * 128 + row;
+    const bool valid = r < n;
+    uint16_t f[6] = {0, 0, 0, 0, 0, 0};
+    uint8_t y = 0;
+    if (valid) {
+      const uint4 raw = *reinterpret_cast<const uint4*>(X + r * 8);
+      const uint16_t* p = reinterpret_cast<const uint16_t*>(&raw);
+#pragma unroll
+      for (int k = 0; k < 6; ++k) f[k] = p[k];
+      y = Y[r];
+    }
+    put_input(S, row, f);
+    float h1[32], h2[32], z3[3];
+    ok = forward(S, tbase, phase, h1, h2, z3, true);
+    if (!ok) break;
+    // loss and dZ3
+    float dz3[3], l = 0.f;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const float yk = float((y >> k) & 1);
+      const float z = z3[k];
+      const float pk = 1.0f / (1.0f + __expf(-z));
+      l += fmaxf(z, 0.f) - z * yk + log1pf(__expf(-fabsf(z)));
+      dz3[k] = valid ? (pk - yk) * inv_n : 0.f;
+    }
+    if (!valid) l = 0.f;
+    l = warp_sum(l);
+    if (lane == 0) atomicAdd(&S.loss, l);
+#pragma unroll
+    for (int k = 0; k < 16; ++k) {
+      const float v = k < 3 ? dz3[k] : 0.f;
+      tc::st_bf16(S.dz3, tc::kmaj(row, k, 16), v);
+      tc::st_bf16(S.at, tc::kmaj(k, row, 128), v);
+    }
+    // bias gradients sum the same BF16-rounded error terms the matrix products use
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const float s = warp_sum(rbf(dz3[k]));
+      if (lane == 0) atomicAdd(&S.gb3[k], s);
+    }
+    before_issue();
+    if (threadIdx.x == 0) {
+      tc::fence_after();
+      tc::mma_bf16(tbase + C_DH2, desc_k(S.dz3, 16, 0), desc_k(S.w3t, 16, 0), tc::idesc_bf16(128, 32), 0);
+      for (int s = 0; s < 8; ++s)
+        tc::mma_bf16(tbase + C_GW3, desc_k(S.at, 128, s), desc_k(S.h2t, 128, s), tc::idesc_bf16(128, 32),
+                     (tiles_done > 0 || s > 0) ? 1 : 0);
+      tc::commit(&S.mbar);
+    }
+    if (!(ok = wait_mma(S, phase))) break;
+    // dZ2
+    float d[32];
+    tc::tmem_ld16(lane_addr + C_DH2, d);
+    tc::tmem_ld16(lane_addr + C_DH2 + 16, d + 16);
+#pragma unroll
+    for (int c = 0; c < 32; ++c) {
+      const float v = h2[c] > 0.f ? d[c] : 0.f;
+      tc::st_bf16(S.dz2, tc::kmaj(row, c, 32), v);
+      tc::st_bf16(S.at, tc::kmaj(c, row, 128), v);
+      const float s = warp_sum(rbf(v));
+      if (lane == 0) atomicAdd(&S.gb2[c], s);
+    }
+    before_issue();
+    if (threadIdx.x == 0) {
+      tc::fence_after();
+      for (int s = 0; s < 2; ++s)
+        tc::mma_bf16(tbase + C_DH1, desc_k(S.dz2, 32, s), desc_k(S.w2t, 32, s), tc::idesc_bf16(128, 32), s);
+      for (int s = 0; s < 8; ++s)
+        tc::mma_bf16(tbase + C_GW2, desc_k(S.at, 128, s), desc_k(S.h1t, 128, s), tc::idesc_bf16(128, 32),
+                     (tiles_done > 0 || s > 0) ? 1 : 0);
+      tc::commit(&S.mbar);
+    }
+    if (!(ok = wait_mma(S, phase))) break;
+    // dZ1
+    tc::tmem_ld16(lane_addr + C_DH1, d);
+    tc::tmem_ld16(lane_addr + C_DH1 + 16, d + 16);
+#pragma unroll
+    for (int c = 0; c < 32; ++c) {
+      const float v = h1[c] > 0.f ? d[c] : 0.f;
+      tc::st_bf16(S.at, tc::kmaj(c, row, 128), v);
+      const float s = warp_sum(rbf(v));
+      if (lane == 0) atomicAdd(&S.gb1[c], s);
+    }
+    before_issue();
+    if (threadIdx.x == 0) {
+      tc::fence_after();
+      for (int s = 0; s < 8; ++s)
+        tc::mma_bf16(tbase + C_GW1, desc_k(S.at, 128, s), desc_k(S.xt, 128, s), tc::idesc_bf16(128, 16),
+                     (tiles_done > 0 || s > 0) ? 1 : 0);
+      tc::commit(&S.mbar);
+    }
+    if (!(ok = wait_mma(S, phase))) break;
+  }
+  if (!ok) {
+    if (threadIdx.x == 0) atomicExch(err, 1);
+    // give in-flight MMAs a bounded chance to finish before the columns are released
+    tc::mbar_wait(&S.mbar, phase, kWaitLimit);
+  } else if (tiles_done > 0) {
+    // weight gradients: rows of the accumulators live in lanes 0..31 (warp 0)
+    if (threadIdx.x < 32) {
+      float v[16];
+      for (int h = 0; h < 2; ++h) {
+        tc::tmem_ld16(lane_addr + C_GW3 + 16 * h, v);
+        if (row < 3)
+          for (int c = 0; c < 16; ++c) atomicAdd(&G[kOffW3 + row * 32 + 16 * h + c], v[c]);
+        tc::tmem_ld16(lane_addr + C_GW2 + 16 * h, v);
+        for (int c = 0; c < 16; ++c) atomicAdd(&G[kOffW2 + row * 32 + 16 * h + c], v[c]);
+      }
+      tc::tmem_ld16(lane_addr + C_GW1, v);
+      for (int c = 0; c < 6; ++c) atomicAdd(&G[kOffW1 + row * 16 + c], v[c]);
+      atomicAdd(&G[kOffB1 + row], S.gb1[row]);
+      atomicAdd(&G[kOffB2 + row], S.gb2[row]);
+      if (row < 3) atomicAdd(&G[kOffB3 + row], S.gb3[row]);
+      if (row == 0) atomicAdd(loss, S.loss);
+    }
+  }
+  teardown(S, tbase);
+}
+
+// Probabilities of the three cut-off bits for n rows.
+__global__ void __launch_bounds__(128) k_predict(Weights W, const uint16_t* __restrict__ X, long n,
+                                                 float* __restrict__ P, int* __restrict__ err) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  Smem& S = *reinterpret_cast<Smem*>(smem_raw);
+  setup(S, W);
+  const uint32_t tbase = S.tmem;
+  uint32_t phase = 0;
+  bool ok = true;
+  const long ntiles = (n + 127) / 128;
+  for (long t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+    const long r = t * 128 + threadIdx.x;
+    uint16_t f[6] = {0, 0, 0, 0, 0, 0};
+    if (r < n) {
+      const uint4 raw = *reinterpret_cast<const uint4*>(X + r * 8);
+      const uint16_t* p = reinterpret_cast<const uint16_t*>(&raw);
+      for (int k = 0; k < 6; ++k) f[k] = p[k];
+    }
+    put_input(S, threadIdx.x, f);
+    float h1[32], h2[32], z3[3];
+    ok = forward(S, tbase, phase, h1, h2, z3, false);
+    if (ok && r < n)
+      for (int k = 0; k < 3; ++k) P[r * 3 + k] = 1.0f / (1.0f + __expf(-z3[k]));
+  }
+  if (!ok) {
+    if (threadIdx.x == 0) atomicExch(err, 1);
+    tc::mbar_wait(&S.mbar, phase, kWaitLimit);
+  }
+  teardown(S, tbase);
+}
+
+// Learned routing of a mixed FV 2D grid: every face of both directions, 4 characteristic fields
+// and 2 sides = 8 stencils per face, 16 faces per 128-row tile.  A stencil is routed (bit set)
+// when all three predicted cut-off probabilities exceed `thr`.  The stencils are computed as the
+// fused stage kernel computes them (float primitives and Roe state from the double state).
+__global__ void __launch_bounds__(128) k_classify(Weights W, Geo G, const double* __restrict__ q,
+                                                  uint8_t* __restrict__ mx, uint8_t* __restrict__ my,
+                                                  float zthr, int* __restrict__ err) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  Smem& S = *reinterpret_cast<Smem*>(smem_raw);
+  setup(S, W);
+  const uint32_t tbase = S.tmem;
+  uint32_t phase = 0;
+  bool ok = true;
+  const size_t nc = size_t(G.nx) * G.ny;
+  const long nxf = long(G.nx + 1) * G.ny, nyf = long(G.ny + 1) * G.nx, nf = nxf + nyf;
+  const long chunks = (nf + 15) / 16;
+  const int t = threadIdx.x, lane = t & 31, s8 = t & 7, r = s8 >> 1, side = s8 & 1;
+  const float g1 = float(G.g1);
+  for (long ch = blockIdx.x; ch < chunks && ok; ch += gridDim.x) {
+    const long face = ch * 16 + (t >> 3);
+    const bool valid = face < nf;
+    uint16_t f[6] = {0, 0, 0, 0, 0, 0};
+    int dir = 1, fi = 0, tt = 0;
+    if (valid) {
+      if (face < nxf) {
+        fi = int(face % (G.nx + 1));
+        tt = int(face / (G.nx + 1));
+      } else {
+        const long k = face - nxf;
+        dir = 2;
+        fi = int(k / G.nx);
+        tt = int(k % G.nx);
+      }
+      // the 8 threads of a face load 3 of its 24 state values each
+      for (int j = 0; j < 3; ++j) {
+        const int idx = s8 * 3 + j, m = idx >> 2, v = idx & 3;
+        const int sidx = fused::cmap(fi - 3 + m, dir == 1 ? G.nx : G.ny, G.bc);
+        const size_t k = dir == 1 ? size_t(tt) * G.nx + sidx : size_t(sidx) * G.nx + tt;
+        S.stage[t >> 3][idx] = fused::d2f(__ldg(q + v * nc + k));
+      }
+    }
+    __syncwarp();
+    if (valid) {
+      const float* cq = S.stage[t >> 3];  // cq[4 m + v]
+      float cp[2][4];
+      for (int h = 0; h < 2; ++h) {  // primitives of the two cells of the face
+        const float* c = cq + 4 * (2 + h);
+        const float ir = __frcp_rn(c[0]);
+        const float u = c[1] * ir, v = c[2] * ir;
+        const float p = (c[3] - 0.5f * (c[1] * u + c[2] * v)) * g1;
+        cp[h][0] = u;
+        cp[h][1] = v;
+        cp[h][2] = (c[3] + p) * ir;
+        cp[h][3] = sqrtf(fabsf(c[0]));
+      }
+      const Roe2<float> R = roe2<float>(g1, cp[0][3], cp[0][0], cp[0][1], cp[0][2], cp[1][3],
+                                        cp[1][0], cp[1][1], cp[1][2]);
+      // row r of the left eigenvector matrix (the rows of roe_left)
+      const float vn = dir == 1 ? R.vxm : R.vym, vt = dir == 1 ? R.vym : R.vxm;
+      const float b2 = R.qm * R.b1, s0 = vn * R.rcm, s1 = R.b1 * vn, t2 = 0.5f * R.b1;
+      float a0, an, at, a3;
+      if (r == 0) { a0 = 0.5f * (b2 + s0); an = -0.5f * (s1 + R.rcm); at = -t2 * vt; a3 = t2; }
+      else if (r == 1) { a0 = -vt; an = 0.f; at = 1.f; a3 = 0.f; }
+      else if (r == 2) { a0 = 1.f - b2; an = s1; at = R.b1 * vt; a3 = -R.b1; }
+      else { a0 = 0.5f * (b2 - s0); an = -0.5f * (s1 - R.rcm); at = -t2 * vt; a3 = t2; }
+      float w[6];
+      for (int m = 0; m < 6; ++m) {
+        const float* c = cq + 4 * m;
+        const float qn = dir == 1 ? c[1] : c[2], qt = dir == 1 ? c[2] : c[1];
+        w[side ? 5 - m : m] = a0 * c[0] + an * qn + at * qt + a3 * c[3];
+      }
+      float mean = 0.f, hi = w[0], lo = w[0];
+      for (int m = 0; m < 6; ++m) {
+        mean += w[m];
+        hi = fmaxf(hi, w[m]);
+        lo = fminf(lo, w[m]);
+      }
+      mean *= (1.0f / 6.0f);
+      const float inv = 1.0f / (hi - lo + 1e-30f);
+      for (int m = 0; m < 6; ++m) {
+        const __nv_bfloat16 b = __float2bfloat16_rn((w[m] - mean) * inv);
+        f[m] = *reinterpret_cast<const uint16_t*>(&b);
+      }
+    }
+    put_input(S, t, f);
+    float h1[32], h2[32], z3[3];
+    ok = forward(S, tbase, phase, h1, h2, z3, false);
+    if (!ok) break;
+    const bool smooth = valid && z3[0] > zthr && z3[1] > zthr && z3[2] > zthr;
+    const unsigned b = __ballot_sync(0xffffffffu, smooth);
+    if (valid && s8 == 0) {
+      const uint8_t byte = uint8_t((b >> (lane & ~7)) & 0xffu);
+      if (face < nxf) mx[face] = byte;
+      else my[face - nxf] = byte;
+    }
+  }
+  if (!ok) {
+    if (threadIdx.x == 0) atomicExch(err, 1);
+    tc::mbar_wait(&S.mbar, phase, kWaitLimit);
+  }
+  teardown(S, tbase);
+}
+
+// Adam on the FP32 master parameters (padded layout), then the BF16 images; zeroes G.
+__global__ void k_adam(float* __restrict__ P, float* __restrict__ G, float* __restrict__ M,
+                       float* __restrict__ V, float lr, float b1, float b2, float eps, int t) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= kParams) return;
+  const float g = G[i];
+  const float m = b1 * M[i] + (1.f - b1) * g;
+  const float v = b2 * V[i] + (1.f - b2) * g * g;
+  M[i] = m;
+  V[i] = v;
+  const float mh = m / (1.f - powf(b1, float(t))), vh = v / (1.f - powf(b2, float(t)));
+  P[i] -= lr * mh / (sqrtf(vh) + eps);
+  G[i] = 0.f;
+}
+
+__global__ void k_images(const float* __restrict__ P, Weights W) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  __nv_bfloat16* w1 = reinterpret_cast<__nv_bfloat16*>(W.w1);
+  __nv_bfloat16* w2 = reinterpret_cast<__nv_bfloat16*>(W.w2);
+  __nv_bfloat16* w3 = reinterpret_cast<__nv_bfloat16*>(W.w3);
+  __nv_bfloat16* w3t = reinterpret_cast<__nv_bfloat16*>(W.w3t);
+  __nv_bfloat16* w2t = reinterpret_cast<__nv_bfloat16*>(W.w2t);
+  if (e < 32 * 16) {
+    const int r = e / 16, k = e % 16;
+    w1[e] = __float2bfloat16_rn(k < 6 ? P[kOffW1 + e] : 0.f);
+    w3t[e] = __float2bfloat16_rn(k < 3 ? P[kOffW3 + k * 32 + r] : 0.f);  // W3^T[j][k]
+  }
+  if (e < 32 * 32) {
+    const int r = e / 32, k = e % 32;
+    w2[e] = __float2bfloat16_rn(P[kOffW2 + e]);
+    w2t[e] = __float2bfloat16_rn(P[kOffW2 + k * 32 + r]);  // W2^T[i][j]
+  }
+  if (e < 16 * 32) {
+    const int r = e / 32;
+    w3[e] = __float2bfloat16_rn(r < 3 ? P[kOffW3 + e] : 0.f);
+  }
+  if (e < 32) {
+    W.b1[e] = P[kOffB1 + e];
+    W.b2[e] = P[kOffB2 + e];
+    if (e < 16) W.b3[e] = e < 3 ? P[kOffB3 + e] : 0.f;
+  }
+}
+
+// Converts float rows [n][6] to the bf16 training layout [n][8].
+__global__ void k_pack_inputs(const float* __restrict__ in, uint16_t* __restrict__ out, long n) {
+  const long r = blockIdx.x * long(blockDim.x) + threadIdx.x;
+  if (r >= n) return;
+  for (int k = 0; k < 8; ++k) {
+    const __nv_bfloat16 b = __float2bfloat16_rn(k < 6 ? in[r * 6 + k] : 0.f);
+    out[r * 8 + k] = *reinterpret_cast<const uint16_t*>(&b);
+  }
+}
+
+}  // namespace
+
+size_t smem_bytes() { return sizeof(Smem); }
+
+}  // namespace mlp
+}  // namespace hteno
+
+using namespace hteno;
+using namespace hteno::mlp;
+
+struct hteno_mlp {
+  Weights W{};          // device images
+  float* P = nullptr;   // FP32 master parameters (padded)
+  float* G = nullptr;   // gradient accumulator (padded)
+  float* M = nullptr;   // Adam moments
+  float* V = nullptr;
+  float* loss = nullptr;
+  int* err = nullptr;
+  void* img = nullptr;  // backing store of W
+  int t = 0;            // Adam step
+  int sms = 148;
+  cudaStream_t stream = nullptr;
+  std::string msg;
+};
+
+namespace {
+
+int merr(hteno_mlp* m, cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return HTENO_OK;
+  m->msg = std::string(what) + ": " + cudaGetErrorString(e);
+  return e == cudaErrorMemoryAllocation ? HTENO_ERR_OOM : HTENO_ERR_CUDA;
+}
+
+int set_attr() {
+  static int done = 0;
+  if (done) return HTENO_OK;
+  const int sm = int(mlp::smem_bytes());
+  if (cudaFuncSetAttribute(k_train, cudaFuncAttributeMaxDynamicSharedMemorySize, sm) != cudaSuccess ||
+      cudaFuncSetAttribute(k_predict, cudaFuncAttributeMaxDynamicSharedMemorySize, sm) != cudaSuccess ||
+      cudaFuncSetAttribute(k_classify, cudaFuncAttributeMaxDynamicSharedMemorySize, sm) != cudaSuccess)
+    return HTENO_ERR_CUDA;
+  done = 1;
+  return HTENO_OK;
+}
+
+int check_err(hteno_mlp* m) {
+  int h = 0;
+  cudaError_t e = cudaMemcpyAsync(&h, m->err, sizeof(int), cudaMemcpyDeviceToHost, m->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(m->stream);
+  if (e != cudaSuccess) return merr(m, e, "mlp");
+  if (h) {
+    m->msg = "tensor-core wait timed out";
+    cudaMemsetAsync(m->err, 0, sizeof(int), m->stream);
+    return HTENO_ERR_TIMEOUT;
+  }
+  return HTENO_OK;
+}
+
+// compact public layout <-> padded internal layout
+void to_padded(const float* c, float* p) {
+  std::memset(p, 0, kParams * sizeof(float));
+  for (int j = 0; j < 32; ++j)
+    for (int i = 0; i < 6; ++i) p[kOffW1 + j * 16 + i] = c[j * 6 + i];
+  for (int j = 0; j < 32; ++j) p[kOffB1 + j] = c[192 + j];
+  for (int e = 0; e < 1024; ++e) p[kOffW2 + e] = c[224 + e];
+  for (int j = 0; j < 32; ++j) p[kOffB2 + j] = c[1248 + j];
+  for (int e = 0; e < 96; ++e) p[kOffW3 + e] = c[1280 + e];
+  for (int k = 0; k < 3; ++k) p[kOffB3 + k] = c[1376 + k];
+}
+void from_padded(const float* p, float* c) {
+  for (int j = 0; j < 32; ++j)
+    for (int i = 0; i < 6; ++i) c[j * 6 + i] = p[kOffW1 + j * 16 + i];
+  for (int j = 0; j < 32; ++j) c[192 + j] = p[kOffB1 + j];
+  for (int e = 0; e < 1024; ++e) c[224 + e] = p[kOffW2 + e];
+  for (int j = 0; j < 32; ++j) c[1248 + j] = p[kOffB2 + j];
+  for (int e = 0; e < 96; ++e) c[1280 + e] = p[kOffW3 + e];
+  for (int k = 0; k < 3; ++k) c[1376 + k] = p[kOffB3 + k];
+}
+
+int refresh_images(hteno_mlp* m) {
+  k_images<<<4, 256, 0, m->stream>>>(m->P, m->W);
+  return merr(m, cudaGetLastError(), "weight images");
+}
+
+}  // namespace
+
+namespace hteno {
+
+// Route masks of a mixed FV 2D grid from its current state (see k_classify).
+int mlp_classify(hteno_mlp* m, const Geo& G, const double* q, uint8_t* mx, uint8_t* my, float thr,
+                 cudaStream_t st) {
+  const long nf = long(G.nx + 1) * G.ny + long(G.ny + 1) * G.nx;
+  const long chunks = (nf + 15) / 16;
+  const int grid = int(std::min<long>(chunks, 2L * m->sms));
+  const float zthr = std::log(thr / (1.0f - thr));  // sigmoid(z) > thr  <=>  z > logit(thr)
+  k_classify<<<grid, 128, mlp::smem_bytes(), st>>>(m->W, G, q, mx, my, zthr, m->err);
+  return cudaGetLastError() == cudaSuccess ? HTENO_OK : HTENO_ERR_CUDA;
+}
+
+int mlp_status(hteno_mlp* m, cudaStream_t st) {
+  int h = 0;
+  if (cudaMemcpyAsync(&h, m->err, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaStreamSynchronize(st) != cudaSuccess)
+    return HTENO_ERR_CUDA;
+  return h ? HTENO_ERR_TIMEOUT : HTENO_OK;
+}
+
+}  // namespace hteno
+
+extern "C" {
+
+int hteno_mlp_create(unsigned long long seed, hteno_mlp** out) {
+  if (!out) return HTENO_ERR_INVALID_ARG;
+  *out = nullptr;
+  hteno_mlp* m = new (std::nothrow) hteno_mlp();
+  if (!m) return HTENO_ERR_OOM;
+  auto fail = [&](int code) {
+    cudaFree(m->P); cudaFree(m->G); cudaFree(m->M); cudaFree(m->V); cudaFree(m->loss);
+    cudaFree(m->err); cudaFree(m->img);
+    if (m->stream) cudaStreamDestroy(m->stream);
+    delete m;
+    return code;
+  };
+  if (set_attr() != HTENO_OK) return fail(HTENO_ERR_CUDA);
+  if (cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking) != cudaSuccess) return fail(HTENO_ERR_CUDA);
+  const size_t pb = kParams * sizeof(float);
+  if (cudaMalloc(&m->P, pb) || cudaMalloc(&m->G, pb) || cudaMalloc(&m->M, pb) || cudaMalloc(&m->V, pb) ||
+      cudaMalloc(&m->loss, sizeof(float)) || cudaMalloc(&m->err, sizeof(int)) ||
+      cudaMalloc(&m->img, kImageBytes))
+    return fail(HTENO_ERR_OOM);
+  char* b = static_cast<char*>(m->img);
+  m->W.w1 = b; m->W.w2 = b + 1024; m->W.w3 = b + 3072; m->W.w3t = b + 4096; m->W.w2t = b + 5120;
+  m->W.b1 = reinterpret_cast<float*>(b + 7168);
+  m->W.b2 = m->W.b1 + 32;
+  m->W.b3 = m->W.b2 + 32;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&m->sms, cudaDevAttrMultiProcessorCount, dev);
+  // He-uniform initialisation of the weights, zero biases
+  std::mt19937_64 rng(seed);
+  std::vector<float> c(kPublicParams, 0.f), p(kParams);
+  auto uni = [&](float a) { return float((double(rng() >> 11) * 0x1.0p-53 * 2.0 - 1.0) * a); };
+  for (int e = 0; e < 192; ++e) c[e] = uni(std::sqrt(6.f / 6.f));
+  for (int e = 0; e < 1024; ++e) c[224 + e] = uni(std::sqrt(6.f / 32.f));
+  for (int e = 0; e < 96; ++e) c[1280 + e] = uni(std::sqrt(6.f / 32.f));
+  to_padded(c.data(), p.data());
+  if (cudaMemcpy(m->P, p.data(), pb, cudaMemcpyHostToDevice) || cudaMemset(m->G, 0, pb) ||
+      cudaMemset(m->M, 0, pb) || cudaMemset(m->V, 0, pb) || cudaMemset(m->err, 0, sizeof(int)) ||
+      cudaMemset(m->img, 0, kImageBytes))
+    return fail(HTENO_ERR_CUDA);
+  if (refresh_images(m) != HTENO_OK || cudaStreamSynchronize(m->stream) != cudaSuccess)
+    return fail(HTENO_ERR_CUDA);
+  *out = m;
+  return HTENO_OK;
+}
+
+int hteno_mlp_destroy(hteno_mlp* m) {
+  if (!m) return HTENO_ERR_INVALID_ARG;
+  cudaStreamSynchronize(m->stream);
+  cudaFree(m->P); cudaFree(m->G); cudaFree(m->M); cudaFree(m->V); cudaFree(m->loss);
+  cudaFree(m->err); cudaFree(m->img);
+  cudaStreamDestroy(m->stream);
+  delete m;
+  return HTENO_OK;
+}
+
+int hteno_mlp_num_params(void) { return kPublicParams; }
+
+int hteno_mlp_set_params(hteno_mlp* m, const float* params) {
+  if (!m || !params) return HTENO_ERR_INVALID_ARG;
+  std::vector<float> p(kParams);
+  to_padded(params, p.data());
+  cudaError_t e = cudaMemcpyAsync(m->P, p.data(), kParams * sizeof(float), cudaMemcpyHostToDevice, m->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(m->stream);
+  if (e != cudaSuccess) return merr(m, e, "set params");
+  m->t = 0;
+  cudaMemsetAsync(m->M, 0, kParams * sizeof(float), m->stream);
+  cudaMemsetAsync(m->V, 0, kParams * sizeof(float), m->stream);
+  const int rc = refresh_images(m);
+  return rc ? rc : merr(m, cudaStreamSynchronize(m->stream), "set params");
+}
+
+int hteno_mlp_get_params(hteno_mlp* m, float* params) {
+  if (!m || !params) return HTENO_ERR_INVALID_ARG;
+  std::vector<float> p(kParams);
+  cudaError_t e = cudaMemcpyAsync(p.data(), m->P, kParams * sizeof(float), cudaMemcpyDeviceToHost, m->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(m->stream);
+  if (e != cudaSuccess) return merr(m, e, "get params");
+  from_padded(p.data(), params);
+  return HTENO_OK;
+}
+
+// Gradient of the mean BCE loss over n rows (x: device bf16 [n][8], y: device u8 [n]); grads in
+// the public layout (host), *loss = mean loss.
+int hteno_mlp_grad(hteno_mlp* m, const uint16_t* x, const uint8_t* y, long n, float* grads, float* loss) {
+  if (!m || !x || !y || n <= 0 || !grads) return HTENO_ERR_INVALID_ARG;
+  cudaMemsetAsync(m->G, 0, kParams * sizeof(float), m->stream);
+  cudaMemsetAsync(m->loss, 0, sizeof(float), m->stream);
+  const long tiles = (n + 127) / 128;
+  const int grid = int(std::min<long>(tiles, 2L * m->sms));
+  k_train<<<grid, 128, mlp::smem_bytes(), m->stream>>>(m->W, x, y, n, n, m->G, m->loss, m->err);
+  int rc = merr(m, cudaGetLastError(), "k_train");
+  if (rc) return rc;
+  rc = check_err(m);
+  if (rc) return rc;
+  std::vector<float> g(kParams);
+  float l = 0.f;
+  cudaError_t e = cudaMemcpyAsync(g.data(), m->G, kParams * sizeof(float), cudaMemcpyDeviceToHost, m->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&l, m->loss, sizeof(float), cudaMemcpyDeviceToHost, m->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(m->stream);
+  if (e != cudaSuccess) return merr(m, e, "grad copy");
+  from_padded(g.data(), grads);
+  if (loss) *loss = l / float(n);
+  cudaMemsetAsync(m->G, 0, kParams * sizeof(float), m->stream);
+  return HTENO_OK;
+}
+
+// Mini-batch Adam over the n rows for `epochs` passes (batches are contiguous slices; shuffle the
+// data beforehand).  *loss receives the mean loss of the last epoch.
+int hteno_mlp_train(hteno_mlp* m, const uint16_t* x, const uint8_t* y, long n, int epochs, long batch,
+                    float lr, float* loss) {
+  if (!m || !x || !y || n <= 0 || epochs < 0 || batch <= 0 || !(lr > 0.f)) return HTENO_ERR_INVALID_ARG;
+  float last = 0.f;
+  for (int ep = 0; ep < epochs; ++ep) {
+    cudaMemsetAsync(m->loss, 0, sizeof(float), m->stream);
+    for (long off = 0; off < n; off += batch) {
+      const long nb = std::min(batch, n - off);
+      const long tiles = (nb + 127) / 128;
+      const int grid = int(std::min<long>(tiles, 2L * m->sms));
+      k_train<<<grid, 128, mlp::smem_bytes(), m->stream>>>(m->W, x + off * 8, y + off, nb, nb, m->G,
+                                                           m->loss, m->err);
+      ++m->t;
+      k_adam<<<(kParams + 255) / 256, 256, 0, m->stream>>>(m->P, m->G, m->M, m->V, lr, 0.9f, 0.999f,
+                                                           1e-8f, m->t);
+      k_images<<<4, 256, 0, m->stream>>>(m->P, m->W);
+    }
+    int rc = merr(m, cudaGetLastError(), "train launch");
+    if (rc) return rc;
+    rc = check_err(m);
+    if (rc) return rc;
+    float l = 0.f;
+    cudaMemcpy(&l, m->loss, sizeof(float), cudaMemcpyDeviceToHost);
+    last = l / float(n);
+  }
+  if (loss) *loss = last;
+  return HTENO_OK;
+}
+
+// Probabilities of the three cut-off bits: x device bf16 [n][8] -> p device float [n][3].
+int hteno_mlp_predict(hteno_mlp* m, const uint16_t* x, long n, float* p) {
+  if (!m || !x || n <= 0 || !p) return HTENO_ERR_INVALID_ARG;
+  const long tiles = (n + 127) / 128;
+  const int grid = int(std::min<long>(tiles, 2L * m->sms));
+  k_predict<<<grid, 128, mlp::smem_bytes(), m->stream>>>(m->W, x, n, p, m->err);
+  const int rc = merr(m, cudaGetLastError(), "k_predict");
+  return rc ? rc : check_err(m);
+}
+
+// float [n][6] (device) -> bf16 training rows [n][8] (device).
+int hteno_mlp_pack(hteno_mlp* m, const float* in, uint16_t* out, long n) {
+  if (!m || !in || !out || n <= 0) return HTENO_ERR_INVALID_ARG;
+  k_pack_inputs<<<unsigned((n + 255) / 256), 256, 0, m->stream>>>(in, out, n);
+  const int rc = merr(m, cudaGetLastError(), "pack");
+  return rc ? rc : merr(m, cudaStreamSynchronize(m->stream), "pack");
+}
+
+const char* hteno_mlp_last_error(hteno_mlp* m) { return m ? m->msg.c_str() : "null handle"; }
+
+}  // extern "C"

@@ -101,6 +101,9 @@ int copy_out(hteno_solver* s, double* dst, const double* src, size_t n, int wher
 }
 
 void release(hteno_solver* s) {
+  cudaFree(s->route_x);
+  cudaFree(s->route_y);
+  cudaFree(s->audit);
   cudaFree(s->q);
   cudaFree(s->q0);
   cudaFree(s->v);
@@ -355,6 +358,30 @@ int hteno_launches_per_step(hteno_solver* s, int* launches) {
   if (!s || !launches) return HTENO_ERR_INVALID_ARG;
   *launches = s->launches_per_step;
   return HTENO_OK;
+}
+
+int hteno_harvest(hteno_solver* s, double keep, unsigned long long seed, unsigned short* x,
+                  unsigned char* y, long capacity, long* count) {
+  if (!s || !x || !y || capacity < 0 || !(keep >= 0.0) || keep > 1.0 || !count)
+    return HTENO_ERR_INVALID_ARG;
+  if (is_hermite(s) || s->cfg.precision != HTENO_PREC_FP64)
+    return set_error(s, HTENO_ERR_UNSUPPORTED, "stencils are recorded by the plain FP64 FV solvers");
+  unsigned long long* dcount = nullptr;
+  cudaError_t e = cudaMallocAsync(&dcount, sizeof(unsigned long long), s->stream);
+  if (e != cudaSuccess) return cuda_error(s, e, "harvest counter");
+  cudaMemsetAsync(dcount, 0, sizeof(unsigned long long), s->stream);
+  int rc = s->cfg.dims == 2 ? fv2d_harvest_entry(s, keep, seed, x, y, capacity, dcount)
+                            : fv1d_harvest(s, keep, seed, x, y, capacity, dcount);
+  unsigned long long h = 0;
+  if (rc == HTENO_OK) {
+    e = cudaMemcpyAsync(&h, dcount, sizeof(h), cudaMemcpyDeviceToHost, s->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    rc = cuda_error(s, e, "harvest count");
+  }
+  cudaFreeAsync(dcount, s->stream);
+  cudaStreamSynchronize(s->stream);
+  *count = long(h);
+  return rc;
 }
 
 const char* hteno_last_error(hteno_solver* s) { return s ? s->err.c_str() : "null handle"; }

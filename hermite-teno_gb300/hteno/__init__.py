@@ -108,6 +108,19 @@ def lib() -> ctypes.CDLL:
         L.hteno_batch_tile.argtypes = [vp, ctypes.POINTER(i), ctypes.POINTER(i), ctypes.POINTER(i)]
         L.hteno_batch_last_error.restype = ctypes.c_char_p
         L.hteno_batch_last_error.argtypes = [vp]
+        L.hteno_set_router.argtypes = [vp, vp, ctypes.c_float, i]
+        L.hteno_router_stats.argtypes = [vp, ctypes.POINTER(ctypes.c_longlong)]
+        L.hteno_harvest.argtypes = [vp, d, ctypes.c_ulonglong, vp, vp, l, ctypes.POINTER(l)]
+        L.hteno_mlp_create.argtypes = [ctypes.c_ulonglong, ctypes.POINTER(vp)]
+        L.hteno_mlp_destroy.argtypes = [vp]
+        L.hteno_mlp_set_params.argtypes = [vp, vp]
+        L.hteno_mlp_get_params.argtypes = [vp, vp]
+        L.hteno_mlp_grad.argtypes = [vp, vp, vp, l, vp, vp]
+        L.hteno_mlp_train.argtypes = [vp, vp, vp, l, i, l, ctypes.c_float, vp]
+        L.hteno_mlp_predict.argtypes = [vp, vp, l, vp]
+        L.hteno_mlp_pack.argtypes = [vp, vp, vp, l]
+        L.hteno_mlp_last_error.restype = ctypes.c_char_p
+        L.hteno_mlp_last_error.argtypes = [vp]
         _lib = L
     return _lib
 
@@ -219,6 +232,26 @@ class Solver:
     def set_stream(self, stream_ptr: int) -> None:
         _check(lib().hteno_set_stream(self.h, ctypes.c_void_p(stream_ptr)), self.h)
 
+    def harvest(self, keep: float, seed: int, x, y) -> int:
+        """Training rows of the learned classifier from the current state into the CUDA tensors
+        x (int16 [cap, 8], BF16 bits) and y (uint8 [cap]); returns the number offered."""
+        n = ctypes.c_long()
+        _check(lib().hteno_harvest(self.h, float(keep), int(seed), x.data_ptr(), y.data_ptr(),
+                                   x.shape[0], ctypes.byref(n)), self.h)
+        return n.value
+
+    def set_router(self, mlp, threshold: float = 0.9, audit_every: int = 0) -> None:
+        """Learned routing (mixed FV 2D): stencils the classifier marks confidently smooth take
+        the linear weights; `mlp` None switches it off.  Keep `mlp` alive meanwhile."""
+        self._router = mlp
+        _check(lib().hteno_set_router(self.h, mlp.h if mlp is not None else None, float(threshold),
+                                      int(audit_every)), self.h)
+
+    def router_stats(self) -> dict:
+        a = (ctypes.c_longlong * 5)()
+        _check(lib().hteno_router_stats(self.h, a), self.h)
+        return {"seen": a[0], "routed": a[1], "misrouted": a[2], "smooth": a[3], "audits": a[4]}
+
     def residual(self, q_dev, rhs_dev) -> None:
         _check(lib().hteno_residual(self.h, _ptr(q_dev)[0], _ptr(rhs_dev)[0]), self.h)
 
@@ -290,6 +323,71 @@ class Batch:
         tx, ty, nt = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
         self._check(lib().hteno_batch_tile(self.h, ctypes.byref(tx), ctypes.byref(ty), ctypes.byref(nt)))
         return tx.value, ty.value, nt.value
+
+
+class Mlp:
+    """The learned stencil classifier (6 -> 32 -> 32 -> 3, BF16 on the tensor cores).  Inputs and
+    labels are CUDA tensors (torch): x uint16/int16 [n, 8] BF16 bits, y uint8 [n]."""
+
+    def __init__(self, seed: int = 0):
+        h = ctypes.c_void_p()
+        rc = lib().hteno_mlp_create(seed, ctypes.byref(h))
+        if rc != 0:
+            raise HtenoError(rc, "mlp create")
+        self.h = h
+        self.nparams = lib().hteno_mlp_num_params()
+
+    def _check(self, rc):
+        if rc != 0:
+            raise HtenoError(rc, lib().hteno_mlp_last_error(self.h).decode())
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().hteno_mlp_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def params(self) -> np.ndarray:
+        out = np.empty(self.nparams, dtype=np.float32)
+        self._check(lib().hteno_mlp_get_params(self.h, out.ctypes.data))
+        return out
+
+    def set_params(self, p) -> None:
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        assert p.size == self.nparams
+        self._check(lib().hteno_mlp_set_params(self.h, p.ctypes.data))
+
+    def grad(self, x, y):
+        g = np.empty(self.nparams, dtype=np.float32)
+        loss = ctypes.c_float()
+        self._check(lib().hteno_mlp_grad(self.h, x.data_ptr(), y.data_ptr(), x.shape[0], g.ctypes.data,
+                                         ctypes.byref(loss)))
+        return g, loss.value
+
+    def train(self, x, y, epochs: int, batch: int, lr: float) -> float:
+        loss = ctypes.c_float()
+        self._check(lib().hteno_mlp_train(self.h, x.data_ptr(), y.data_ptr(), x.shape[0], epochs, batch,
+                                          ctypes.c_float(lr), ctypes.byref(loss)))
+        return loss.value
+
+    def predict(self, x, out):
+        self._check(lib().hteno_mlp_predict(self.h, x.data_ptr(), x.shape[0], out.data_ptr()))
+        return out
+
+    def pack(self, xf, out):
+        self._check(lib().hteno_mlp_pack(self.h, xf.data_ptr(), out.data_ptr(), xf.shape[0]))
+        return out
 
 
 def measure_fma_peak(kind: int) -> float:

@@ -188,6 +188,57 @@ int hteno_batch_get_time(hteno_batch* b, int i, double* t, long* steps, int* sta
 int hteno_batch_tile(hteno_batch* b, int* tx, int* ty, int* threads);
 const char* hteno_batch_last_error(hteno_batch* b);
 
+/* ---- Learned stencil classifier (tensor cores) -------------------------------------------- */
+
+/* A 6 -> 32 -> 32 -> 3 MLP (ReLU hidden layers, sigmoid outputs) predicting the three TENO5
+ * cut-off bits (cutOff, Schemes_Lagrange.cpp:1141-1149) of the left-biased side of a normalised
+ * 6-cell characteristic stencil (u - mean) / (max - min + 1e-30); the right side is the mirrored
+ * stencil.  BF16 weights and activations, FP32 accumulation, tcgen05 tensor cores for inference
+ * and training (forward, backward, weight gradients); Adam on FP32 master weights.  No
+ * reference counterpart (the reference's precedent for a cell sensor is the LMPE flag of
+ * FVHermite_System1D.cpp:239-290).
+ * Parameter vector (hteno_mlp_num_params() floats): W1 [32][6], b1 [32], W2 [32][32], b2 [32],
+ * W3 [3][32], b3 [3]; W[out][in].  Inputs: device BF16 rows [n][8] (6 features, 2 zeros);
+ * labels: device bytes [n], bit k = cut-off bit k. */
+typedef struct hteno_mlp hteno_mlp;
+int hteno_mlp_create(unsigned long long seed, hteno_mlp** out);
+int hteno_mlp_destroy(hteno_mlp* m);
+int hteno_mlp_num_params(void);
+int hteno_mlp_set_params(hteno_mlp* m, const float* params); /* host */
+int hteno_mlp_get_params(hteno_mlp* m, float* params);       /* host */
+/* Records training rows from the current state of a plain FP64 FV solver (2D or 1D): for
+ * every face, characteristic field and side (the right side as the mirrored stencil), kept with
+ * probability `keep` (deterministic in `seed`), the normalised 6-cell characteristic stencil the
+ * reconstruction sees (x, BF16 [capacity][8], device) and the cut-off bits the plain solver
+ * decides for it (y [capacity], device).  *count = rows offered (only the first `capacity` are
+ * written). */
+int hteno_harvest(hteno_solver* s, double keep, unsigned long long seed, unsigned short* x,
+                  unsigned char* y, long capacity, long* count);
+/* Gradient (host, parameter layout) and mean loss of the mean binary cross-entropy over n rows. */
+int hteno_mlp_grad(hteno_mlp* m, const unsigned short* x, const unsigned char* y, long n,
+                   float* grads, float* loss);
+/* Mini-batch Adam, `epochs` passes over the rows in order; *loss = mean loss of the last pass. */
+int hteno_mlp_train(hteno_mlp* m, const unsigned short* x, const unsigned char* y, long n,
+                    int epochs, long batch, float lr, float* loss);
+/* p [n][3] (device): probabilities of the three cut-off bits. */
+int hteno_mlp_predict(hteno_mlp* m, const unsigned short* x, long n, float* p);
+/* float rows [n][6] (device) -> BF16 rows [n][8] (device). */
+int hteno_mlp_pack(hteno_mlp* m, const float* in, unsigned short* out, long n);
+const char* hteno_mlp_last_error(hteno_mlp* m);
+
+/* Learned routing of a mixed-precision FV 2D solver: before every step the classifier marks,
+ * from the step-start state, each (face, field, side) stencil whose three predicted cut-off
+ * probabilities all exceed `threshold`; the three stages of that step reconstruct those with the
+ * optimal linear weights (Schemes::Lagrange::linear, Schemes_Lagrange.cpp:1219-1233, the TENO5
+ * result when all three candidates are kept) and skip the nonlinear weights; every other stencil
+ * takes full TENO.  Every `audit_every` steps (0: never) the stages also evaluate the plain TENO
+ * cut-off of every stencil and count the routing errors.  m = NULL switches routing off; the
+ * classifier must outlive its use by the solver. */
+int hteno_set_router(hteno_solver* s, hteno_mlp* m, float threshold, int audit_every);
+/* stats[5]: audited stencils, routed, misrouted (routed though plain TENO cut a candidate),
+ * all-smooth by plain TENO, number of audited steps.  Also reports a classifier timeout. */
+int hteno_router_stats(hteno_solver* s, long long* stats);
+
 /* ---- Tracing: per-kernel CUDA-event timing of hteno_step ---------------------------------- */
 
 /* When enabled, every kernel launch of hteno_step[_async] is bracketed by CUDA events on the

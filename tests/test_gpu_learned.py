@@ -1,0 +1,146 @@
+"""Learned routing end to end: the plain solver records (stencil, TENO cut-off) rows, the tensor-
+core MLP trains on them, and a mixed-precision solver routes confidently smooth stencils to the
+linear weights.  Checked: the recorded labels agree with the cut-off decided on the recorded
+stencils; a router that routes everything (nothing) reproduces the linear (plain TENO) mixed
+solver bit for bit; the audit counts; and what the trained network gains."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def teno5_pattern(v):
+    """Cut-off bits of the left-biased TENO5 side (cutOff, Schemes_Lagrange.cpp:1141-1149) for rows
+    v [n, >=5], float64 (scale-invariant up to the 1e-40 offset)."""
+    c0 = v[:, 2] - 2 * v[:, 3] + v[:, 4]
+    b0 = (3 * v[:, 2] - 4 * v[:, 3] + v[:, 4]) / 2
+    c1 = v[:, 1] - 2 * v[:, 2] + v[:, 3]
+    b1 = (v[:, 1] - v[:, 3]) / 2
+    c2 = v[:, 0] - 2 * v[:, 1] + v[:, 2]
+    b2 = (v[:, 0] - 4 * v[:, 1] + 3 * v[:, 2]) / 2
+    si = np.stack([b * b + 13 / 12 * c * c for b, c in ((b0, c0), (b1, c1), (b2, c2))], axis=1)
+    u = v
+    b35 = (u[:, 4] * (6908 * u[:, 4] - 51001 * u[:, 3] + 67923 * u[:, 2] - 38947 * u[:, 1] + 8209 * u[:, 0])
+           + u[:, 3] * (104963 * u[:, 3] - 299076 * u[:, 2] + 179098 * u[:, 1] - 38947 * u[:, 0])
+           + u[:, 2] * (231153 * u[:, 2] - 299076 * u[:, 1] + 67923 * u[:, 0])
+           + u[:, 1] * (104963 * u[:, 1] - 51001 * u[:, 0]) + 6908 * u[:, 0] ** 2) / 5040
+    tau = np.abs(b35 - (si[:, 0] + si[:, 2] + 4 * si[:, 1]) / 6)
+    w = (1 + tau[:, None] / (si + 1e-40)) ** 6
+    w = w / w.sum(axis=1, keepdims=True)
+    return ((w >= 5e-4) * np.array([1, 2, 4])).sum(axis=1)
+
+
+def bf16_to_float(bits):
+    return (bits.astype(np.uint32) << 16).view(np.float32).astype(np.float64)
+
+
+def test_harvest_counts_and_labels(hteno_lib, cuda):
+    from hteno import ic
+
+    h = hteno_lib
+    nx, ny = 64, 48
+    total = ((nx + 1) * ny + (ny + 1) * nx) * 4 * 2
+    x = cuda.empty((total + 10, 8), dtype=cuda.int16, device="cuda")
+    y = cuda.empty((total + 10,), dtype=cuda.uint8, device="cuda")
+    with h.Solver(h.config(dims=2, nx=nx, ny=ny, flux=1)) as s:
+        s.set_state(ic.four_quadrant(nx, ny, 3))
+        s.step(10)
+        assert s.harvest(1.0, 1, x, y) == total
+        xa = x[:total].cpu().numpy().view(np.uint16)
+        ya = y[:total].cpu().numpy()
+        n3 = s.harvest(0.3, 2, x, y)
+        assert abs(n3 - 0.3 * total) < 0.05 * total
+        x2 = x[:n3].clone()
+        assert s.harvest(0.3, 2, x, y) == n3 and bool((x[:n3] == x2).all())  # deterministic
+    assert ya.max() <= 7 and 0.3 < (ya == 7).mean() < 1.0
+    v = bf16_to_float(xa[:, :6])
+    assert np.abs(v).max() <= 1.0 + 1e-2 and (xa[:, 6:] == 0).all()
+    # the label is the cut-off of the recorded stencil (normalisation is label-preserving up to
+    # the 1e-40 offset; BF16 rounding moves a few near-threshold decisions)
+    agree = (teno5_pattern(v) == ya).mean()
+    assert agree >= 0.97, agree
+
+
+def test_harvest_1d(hteno_lib, cuda):
+    from hteno import ic
+
+    h = hteno_lib
+    x = cuda.empty((401 * 6, 8), dtype=cuda.int16, device="cuda")
+    y = cuda.empty((401 * 6,), dtype=cuda.uint8, device="cuda")
+    with h.Solver(h.config(dims=1, nx=400, flux=1, recon=0, cfl=0.5)) as s:
+        s.set_state(ic.sod(400))
+        s.step(20, 0.2)
+        assert s.harvest(1.0, 5, x, y) == 401 * 6
+    ya = y.cpu().numpy()
+    assert (ya == 7).mean() > 0.5 and (ya != 7).any()
+
+
+def constant_classifier(h, logit):
+    m = h.Mlp()
+    p = np.zeros(m.nparams, dtype=np.float32)
+    p[1376:1379] = logit  # b3: every stencil gets the same probabilities
+    m.set_params(p)
+    return m
+
+
+def run_mixed(h, q, steps, router=None, audit=0, **kw):
+    cfg = h.config(dims=2, nx=q.shape[2], ny=q.shape[1], flux=1, precision=1, **kw)
+    with h.Solver(cfg) as s:
+        if router is not None:
+            s.set_router(router, 0.9, audit)
+        s.set_state(q)
+        s.step(steps)
+        st = s.router_stats() if router is not None else None
+        return s.get_state(), st
+
+
+def test_router_all_and_nothing(hteno_lib, cuda):
+    from hteno import ic
+
+    h = hteno_lib
+    q = ic.four_quadrant(70, 52, 8)
+    with constant_classifier(h, 20.0) as all_smooth, constant_classifier(h, -20.0) as none:
+        got_all, st = run_mixed(h, q, 6, all_smooth, audit=1)
+        want_lin, _ = run_mixed(h, q, 6, recon=2)
+        np.testing.assert_array_equal(got_all, want_lin)
+        faces = (71 * 52 + 53 * 70) * 8
+        assert st["audits"] == 6 and st["seen"] == faces * 3 * 6 and st["routed"] == st["seen"]
+        assert st["misrouted"] == st["seen"] - st["smooth"]
+        got_none, st0 = run_mixed(h, q, 6, none, audit=2)
+        want_teno, _ = run_mixed(h, q, 6)
+        np.testing.assert_array_equal(got_none, want_teno)
+        assert st0["routed"] == 0 and st0["audits"] == 3 and st0["seen"] == faces * 3 * 3
+
+
+def test_trained_router_gains(hteno_lib, cuda):
+    """Train on rows harvested from plain runs (fresh seeds), then route a mixed 256^2 run: most
+    stencils skip the nonlinear weights, few are misrouted, and the density error against FP64
+    stays within the mixed path's bound."""
+    from hteno import ic, learned
+
+    h = hteno_lib
+    x, y = learned.harvest_runs(h, cuda, seeds=[41, 42], n=256, snapshots=(0, 15, 30), keep=0.5)
+    assert x.shape[0] > 300000
+    with h.Mlp(seed=1) as m:
+        loss = m.train(x, y, epochs=6, batch=8192, lr=3e-3)
+        acc, routed, mis = learned.accuracy(m, cuda, x, y, 0.9)
+        assert acc > 0.9 and routed > 0.3 and mis < 0.02, (loss, acc, routed, mis)
+        q = ic.four_quadrant(256, 256, 99)
+        cfg = h.config(dims=2, nx=256, ny=256, flux=1)
+        with h.Solver(cfg) as s:
+            s.set_state(q)
+            s.step(30)
+            t_ref, _, _ = s.time()
+            ref = s.get_state()
+        cfg = h.config(dims=2, nx=256, ny=256, flux=1, precision=1)
+        with h.Solver(cfg) as s:
+            s.set_router(m, 0.9, 5)
+            s.set_state(q)
+            s.step(1000, t_ref)
+            st = s.router_stats()
+            got = s.get_state()
+    l1 = np.abs(got[0] - ref[0]).mean()
+    assert l1 <= 1e-4, l1
+    assert st["routed"] / st["seen"] > 0.3 and st["misrouted"] / max(1, st["routed"]) < 0.02, st
