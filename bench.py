@@ -14,6 +14,12 @@ path has no exchange step at this size: replicas only), timed between barriers; 
 value is the sum over ranks divided by the slowest rank's time.
 --impl reference times the reference algorithm on the host cores (the CPU oracle, the
 reference's own sources cannot be built on the GPU host), rank 0 only.
+
+Besides the headline line's plain FP64 value, "paths" reports the other measured workloads:
+the mixed-precision path on the same grid (with its density error against FP64), the
+Hermite-WENO 2048^2 blob/shock case (FP64 and mixed), the 4096^2 learned-routing case (FP64,
+FP32, FP32 + learned classifier, with training and audit figures) and the batch of 256 uneven
+grids.  --no-mixed / --no-hermite / --no-learned / --no-batch skip them.
 """
 from __future__ import annotations
 
@@ -52,6 +58,10 @@ def parse():
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-hermite", action="store_true")
     ap.add_argument("--hermite-steps", type=int, default=10)
+    ap.add_argument("--no-learned", action="store_true")
+    ap.add_argument("--c5-steps", type=int, default=20)
+    ap.add_argument("--c5-fp64-steps", type=int, default=3)
+    ap.add_argument("--c5-epochs", type=int, default=4)
     ap.add_argument("--batch-steps", type=int, default=100)
     return ap.parse_args()
 
@@ -284,6 +294,89 @@ def hermite_path(hteno, torch, stream, steps, ref_steps, world, n=2048):
     return out
 
 
+def learned_path(hteno, torch, stream, args, world, n=4096):
+    """The learned-routing workload: 4096 x 4096 seeded four-quadrant data, TENO5 + HLLC.
+    The classifier trains on rows the plain FP64 solver records from runs with fresh seeds of the
+    1024^2 four-quadrant problem and the 400-cell Sod tube.  Three arms run from the same
+    state: plain FP64, FP32 (mixed) and FP32 + learned routing with an audit every 50 steps.
+    The mixed arms are timed over `c5_steps`; the FP64 arm over `c5_fp64_steps`.  Densities are
+    compared at the FP64 arm's final time."""
+    from hteno import ic, learned
+
+    out = {"workload": f"fv2d_fourquadrant_{n}x{n}_teno5_hllc_learned_routing"}
+    t0 = time.perf_counter()
+    x, y = learned.harvest_runs(hteno, torch, seeds=[201, 202, 203], n=1024, snapshots=(0, 20, 40),
+                                keep=0.066)
+    t1 = time.perf_counter()
+    m = hteno.Mlp(seed=0)
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    loss = m.train(x, y, epochs=args.c5_epochs, batch=65536, lr=3e-3)
+    torch.cuda.synchronize()
+    t3 = time.perf_counter()
+    acc, routed, mis = learned.accuracy(m, torch, x, y, 0.9)
+    out["training"] = {"rows": int(x.shape[0]), "smooth_fraction": float((y == 7).float().mean().item()),
+                       "harvest_s": t1 - t0, "train_s": t3 - t2, "epochs": args.c5_epochs,
+                       "rows_per_s": x.shape[0] * args.c5_epochs / (t3 - t2), "final_loss": loss,
+                       "bit_accuracy": acc, "routed_fraction": routed, "misrouted_of_routed": mis}
+    del x, y
+    q = ic.four_quadrant(n, n, 7)
+
+    cfg64 = hteno.config(dims=2, nx=n, ny=n, flux=hteno.FLUX_HLLC, precision=hteno.PREC_FP64)
+    with hteno.Solver(cfg64) as s:
+        s.set_stream(stream.cuda_stream)
+        s.set_state(q)
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        s.step_async(args.c5_fp64_steps)
+        ev1.record(stream)
+        ev1.synchronize()
+        s.sync()
+        ms64 = ev0.elapsed_time(ev1)
+        t_ref = s.time()[0]
+        ref = s.get_state()
+    out["fp64"] = {"value": n * n * args.c5_fp64_steps * world / (ms64 / 1e3) / 1e6, "unit": UNIT,
+                   "ms_per_step": ms64 / args.c5_fp64_steps, "steps": args.c5_fp64_steps}
+    cfg32 = hteno.config(dims=2, nx=n, ny=n, flux=hteno.FLUX_HLLC, precision=hteno.PREC_MIXED)
+    for name, router in (("fp32_plain", None), ("fp32_learned", m)):
+        with hteno.Solver(cfg32) as s:
+            s.set_stream(stream.cuda_stream)
+            if router is not None:
+                s.set_router(router, 0.9, 50)
+            s.set_state(q)
+            s.step_async(2)  # warm-up
+            s.sync()
+            ev0 = torch.cuda.Event(enable_timing=True)
+            ev1 = torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            ev0.record(stream)
+            s.step_async(args.c5_steps)
+            ev1.record(stream)
+            ev1.synchronize()
+            s.sync()
+            ms = ev0.elapsed_time(ev1)
+            st = s.router_stats() if router is not None else None
+            # accuracy: the same arm from the initial state to the FP64 arm's time
+            s.set_state(q)
+            s.step(1 << 20, t_ref)
+            l1, linf = density_errors(s.get_state(), ref)
+        d = {"value": n * n * args.c5_steps * world / (ms / 1e3) / 1e6, "unit": UNIT,
+             "ms_per_step": ms / args.c5_steps, "steps": args.c5_steps,
+             "speedup_vs_fp64": (ms64 / args.c5_fp64_steps) / (ms / args.c5_steps),
+             "l1_rho_vs_fp64": l1, "linf_rho_vs_fp64": linf, "t_compared": t_ref}
+        if st is not None:
+            d["router"] = {"audited_stencils": st["seen"], "routed_fraction": st["routed"] / max(1, st["seen"]),
+                           "misrouted_of_routed": st["misrouted"] / max(1, st["routed"]),
+                           "plain_teno_smooth_fraction": st["smooth"] / max(1, st["seen"]),
+                           "audited_steps": st["audits"], "threshold": 0.9, "audit_every": 50}
+        out[name] = d
+    m.close()
+    out["learned_vs_fp32_plain"] = out["fp32_plain"]["ms_per_step"] / out["fp32_learned"]["ms_per_step"]
+    return out
+
+
 def density_errors(a, b):
     d = np.abs(a[0] - b[0])
     return float(d.mean()), float(d.max())
@@ -422,6 +515,8 @@ def run_gpu(args):
         paths["fp32_mixed"] = mixed_path(hteno, torch, q, stream, args, t_plain, ref_state, ms_max, world)
     if not args.no_hermite:
         paths["hermite_2048"] = hermite_path(hteno, torch, stream, args.hermite_steps, 3, world)
+    if not args.no_learned:
+        paths["learned_4096"] = learned_path(hteno, torch, stream, args, world)
     if not args.no_batch:
         paths["batch_256_mixed"] = batch_path(hteno, torch, stream, args.batch_steps, world)
 

@@ -117,10 +117,21 @@ __device__ __forceinline__ float teno_side_s(float p0, float p1, float p2, const
 }
 
 // Audit counters of the learned router: stencils seen, routed to the linear weights, routed
-// although the plain TENO cut-off would not have kept all three candidates, all-smooth by TENO.
+// although the plain TENO cut-off would not have kept all three candidates (flat stencils, whose
+// candidates coincide to float rounding, excepted), all-smooth by TENO.
 struct RouteCount {
   int seen = 0, routed = 0, misrouted = 0, smooth = 0;
 };
+
+__device__ __forceinline__ bool flat6(const float* u) {
+  float hi = u[0], lo = u[0];
+#pragma unroll
+  for (int m = 1; m < 6; ++m) {
+    hi = fmaxf(hi, u[m]);
+    lo = fminf(lo, u[m]);
+  }
+  return !(hi - lo > 1e-6f * fmaxf(fabsf(hi), fabsf(lo)));
+}
 
 // recon_s with routing: a side whose route bit is set takes the optimal linear weights (the TENO
 // result when all three cut-off bits are on) without evaluating the smoothness indicators; when
@@ -142,7 +153,7 @@ __device__ __forceinline__ void recon_routed(const DevConst& C, int kind, const 
       rc.seen += 1;
       rc.smooth += pat == 7;
       rc.routed += route & 1;
-      rc.misrouted += (route & 1) && pat != 7;
+      rc.misrouted += (route & 1) && pat != 7 && !flat6(u);
     }
   }
   p0 = C.f_crj[0][0] * u[3] + C.f_crj[1][0] * u[4] + C.f_crj[2][0] * u[5];
@@ -158,7 +169,7 @@ __device__ __forceinline__ void recon_routed(const DevConst& C, int kind, const 
       rc.seen += 1;
       rc.smooth += pat == 7;
       rc.routed += (route >> 1) & 1;
-      rc.misrouted += (route & 2) && pat != 7;
+      rc.misrouted += (route & 2) && pat != 7 && !flat6(u);
     }
   }
 }

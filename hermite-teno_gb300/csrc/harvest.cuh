@@ -40,8 +40,15 @@ __device__ __forceinline__ int label(const double* w, bool improved) {
   return par::cutoff_pattern(SI, tau, HTENO_LAG_EPSZ, HTENO_LAG_CT);
 }
 
+// A stencil whose spread is below HTENO_FLAT_SPREAD of its magnitude is "flat": every TENO
+// candidate gives the same value to within float rounding, so its cut-off bits (set by rounding
+// noise) do not matter.  Flat stencils are not recorded, and the router sends them to the linear
+// weights without asking the network.
+#define HTENO_FLAT_SPREAD 1e-6
+
 // Appends (normalised stencil as BF16 [8], label) unless the buffer is full; `count` keeps
-// counting past the capacity so the caller sees how many were offered.
+// counting past the capacity so the caller sees how many were offered.  Normalised values are
+// clamped to [-1, 1] (the bound in exact arithmetic).
 __device__ __forceinline__ void emit(const double* w, int lab, uint16_t* X, uint8_t* Y, long cap,
                                      unsigned long long* count) {
   double mean = 0.0, mx = w[0], mn = w[0];
@@ -52,13 +59,15 @@ __device__ __forceinline__ void emit(const double* w, int lab, uint16_t* X, uint
     mn = fmin(mn, w[k]);
   }
   mean /= 6.0;
+  if (!(mx - mn > HTENO_FLAT_SPREAD * fmax(fabs(mx), fabs(mn)))) return;  // flat (or NaN)
   const double inv = 1.0 / (mx - mn + 1e-30);
   const unsigned long long slot = atomicAdd(count, 1ull);
   if (slot >= (unsigned long long)cap) return;
   uint16_t bits[8];
 #pragma unroll
   for (int k = 0; k < 8; ++k) {
-    const __nv_bfloat16 b = __float2bfloat16_rn(k < 6 ? float((w[k] - mean) * inv) : 0.0f);
+    const __nv_bfloat16 b =
+        __float2bfloat16_rn(k < 6 ? float(fmin(1.0, fmax(-1.0, (w[k] - mean) * inv))) : 0.0f);
     bits[k] = *reinterpret_cast<const uint16_t*>(&b);
   }
   uint4 packed;

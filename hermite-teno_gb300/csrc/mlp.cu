@@ -24,6 +24,9 @@
 
 #include "fv2d_fused.cuh"
 #include "hteno_internal.h"
+#ifndef HTENO_FLAT_SPREAD
+#define HTENO_FLAT_SPREAD 1e-6  // same flatness rule as the harvest (harvest.cuh)
+#endif
 #include "mlp_internal.cuh"
 
 struct hteno_mlp;
@@ -394,6 +397,7 @@ __global__ void __launch_bounds__(128) k_classify(Weights W, Geo G, const double
     const long face = ch * 16 + (t >> 3);
     const bool valid = face < nf;
     uint16_t f[6] = {0, 0, 0, 0, 0, 0};
+    bool flat = false;
     int dir = 1, fi = 0, tt = 0;
     if (valid) {
       if (face < nxf) {
@@ -450,9 +454,10 @@ __global__ void __launch_bounds__(128) k_classify(Weights W, Geo G, const double
         lo = fminf(lo, w[m]);
       }
       mean *= (1.0f / 6.0f);
+      flat = !(hi - lo > float(HTENO_FLAT_SPREAD) * fmaxf(fabsf(hi), fabsf(lo)));
       const float inv = 1.0f / (hi - lo + 1e-30f);
       for (int m = 0; m < 6; ++m) {
-        const __nv_bfloat16 b = __float2bfloat16_rn((w[m] - mean) * inv);
+        const __nv_bfloat16 b = __float2bfloat16_rn(fminf(1.f, fmaxf(-1.f, (w[m] - mean) * inv)));
         f[m] = *reinterpret_cast<const uint16_t*>(&b);
       }
     }
@@ -460,7 +465,7 @@ __global__ void __launch_bounds__(128) k_classify(Weights W, Geo G, const double
     float h1[32], h2[32], z3[3];
     ok = forward(S, tbase, phase, h1, h2, z3, false);
     if (!ok) break;
-    const bool smooth = valid && z3[0] > zthr && z3[1] > zthr && z3[2] > zthr;
+    const bool smooth = valid && (flat || (z3[0] > zthr && z3[1] > zthr && z3[2] > zthr));
     const unsigned b = __ballot_sync(0xffffffffu, smooth);
     if (valid && s8 == 0) {
       const uint8_t byte = uint8_t((b >> (lane & ~7)) & 0xffu);

@@ -108,3 +108,85 @@ def face_difference_moments(q_fn, nx, ny, xl, xr, yb, yt):
     v = (q_fn(X + dx / 2.0, Y) - q_fn(X - dx / 2.0, Y)) / dx
     w = (q_fn(X, Y + dy / 2.0) - q_fn(X, Y - dy / 2.0)) / dy
     return np.ascontiguousarray(v), np.ascontiguousarray(w)
+
+
+# ---- smooth cases with exact solutions (periodic) ----------------------------------------------
+# Cell averages by the 9-point Gauss-Legendre rule per direction, as the reference's
+# entropyWaves / isentropicVortex do (Equations_Euler2D.cpp:454-471, 513-528,
+# Equations_Euler1D.cpp:263-277; nodes and weights of Schemes_Lagrange.cpp:22-42).
+
+def _gauss9():
+    a, w = np.polynomial.legendre.leggauss(9)
+    return a, w
+
+
+def cell_average_2d(f, nx, ny, xl, xr, yb, yt):
+    """Cell averages [k][ny][nx] of f(X, Y) -> [k, ...] over the uniform grid."""
+    a, w = _gauss9()
+    dx, dy = (xr - xl) / nx, (yt - yb) / ny
+    X, Y = np.meshgrid(xl + (np.arange(nx) + 0.5) * dx, yb + (np.arange(ny) + 0.5) * dy)
+    acc = None
+    for i in range(9):
+        for j in range(9):
+            v = w[i] * w[j] * np.asarray(f(X + dx * a[i] / 2.0, Y + dy * a[j] / 2.0)) / 4.0
+            acc = v if acc is None else acc + v
+    return np.ascontiguousarray(acc)
+
+
+def cell_average_1d(f, nx, xl, xr):
+    a, w = _gauss9()
+    dx = (xr - xl) / nx
+    X = xl + (np.arange(nx) + 0.5) * dx
+    acc = None
+    for i in range(9):
+        v = w[i] * np.asarray(f(X + dx * a[i] / 2.0)) / 2.0
+        acc = v if acc is None else acc + v
+    return np.ascontiguousarray(acc)
+
+
+def entropy_wave_2d(nx, ny, t=0.0, xl=-1.0, xr=1.0, yb=-1.0, yt=1.0, rho=1.0, u=1.0, v=1.0, p=1.0,
+                    amp=0.5, gamma=1.4, derivative=False):
+    """FV::System2D::entropyWave (FV_System2D.cpp:49-74): rho = rho_inf + A sin(pi (x + y)),
+    constant u, v, p, advected to time t; derivative=True gives the cell averages of d/dx
+    (= d/dy), the Hermite moments (dconservativeOfEntropyWave, Equations_Euler2D.cpp:442-452)."""
+    def q(X, Y):
+        xs, ys = X - u * t, Y - v * t
+        if derivative:
+            d = amp * np.cos(np.pi * (xs + ys)) * np.pi
+            return np.stack([d, u * d, v * d, 0.5 * (u * u + v * v) * d])
+        r = rho + amp * np.sin(np.pi * (xs + ys))
+        return conservative2(r, u + 0 * r, v + 0 * r, p + 0 * r, gamma)
+    return cell_average_2d(q, nx, ny, xl, xr, yb, yt)
+
+
+def isentropic_vortex_2d(nx, ny, t=0.0, xl=-5.0, xr=5.0, yb=-5.0, yt=5.0, gamma=1.4, b=5.0):
+    """FV::System2D::isentropicVortex (FV_System2D.cpp:76-99; conservativeOfIsentropicVortex,
+    Equations_Euler2D.cpp:656-666): the vortex of strength b on a (1, 1) mean flow, advected to
+    time t (periodic domain of side L: positions wrap)."""
+    L = xr - xl
+    g1 = gamma - 1.0
+
+    def q(X, Y):
+        xs = (X - t - xl) % L + xl
+        ys = (Y - t - yb) % (yt - yb) + yb
+        r = xs ** 2 + ys ** 2
+        rho = (1.0 - g1 * b ** 2 / 8.0 / gamma / np.pi ** 2 * np.exp(1 - r)) ** (1.0 / g1)
+        uu = 1.0 - b * ys / 2.0 / np.pi * np.exp(0.5 * (1 - r))
+        vv = 1.0 + b * xs / 2.0 / np.pi * np.exp(0.5 * (1 - r))
+        return conservative2(rho, uu, vv, rho ** gamma, gamma)
+    return cell_average_2d(q, nx, ny, xl, xr, yb, yt)
+
+
+def entropy_wave_1d(nx, t=0.0, xl=-1.0, xr=1.0, rho=1.0, u=1.0, p=1.0, amp=0.5, gamma=1.4,
+                    derivative=False):
+    """FV::System1D / FVHermite::System1D entropyWave (Equations_Euler1D.cpp:243-294):
+    rho = rho_inf + A sin(pi x), constant u, p, at time t; derivative=True: cell averages of
+    d/dx (the Hermite moment)."""
+    def q(X):
+        xs = X - u * t
+        if derivative:
+            d = amp * np.cos(np.pi * xs) * np.pi
+            return np.stack([d, u * d, 0.5 * u * u * d])
+        r = rho + amp * np.sin(np.pi * xs)
+        return np.stack([r, r * u, p / (gamma - 1.0) + 0.5 * r * u * u])
+    return cell_average_1d(q, nx, xl, xr)

@@ -94,6 +94,14 @@ def loss_and_grad(p, x, labels):
 
 
 def normalise(stencils):
-    """(u - mean) / (max - min + 1e-30) per 6-cell row."""
+    """(u - mean) / (max - min + 1e-30) per 6-cell row, clamped to [-1, 1]."""
     s = np.asarray(stencils, dtype=np.float64)
-    return (s - s.mean(axis=1, keepdims=True)) / (s.max(axis=1, keepdims=True) - s.min(axis=1, keepdims=True) + 1e-30)
+    v = (s - s.mean(axis=1, keepdims=True)) / (s.max(axis=1, keepdims=True) - s.min(axis=1, keepdims=True) + 1e-30)
+    return np.clip(v, -1.0, 1.0)
+
+
+def flat(stencils, spread=1e-6):
+    """Rows whose spread is at most `spread` of their magnitude (not recorded by the harvest)."""
+    s = np.asarray(stencils, dtype=np.float64)
+    hi, lo = s.max(axis=1), s.min(axis=1)
+    return ~(hi - lo > spread * np.maximum(np.abs(hi), np.abs(lo)))
