@@ -57,11 +57,12 @@ def parse():
     ap.add_argument("--no-mixed", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-hermite", action="store_true")
+    ap.add_argument("--no-sod", action="store_true")
     ap.add_argument("--hermite-steps", type=int, default=10)
     ap.add_argument("--no-learned", action="store_true")
     ap.add_argument("--c5-steps", type=int, default=20)
     ap.add_argument("--c5-fp64-steps", type=int, default=3)
-    ap.add_argument("--c5-epochs", type=int, default=4)
+    ap.add_argument("--c5-epochs", type=int, default=10)
     ap.add_argument("--batch-steps", type=int, default=100)
     return ap.parse_args()
 
@@ -305,13 +306,13 @@ def learned_path(hteno, torch, stream, args, world, n=4096):
 
     out = {"workload": f"fv2d_fourquadrant_{n}x{n}_teno5_hllc_learned_routing"}
     t0 = time.perf_counter()
-    x, y = learned.harvest_runs(hteno, torch, seeds=[201, 202, 203], n=1024, snapshots=(0, 20, 40),
-                                keep=0.066)
+    x, y = learned.harvest_runs(hteno, torch, seeds=[201, 202, 203, 204], n=1024,
+                                snapshots=(0, 20, 40, 60), keep=1.0)
     t1 = time.perf_counter()
     m = hteno.Mlp(seed=0)
     torch.cuda.synchronize()
     t2 = time.perf_counter()
-    loss = m.train(x, y, epochs=args.c5_epochs, batch=65536, lr=3e-3)
+    loss = m.train(x, y, epochs=args.c5_epochs, batch=16384, lr=3e-3)
     torch.cuda.synchronize()
     t3 = time.perf_counter()
     acc, routed, mis = learned.accuracy(m, torch, x, y, 0.9)
@@ -368,6 +369,7 @@ def learned_path(hteno, torch, stream, args, world, n=4096):
              "l1_rho_vs_fp64": l1, "linf_rho_vs_fp64": linf, "t_compared": t_ref}
         if st is not None:
             d["router"] = {"audited_stencils": st["seen"], "routed_fraction": st["routed"] / max(1, st["seen"]),
+                           "network_rows_last_step": st["network_rows"],
                            "misrouted_of_routed": st["misrouted"] / max(1, st["routed"]),
                            "plain_teno_smooth_fraction": st["smooth"] / max(1, st["seen"]),
                            "audited_steps": st["audits"], "threshold": 0.9, "audit_every": 50}
@@ -375,6 +377,34 @@ def learned_path(hteno, torch, stream, args, world, n=4096):
     m.close()
     out["learned_vs_fp32_plain"] = out["fp32_plain"]["ms_per_step"] / out["fp32_learned"]["ms_per_step"]
     return out
+
+
+def sod_path(hteno, torch):
+    """The 1D benchmark tube: 400 cells, Sod data, TENO5 + HLLC, CFL 0.5, plain FP64, to t = 0.2
+    (a latency case): wall time of the whole run through the C-ABI on the GPU and of the CPU
+    oracle (one thread, as the reference's 1D solver runs), and the largest difference."""
+    import oracle
+    from hteno import ic
+
+    q = ic.sod(400)
+    cfg = hteno.config(dims=1, nx=400, flux=hteno.FLUX_HLLC, recon=hteno.RECON_TENO5, cfl=0.5,
+                       precision=hteno.PREC_FP64)
+    with hteno.Solver(cfg) as s:
+        s.set_state(q)
+        s.step(1 << 20, 0.2)  # warm
+        s.set_state(q)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        s.step(1 << 20, 0.2)
+        gpu_s = time.perf_counter() - t0
+        _, n, _ = s.time()
+        got = s.get_state()
+    t0 = time.perf_counter()
+    want, _, n_o = oracle.fv1d_run(q, 1 << 20, t_final=0.2, flux=1, recon=0, cfl=0.5)
+    cpu_s = time.perf_counter() - t0
+    return {"workload": "fv1d_sod_400_teno5_hllc_cfl0.5_t0.2_fp64", "steps": n, "gpu_wall_s": gpu_s,
+            "cpu_oracle_wall_s": cpu_s, "cpu_cores": 1, "max_abs_diff_vs_oracle": float(np.abs(got - want).max()),
+            "value": 400 * n / gpu_s / 1e6, "unit": UNIT}
 
 
 def density_errors(a, b):
@@ -513,6 +543,8 @@ def run_gpu(args):
     paths = {}
     if not args.no_mixed:
         paths["fp32_mixed"] = mixed_path(hteno, torch, q, stream, args, t_plain, ref_state, ms_max, world)
+    if not args.no_sod and rank == 0:
+        paths["sod_1d_400"] = sod_path(hteno, torch)
     if not args.no_hermite:
         paths["hermite_2048"] = hermite_path(hteno, torch, stream, args.hermite_steps, 3, world)
     if not args.no_learned:

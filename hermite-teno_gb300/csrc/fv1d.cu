@@ -163,6 +163,27 @@ __global__ void __launch_bounds__(kThreads) k1_harvest(Geo1 G, const double* __r
                        p, X, Y, cap, count);
 }
 
+// KXRCF troubled-cell sensor of FV::System1D::rhs (FV_System1D.cpp:166-192): from the density
+// averages, the two one-sided face values of the upwind face (chosen by the sign of rho*u),
+// flagged when |h1 - h2| / ((dx/2)^1.5 |rho_i|) > 1.  The reference computes the flag for cells
+// s+1 .. nxx-s-2 of its ghost-padded array (every interior cell) and reconstructs with teno5i
+// either way; here the flags are an output.
+__global__ void k1_kxrcf(Geo1 G, const double* __restrict__ q, double crm, uint8_t* __restrict__ flag) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= G.nx) return;
+  const int n = G.nx;
+  auto rho = [&](int k) { return q[bmap(k, n, G.bc)]; };
+  double h1, h2;
+  if (q[n + i] < 0.0) {
+    h1 = (2.0 * rho(i - 1) + 5.0 * rho(i) - rho(i + 1)) / 6.0;
+    h2 = (-rho(i - 2) + 5.0 * rho(i - 1) + 2.0 * rho(i)) / 6.0;
+  } else {
+    h2 = (2.0 * rho(i) + 5.0 * rho(i + 1) - rho(i + 2)) / 6.0;
+    h1 = (-rho(i - 1) + 5.0 * rho(i) + 2.0 * rho(i + 1)) / 6.0;
+  }
+  flag[i] = fabs(h1 - h2) / (crm * fabs(rho(i))) > 1.0 ? 1 : 0;
+}
+
 Geo1 geo1_of(const hteno_solver* s) {
   Geo1 G;
   G.nx = s->cfg.nx;
@@ -213,6 +234,15 @@ int fv1d_harvest(hteno_solver* s, double p, unsigned long long seed, uint16_t* X
   k1_harvest<<<unsigned((G.nx + 1 + kThreads - 1) / kThreads), kThreads, 0, s->stream>>>(
       G, s->q, p, seed, X, Y, cap, count);
   return cuda_error(s, cudaGetLastError(), "harvest");
+}
+
+int fv1d_kxrcf(hteno_solver* s, uint8_t* flags) {
+  const Geo1 G = geo1_of(s);
+  const double crm = pow(G.dx / 2.0, 1.5);  // circleRadMod (FV_System1D.cpp:19)
+  k1_kxrcf<<<unsigned((G.nx + kThreads - 1) / kThreads), kThreads, 0, s->stream>>>(G, s->q, crm, flags);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+  return cuda_error(s, e, "kxrcf");
 }
 
 int fv1d_step_async(hteno_solver* s, int nsteps) {

@@ -1,5 +1,6 @@
 // Mixed-precision FV 2D path: one fused launch per RK stage (fv2d_fused.cuh), with the tile
 // shape picked per solver by timing the candidates on the solver's own grid and state.
+#include <algorithm>
 #include <cstdlib>
 
 #include "fv2d_fused.cuh"
@@ -162,7 +163,8 @@ void fv2d_fused_step(hteno_solver* s, const Geo& G, double* qc) {
   if (s->router) {
     const int kc = trace_kind(s, "classify", 0.0, 0.0);
     trace_begin(s, kc);
-    mlp_classify(s->router, G, s->q, s->route_x, s->route_y, s->router_thr, s->stream);
+    mlp_classify(s->router, G, s->q, s->route_x, s->route_y, s->router_thr, s->route_rows,
+                 s->route_info, s->audit + 4, s->route_cap, s->stream);
     trace_end(s);
     const bool aud = s->audit_every > 0 && s->router_steps % s->audit_every == 0;
     for (fused::StageArgs* a : {&a1, &a2, &a3}) {
@@ -204,30 +206,35 @@ int hteno_set_router(hteno_solver* s, hteno_mlp* m, float threshold, int audit_e
   }
   if (!s->route_x) {
     const size_t bx = size_t(s->cfg.nx + 1) * s->cfg.ny, by = size_t(s->cfg.ny + 1) * s->cfg.nx;
-    cudaError_t e = cudaMalloc(&s->route_x, bx);
-    if (e == cudaSuccess) e = cudaMalloc(&s->route_y, by);
-    if (e == cudaSuccess) e = cudaMalloc(&s->audit, 4 * sizeof(unsigned long long));
+    // rows for the network: up to every stencil of every face, at most 64 M rows (1.5 GB)
+    s->route_cap = long(std::min<size_t>(8 * (bx + by), size_t(64) << 20));
+    cudaError_t e = cudaMalloc(&s->route_x, (bx + 3) & ~size_t(3));
+    if (e == cudaSuccess) e = cudaMalloc(&s->route_y, (by + 3) & ~size_t(3));
+    if (e == cudaSuccess) e = cudaMalloc(&s->audit, 5 * sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMalloc(&s->route_rows, size_t(s->route_cap) * sizeof(uint4));
+    if (e == cudaSuccess) e = cudaMalloc(&s->route_info, size_t(s->route_cap) * sizeof(unsigned long long));
     if (e != cudaSuccess) return cuda_error(s, e, "route masks");
   }
-  cudaMemset(s->audit, 0, 4 * sizeof(unsigned long long));
+  cudaMemset(s->audit, 0, 5 * sizeof(unsigned long long));
   s->router = m;
   s->router_thr = threshold;
   s->audit_every = audit_every;
   s->router_steps = 0;
   s->audits = 0;
-  s->launches_per_step = 2 + 3 + 1;
+  s->launches_per_step = 2 + 3 + 2;
   return HTENO_OK;
 }
 
 int hteno_router_stats(hteno_solver* s, long long* stats) {
   if (!s || !stats) return HTENO_ERR_INVALID_ARG;
   if (!s->router || !s->audit) return set_error(s, HTENO_ERR_UNSUPPORTED, "no router set");
-  unsigned long long h[4] = {0, 0, 0, 0};
+  unsigned long long h[5] = {0, 0, 0, 0, 0};
   cudaError_t e = cudaMemcpyAsync(h, s->audit, sizeof(h), cudaMemcpyDeviceToHost, s->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
   if (e != cudaSuccess) return cuda_error(s, e, "router stats");
   for (int k = 0; k < 4; ++k) stats[k] = (long long)h[k];
   stats[4] = s->audits;
+  stats[5] = (long long)h[4];
   const int rc = mlp_status(s->router, s->stream);
   return rc == HTENO_OK ? HTENO_OK : set_error(s, rc, "classifier tensor-core wait timed out");
 }

@@ -76,8 +76,11 @@ struct hteno_solver {
   long router_steps = 0;
   uint8_t* route_x = nullptr;
   uint8_t* route_y = nullptr;
-  unsigned long long* audit = nullptr;  // [4]: seen, routed, misrouted, smooth
+  unsigned long long* audit = nullptr;  // [4]: seen, routed, misrouted, smooth; [4]: rows asked
   long audits = 0;
+  uint4* route_rows = nullptr;             // non-flat stencils handed to the network
+  unsigned long long* route_info = nullptr;
+  long route_cap = 0;
   bool strict = false;
   std::string err;
 
@@ -114,6 +117,7 @@ int fv2d_residual(hteno_solver* s, const double* q, double* rhs);
 int fv1d_setup(hteno_solver* s);
 int fv1d_prepare(hteno_solver* s);
 int fv1d_step_async(hteno_solver* s, int nsteps);
+int fv1d_kxrcf(hteno_solver* s, uint8_t* flags);
 int fv1d_harvest(hteno_solver* s, double p, unsigned long long seed, uint16_t* X, uint8_t* Y,
                  long cap, unsigned long long* count);
 int fv2d_harvest_entry(hteno_solver* s, double p, unsigned long long seed, uint16_t* X, uint8_t* Y,

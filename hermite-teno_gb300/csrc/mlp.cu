@@ -375,102 +375,155 @@ __global__ void __launch_bounds__(128) k_predict(Weights W, const uint16_t* __re
   teardown(S, tbase);
 }
 
-// Learned routing of a mixed FV 2D grid: every face of both directions, 4 characteristic fields
-// and 2 sides = 8 stencils per face, 16 faces per 128-row tile.  A stencil is routed (bit set)
-// when all three predicted cut-off probabilities exceed `thr`.  The stencils are computed as the
-// fused stage kernel computes them (float primitives and Roe state from the double state).
-__global__ void __launch_bounds__(128) k_classify(Weights W, Geo G, const double* __restrict__ q,
-                                                  uint8_t* __restrict__ mx, uint8_t* __restrict__ my,
-                                                  float zthr, int* __restrict__ err) {
-  extern __shared__ __align__(128) unsigned char smem_raw[];
-  Smem& S = *reinterpret_cast<Smem*>(smem_raw);
-  setup(S, W);
-  const uint32_t tbase = S.tmem;
-  uint32_t phase = 0;
-  bool ok = true;
+// Learned routing of a mixed FV 2D grid, pass 1: one thread per face (x faces, then y faces)
+// computes the 8 stencils the fused kernel will reconstruct (4 characteristic fields x 2 sides,
+// float, from the double state as the fused kernel sees it).  Flat stencils are routed at once
+// (their route bits form the face's mask byte); the others are appended, normalised and in BF16,
+// to the row list for the network, with (face << 3 | bit) beside each.  Appends are aggregated
+// per block: one atomic per block.
+__global__ void __launch_bounds__(256) k_route_prep(Geo G, const double* __restrict__ q,
+                                                    uint8_t* __restrict__ mx, uint8_t* __restrict__ my,
+                                                    uint4* __restrict__ rows,
+                                                    unsigned long long* __restrict__ info,
+                                                    unsigned long long* __restrict__ nrows, long cap) {
+  __shared__ int warp_tot[8];
+  __shared__ unsigned long long block_base;
   const size_t nc = size_t(G.nx) * G.ny;
   const long nxf = long(G.nx + 1) * G.ny, nyf = long(G.ny + 1) * G.nx, nf = nxf + nyf;
-  const long chunks = (nf + 15) / 16;
-  const int t = threadIdx.x, lane = t & 31, s8 = t & 7, r = s8 >> 1, side = s8 & 1;
+  const long face = blockIdx.x * long(blockDim.x) + threadIdx.x;
   const float g1 = float(G.g1);
-  for (long ch = blockIdx.x; ch < chunks && ok; ch += gridDim.x) {
-    const long face = ch * 16 + (t >> 3);
-    const bool valid = face < nf;
-    uint16_t f[6] = {0, 0, 0, 0, 0, 0};
-    bool flat = false;
-    int dir = 1, fi = 0, tt = 0;
-    if (valid) {
-      if (face < nxf) {
-        fi = int(face % (G.nx + 1));
-        tt = int(face / (G.nx + 1));
-      } else {
-        const long k = face - nxf;
-        dir = 2;
-        fi = int(k / G.nx);
-        tt = int(k % G.nx);
-      }
-      // the 8 threads of a face load 3 of its 24 state values each
-      for (int j = 0; j < 3; ++j) {
-        const int idx = s8 * 3 + j, m = idx >> 2, v = idx & 3;
-        const int sidx = fused::cmap(fi - 3 + m, dir == 1 ? G.nx : G.ny, G.bc);
-        const size_t k = dir == 1 ? size_t(tt) * G.nx + sidx : size_t(sidx) * G.nx + tt;
-        S.stage[t >> 3][idx] = fused::d2f(__ldg(q + v * nc + k));
-      }
+  uint4 row[8];
+  int nmine = 0;
+  uint8_t byte = 0;
+  if (face < nf) {
+    int dir = 1, fi, tt;
+    if (face < nxf) {
+      fi = int(face % (G.nx + 1));
+      tt = int(face / (G.nx + 1));
+    } else {
+      const long k = face - nxf;
+      dir = 2;
+      fi = int(k / G.nx);
+      tt = int(k % G.nx);
     }
-    __syncwarp();
-    if (valid) {
-      const float* cq = S.stage[t >> 3];  // cq[4 m + v]
-      float cp[2][4];
-      for (int h = 0; h < 2; ++h) {  // primitives of the two cells of the face
-        const float* c = cq + 4 * (2 + h);
-        const float ir = __frcp_rn(c[0]);
-        const float u = c[1] * ir, v = c[2] * ir;
-        const float p = (c[3] - 0.5f * (c[1] * u + c[2] * v)) * g1;
-        cp[h][0] = u;
-        cp[h][1] = v;
-        cp[h][2] = (c[3] + p) * ir;
-        cp[h][3] = sqrtf(fabsf(c[0]));
-      }
-      const Roe2<float> R = roe2<float>(g1, cp[0][3], cp[0][0], cp[0][1], cp[0][2], cp[1][3],
-                                        cp[1][0], cp[1][1], cp[1][2]);
-      // row r of the left eigenvector matrix (the rows of roe_left)
-      const float vn = dir == 1 ? R.vxm : R.vym, vt = dir == 1 ? R.vym : R.vxm;
-      const float b2 = R.qm * R.b1, s0 = vn * R.rcm, s1 = R.b1 * vn, t2 = 0.5f * R.b1;
-      float a0, an, at, a3;
-      if (r == 0) { a0 = 0.5f * (b2 + s0); an = -0.5f * (s1 + R.rcm); at = -t2 * vt; a3 = t2; }
-      else if (r == 1) { a0 = -vt; an = 0.f; at = 1.f; a3 = 0.f; }
-      else if (r == 2) { a0 = 1.f - b2; an = s1; at = R.b1 * vt; a3 = -R.b1; }
-      else { a0 = 0.5f * (b2 - s0); an = -0.5f * (s1 - R.rcm); at = -t2 * vt; a3 = t2; }
+    float cq[6][4];
+    for (int m = 0; m < 6; ++m) {
+      const int sidx = fused::cmap(fi - 3 + m, dir == 1 ? G.nx : G.ny, G.bc);
+      const size_t k = dir == 1 ? size_t(tt) * G.nx + sidx : size_t(sidx) * G.nx + tt;
+      for (int v = 0; v < 4; ++v) cq[m][v] = fused::d2f(__ldg(q + v * nc + k));
+    }
+    float cp[2][4];
+    for (int h = 0; h < 2; ++h) {  // primitives of the two cells of the face
+      const float* c = cq[2 + h];
+      const float ir = __frcp_rn(c[0]);
+      const float u = c[1] * ir, v = c[2] * ir;
+      const float p = (c[3] - 0.5f * (c[1] * u + c[2] * v)) * g1;
+      cp[h][0] = u;
+      cp[h][1] = v;
+      cp[h][2] = (c[3] + p) * ir;
+      cp[h][3] = sqrtf(fabsf(c[0]));
+    }
+    const Roe2<float> R = roe2<float>(g1, cp[0][3], cp[0][0], cp[0][1], cp[0][2], cp[1][3], cp[1][0],
+                                      cp[1][1], cp[1][2]);
+    float ch[4][6];
+    for (int m = 0; m < 6; ++m) {
+      float cc[4];
+      roe_left(R, dir, cq[m], cc);
+      for (int r = 0; r < 4; ++r) ch[r][m] = cc[r];
+    }
+    for (int b = 0; b < 8; ++b) {
+      const int r = b >> 1, side = b & 1;
       float w[6];
-      for (int m = 0; m < 6; ++m) {
-        const float* c = cq + 4 * m;
-        const float qn = dir == 1 ? c[1] : c[2], qt = dir == 1 ? c[2] : c[1];
-        w[side ? 5 - m : m] = a0 * c[0] + an * qn + at * qt + a3 * c[3];
-      }
+      for (int m = 0; m < 6; ++m) w[side ? 5 - m : m] = ch[r][m];
       float mean = 0.f, hi = w[0], lo = w[0];
       for (int m = 0; m < 6; ++m) {
         mean += w[m];
         hi = fmaxf(hi, w[m]);
         lo = fminf(lo, w[m]);
       }
-      mean *= (1.0f / 6.0f);
-      flat = !(hi - lo > float(HTENO_FLAT_SPREAD) * fmaxf(fabsf(hi), fabsf(lo)));
-      const float inv = 1.0f / (hi - lo + 1e-30f);
-      for (int m = 0; m < 6; ++m) {
-        const __nv_bfloat16 b = __float2bfloat16_rn(fminf(1.f, fmaxf(-1.f, (w[m] - mean) * inv)));
-        f[m] = *reinterpret_cast<const uint16_t*>(&b);
+      if (!(hi - lo > float(HTENO_FLAT_SPREAD) * fmaxf(fabsf(hi), fabsf(lo)))) {
+        byte |= uint8_t(1u << b);  // flat: routed without the network
+        continue;
       }
+      mean *= (1.0f / 6.0f);
+      const float inv = 1.0f / (hi - lo);
+      uint16_t f[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+      for (int m = 0; m < 6; ++m) {
+        const __nv_bfloat16 bv = __float2bfloat16_rn(fminf(1.f, fmaxf(-1.f, (w[m] - mean) * inv)));
+        f[m] = *reinterpret_cast<const uint16_t*>(&bv);
+      }
+      row[nmine] = make_uint4(f[0] | (uint32_t(f[1]) << 16), f[2] | (uint32_t(f[3]) << 16),
+                              f[4] | (uint32_t(f[5]) << 16), 0u);
+      row[nmine].w = uint32_t(b);  // temporarily: the bit (the pad column is rewritten below)
+      ++nmine;
     }
-    put_input(S, t, f);
+    if (face < nxf) mx[face] = byte;
+    else my[face - nxf] = byte;
+  }
+  // block-aggregated append
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  int incl = nmine;
+  for (int o = 1; o < 32; o <<= 1) {
+    const int v = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += v;
+  }
+  if (lane == 31) warp_tot[wid] = incl;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int tot = 0;
+    for (int w = 0; w < int(blockDim.x >> 5); ++w) {
+      const int t = warp_tot[w];
+      warp_tot[w] = tot;
+      tot += t;
+    }
+    block_base = tot ? atomicAdd(nrows, (unsigned long long)tot) : 0ull;
+  }
+  __syncthreads();
+  const unsigned long long base = block_base + warp_tot[wid] + (incl - nmine);
+  for (int k = 0; k < nmine; ++k) {
+    const unsigned long long slot = base + k;
+    if (slot >= (unsigned long long)cap) break;  // beyond capacity: left unrouted (full TENO)
+    const uint32_t bit = row[k].w;
+    row[k].w = 0u;
+    rows[slot] = row[k];
+    info[slot] = (unsigned long long)(face) << 3 | bit;
+  }
+}
+
+// Pass 2: the network over the appended rows; a row whose three probabilities all exceed the
+// threshold sets its bit in the face's mask byte.
+__global__ void __launch_bounds__(128) k_route_rows(Weights W, const uint4* __restrict__ rows,
+                                                    const unsigned long long* __restrict__ info,
+                                                    const unsigned long long* __restrict__ nrows, long cap,
+                                                    long nxf, uint8_t* __restrict__ mx,
+                                                    uint8_t* __restrict__ my, float zthr,
+                                                    int* __restrict__ err) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  Smem& S = *reinterpret_cast<Smem*>(smem_raw);
+  const long n = long(min(*nrows, (unsigned long long)cap));
+  const long ntiles = (n + 127) / 128;
+  if (long(blockIdx.x) >= ntiles) return;  // uniform over the block; no tensor memory taken
+  setup(S, W);
+  const uint32_t tbase = S.tmem;
+  uint32_t phase = 0;
+  bool ok = true;
+  for (long t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+    const long r = t * 128 + threadIdx.x;
+    uint16_t f[6] = {0, 0, 0, 0, 0, 0};
+    if (r < n) {
+      const uint4 raw = rows[r];
+      const uint16_t* p = reinterpret_cast<const uint16_t*>(&raw);
+      for (int k = 0; k < 6; ++k) f[k] = p[k];
+    }
+    put_input(S, threadIdx.x, f);
     float h1[32], h2[32], z3[3];
     ok = forward(S, tbase, phase, h1, h2, z3, false);
-    if (!ok) break;
-    const bool smooth = valid && (flat || (z3[0] > zthr && z3[1] > zthr && z3[2] > zthr));
-    const unsigned b = __ballot_sync(0xffffffffu, smooth);
-    if (valid && s8 == 0) {
-      const uint8_t byte = uint8_t((b >> (lane & ~7)) & 0xffu);
-      if (face < nxf) mx[face] = byte;
-      else my[face - nxf] = byte;
+    if (ok && r < n && z3[0] > zthr && z3[1] > zthr && z3[2] > zthr) {
+      const unsigned long long in = info[r];
+      const long face = long(in >> 3);
+      uint8_t* m = face < nxf ? mx + face : my + (face - nxf);
+      const size_t a = reinterpret_cast<size_t>(m);
+      atomicOr(reinterpret_cast<unsigned int*>(a & ~size_t(3)), (1u << (in & 7)) << (8 * (a & 3)));
     }
   }
   if (!ok) {
@@ -572,7 +625,7 @@ int set_attr() {
   const int sm = int(mlp::smem_bytes());
   if (cudaFuncSetAttribute(k_train, cudaFuncAttributeMaxDynamicSharedMemorySize, sm) != cudaSuccess ||
       cudaFuncSetAttribute(k_predict, cudaFuncAttributeMaxDynamicSharedMemorySize, sm) != cudaSuccess ||
-      cudaFuncSetAttribute(k_classify, cudaFuncAttributeMaxDynamicSharedMemorySize, sm) != cudaSuccess)
+      cudaFuncSetAttribute(k_route_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, sm) != cudaSuccess)
     return HTENO_ERR_CUDA;
   done = 1;
   return HTENO_OK;
@@ -621,14 +674,17 @@ int refresh_images(hteno_mlp* m) {
 
 namespace hteno {
 
-// Route masks of a mixed FV 2D grid from its current state (see k_classify).
+// Route masks of a mixed FV 2D grid from its current state (k_route_prep, then k_route_rows on
+// the non-flat stencils).  rows/info/nrows: scratch of `cap` rows owned by the caller.
 int mlp_classify(hteno_mlp* m, const Geo& G, const double* q, uint8_t* mx, uint8_t* my, float thr,
+                 uint4* rows, unsigned long long* info, unsigned long long* nrows, long cap,
                  cudaStream_t st) {
-  const long nf = long(G.nx + 1) * G.ny + long(G.ny + 1) * G.nx;
-  const long chunks = (nf + 15) / 16;
-  const int grid = int(std::min<long>(chunks, 2L * m->sms));
+  const long nxf = long(G.nx + 1) * G.ny, nf = nxf + long(G.ny + 1) * G.nx;
+  cudaMemsetAsync(nrows, 0, sizeof(unsigned long long), st);
+  k_route_prep<<<unsigned((nf + 255) / 256), 256, 0, st>>>(G, q, mx, my, rows, info, nrows, cap);
   const float zthr = std::log(thr / (1.0f - thr));  // sigmoid(z) > thr  <=>  z > logit(thr)
-  k_classify<<<grid, 128, mlp::smem_bytes(), st>>>(m->W, G, q, mx, my, zthr, m->err);
+  k_route_rows<<<2 * m->sms, 128, mlp::smem_bytes(), st>>>(m->W, rows, info, nrows, cap, nxf, mx, my,
+                                                          zthr, m->err);
   return cudaGetLastError() == cudaSuccess ? HTENO_OK : HTENO_ERR_CUDA;
 }
 

@@ -104,6 +104,8 @@ void release(hteno_solver* s) {
   cudaFree(s->route_x);
   cudaFree(s->route_y);
   cudaFree(s->audit);
+  cudaFree(s->route_rows);
+  cudaFree(s->route_info);
   cudaFree(s->q);
   cudaFree(s->q0);
   cudaFree(s->v);
@@ -382,6 +384,13 @@ int hteno_harvest(hteno_solver* s, double keep, unsigned long long seed, unsigne
   cudaStreamSynchronize(s->stream);
   *count = long(h);
   return rc;
+}
+
+int hteno_kxrcf(hteno_solver* s, unsigned char* flags) {
+  if (!s || !flags) return HTENO_ERR_INVALID_ARG;
+  if (s->cfg.dims != 1 || is_hermite(s))
+    return set_error(s, HTENO_ERR_UNSUPPORTED, "the KXRCF sensor belongs to the FV 1D scheme");
+  return fv1d_kxrcf(s, flags);
 }
 
 const char* hteno_last_error(hteno_solver* s) { return s ? s->err.c_str() : "null handle"; }

@@ -110,6 +110,7 @@ def lib() -> ctypes.CDLL:
         L.hteno_batch_last_error.argtypes = [vp]
         L.hteno_set_router.argtypes = [vp, vp, ctypes.c_float, i]
         L.hteno_router_stats.argtypes = [vp, ctypes.POINTER(ctypes.c_longlong)]
+        L.hteno_kxrcf.argtypes = [vp, vp]
         L.hteno_harvest.argtypes = [vp, d, ctypes.c_ulonglong, vp, vp, l, ctypes.POINTER(l)]
         L.hteno_mlp_create.argtypes = [ctypes.c_ulonglong, ctypes.POINTER(vp)]
         L.hteno_mlp_destroy.argtypes = [vp]
@@ -232,6 +233,10 @@ class Solver:
     def set_stream(self, stream_ptr: int) -> None:
         _check(lib().hteno_set_stream(self.h, ctypes.c_void_p(stream_ptr)), self.h)
 
+    def kxrcf(self, flags) -> None:
+        """KXRCF troubled-cell flags (FV 1D) into the CUDA uint8 tensor `flags` [nx]."""
+        _check(lib().hteno_kxrcf(self.h, flags.data_ptr()), self.h)
+
     def harvest(self, keep: float, seed: int, x, y) -> int:
         """Training rows of the learned classifier from the current state into the CUDA tensors
         x (int16 [cap, 8], BF16 bits) and y (uint8 [cap]); returns the number offered."""
@@ -248,9 +253,10 @@ class Solver:
                                       int(audit_every)), self.h)
 
     def router_stats(self) -> dict:
-        a = (ctypes.c_longlong * 5)()
+        a = (ctypes.c_longlong * 6)()
         _check(lib().hteno_router_stats(self.h, a), self.h)
-        return {"seen": a[0], "routed": a[1], "misrouted": a[2], "smooth": a[3], "audits": a[4]}
+        return {"seen": a[0], "routed": a[1], "misrouted": a[2], "smooth": a[3], "audits": a[4],
+                "network_rows": a[5]}
 
     def residual(self, q_dev, rhs_dev) -> None:
         _check(lib().hteno_residual(self.h, _ptr(q_dev)[0], _ptr(rhs_dev)[0]), self.h)

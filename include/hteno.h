@@ -206,6 +206,12 @@ int hteno_mlp_destroy(hteno_mlp* m);
 int hteno_mlp_num_params(void);
 int hteno_mlp_set_params(hteno_mlp* m, const float* params); /* host */
 int hteno_mlp_get_params(hteno_mlp* m, float* params);       /* host */
+/* KXRCF troubled-cell flags of an FV 1D solver's current state (FV::System1D::rhs,
+ * FV_System1D.cpp:166-192): flags[nx] (device bytes) = 1 where |h1 - h2| / ((dx/2)^1.5 |rho|) > 1,
+ * h1, h2 the two one-sided density values at the upwind face.  The reference computes the flag
+ * and reconstructs with teno5i either way; here it is an output (the reference's precedent for a
+ * troubled-cell sensor, beside LMPE and the learned router). */
+int hteno_kxrcf(hteno_solver* s, unsigned char* flags);
 /* Records training rows from the current state of a plain FP64 FV solver (2D or 1D): for
  * every face, characteristic field and side (the right side as the mirrored stencil), kept with
  * probability `keep` (deterministic in `seed`), the normalised 6-cell characteristic stencil the
@@ -235,8 +241,11 @@ const char* hteno_mlp_last_error(hteno_mlp* m);
  * cut-off of every stencil and count the routing errors.  m = NULL switches routing off; the
  * classifier must outlive its use by the solver. */
 int hteno_set_router(hteno_solver* s, hteno_mlp* m, float threshold, int audit_every);
-/* stats[5]: audited stencils, routed, misrouted (routed though plain TENO cut a candidate),
- * all-smooth by plain TENO, number of audited steps.  Also reports a classifier timeout. */
+/* stats[6]: audited stencils, routed, misrouted (routed though plain TENO cut a candidate; flat
+ * stencils excepted), all-smooth by plain TENO, number of audited steps, and the number of
+ * stencils the last classification handed to the network (the others were flat: their spread is
+ * below 1e-6 of their magnitude, every candidate gives the same value to float rounding, and
+ * they are routed without the network).  Also reports a classifier timeout. */
 int hteno_router_stats(hteno_solver* s, long long* stats);
 
 /* ---- Tracing: per-kernel CUDA-event timing of hteno_step ---------------------------------- */

@@ -250,3 +250,34 @@ def test_fv1d_periodic_and_linear(hteno_lib, cuda, oracle):
         want, _, _ = oracle.fv1d_run(q, 30, recon=recon, flux=0, bc=1, cfl=0.5)
         got, _, _ = gpu_run1d(hteno_lib, q, 30, recon=recon, flux=0, bc=1, cfl=0.5)
         assert rel_linf(got, want) <= TOL
+
+
+def kxrcf_ref(q, dx, bc=0):
+    """FV::System1D KXRCF flags (FV_System1D.cpp:166-192) restated in numpy."""
+    n = q.shape[1]
+    idx = lambda k: np.clip(k, 0, n - 1) if bc == 0 else k % n
+    rho = lambda k: q[0, idx(k)]
+    i = np.arange(n)
+    left = q[1] < 0.0
+    h1 = np.where(left, (2.0 * rho(i - 1) + 5.0 * rho(i) - rho(i + 1)) / 6.0,
+                  (-rho(i - 1) + 5.0 * rho(i) + 2.0 * rho(i + 1)) / 6.0)
+    h2 = np.where(left, (-rho(i - 2) + 5.0 * rho(i - 1) + 2.0 * rho(i)) / 6.0,
+                  (2.0 * rho(i) + 5.0 * rho(i + 1) - rho(i + 2)) / 6.0)
+    return (np.abs(h1 - h2) / ((dx / 2.0) ** 1.5 * np.abs(rho(i))) > 1.0).astype(np.uint8)
+
+
+def test_fv1d_kxrcf_sensor(hteno_lib, cuda):
+    """The KXRCF sensor flags the Sod tube's discontinuities and agrees with the formula."""
+    from hteno import ic
+
+    h = hteno_lib
+    with h.Solver(h.config(dims=1, nx=400, flux=1, recon=0, cfl=0.5)) as s:
+        s.set_state(ic.sod(400))
+        s.step(1 << 20, 0.2)
+        q = s.get_state()
+        f = cuda.zeros(400, dtype=cuda.uint8, device="cuda")
+        s.kxrcf(f)
+        got = f.cpu().numpy()
+    want = kxrcf_ref(q, 1.0 / 400)
+    assert (got != want).sum() <= 2  # threshold ties aside
+    assert 3 <= got.sum() <= 80 and got[:80].sum() == 0  # flags sit at the waves only
