@@ -89,13 +89,9 @@ def barrier(torch, world):
 
 
 def allreduce_max(torch, world, x):
-    if world == 1:
-        return x
-    import torch.distributed as dist
+    from hteno import replicas
 
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    return float(t.item())
+    return replicas.reduce(torch, x, "max", "cuda") if world > 1 else x
 
 
 def config_block(args, world):
@@ -362,11 +358,14 @@ def learned_path(hteno, torch, stream, args, world, n=4096):
             # accuracy: the same arm from the initial state to the FP64 arm's time
             s.set_state(q)
             s.step(1 << 20, t_ref)
-            l1, linf = density_errors(s.get_state(), ref)
+            got = s.get_state()
+            l1, linf = density_errors(got, ref)
+            shift = shock_shift(got, ref)
         d = {"value": n * n * args.c5_steps * world / (ms / 1e3) / 1e6, "unit": UNIT,
              "ms_per_step": ms / args.c5_steps, "steps": args.c5_steps,
              "speedup_vs_fp64": (ms64 / args.c5_fp64_steps) / (ms / args.c5_steps),
-             "l1_rho_vs_fp64": l1, "linf_rho_vs_fp64": linf, "t_compared": t_ref}
+             "l1_rho_vs_fp64": l1, "linf_rho_vs_fp64": linf, "shock_shift_cells": shift,
+             "t_compared": t_ref}
         if st is not None:
             d["router"] = {"audited_stencils": st["seen"], "routed_fraction": st["routed"] / max(1, st["seen"]),
                            "network_rows_last_step": st["network_rows"],
@@ -408,8 +407,15 @@ def sod_path(hteno, torch):
 
 
 def density_errors(a, b):
-    d = np.abs(a[0] - b[0])
-    return float(d.mean()), float(d.max())
+    from hteno import metrics
+
+    return metrics.density_errors(a, b)
+
+
+def shock_shift(a, b):
+    from hteno import metrics
+
+    return metrics.shock_shift(a[0], b[0])
 
 
 def mixed_path(hteno, torch, q, stream, args, t_end, ref_state, ms_plain, world):

@@ -117,20 +117,17 @@ __device__ __forceinline__ float teno_side_s(float p0, float p1, float p2, const
 }
 
 // Audit counters of the learned router: stencils seen, routed to the linear weights, routed
-// although the plain TENO cut-off would not have kept all three candidates (flat stencils, whose
-// candidates coincide to float rounding, excepted), all-smooth by TENO.
+// although the plain TENO cut-off would not have kept all three candidates (flat stencils, six
+// equal float values, excepted: their float cut-off bits are rounding noise), all-smooth by TENO.
 struct RouteCount {
   int seen = 0, routed = 0, misrouted = 0, smooth = 0;
 };
 
 __device__ __forceinline__ bool flat6(const float* u) {
-  float hi = u[0], lo = u[0];
+  bool eq = true;
 #pragma unroll
-  for (int m = 1; m < 6; ++m) {
-    hi = fmaxf(hi, u[m]);
-    lo = fminf(lo, u[m]);
-  }
-  return !(hi - lo > 1e-6f * fmaxf(fabsf(hi), fabsf(lo)));
+  for (int m = 1; m < 6; ++m) eq &= u[m] == u[0];
+  return eq;
 }
 
 // recon_s with routing: a side whose route bit is set takes the optimal linear weights (the TENO

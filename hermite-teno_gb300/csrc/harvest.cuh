@@ -40,11 +40,18 @@ __device__ __forceinline__ int label(const double* w, bool improved) {
   return par::cutoff_pattern(SI, tau, HTENO_LAG_EPSZ, HTENO_LAG_CT);
 }
 
-// A stencil whose spread is below HTENO_FLAT_SPREAD of its magnitude is "flat": every TENO
-// candidate gives the same value to within float rounding, so its cut-off bits (set by rounding
-// noise) do not matter.  Flat stencils are not recorded, and the router sends them to the linear
-// weights without asking the network.
-#define HTENO_FLAT_SPREAD 1e-6
+// A stencil whose six values are equal once rounded to float is "flat": the float
+// reconstruction of the mixed path sees a constant, for which plain TENO keeps all three
+// candidates, so it takes the linear weights without asking the network (losslessly).  The
+// plain FP64 solver's cut-off bits on such stencils are set by rounding noise (~1e-16 relative
+// differences left by the flux evaluation in constant regions), so they are not recorded.
+__device__ __forceinline__ bool flat_in_float(const double* w) {
+  const float f0 = __double2float_rn(w[0]);
+#pragma unroll
+  for (int k = 1; k < 6; ++k)
+    if (__double2float_rn(w[k]) != f0) return false;
+  return true;
+}
 
 // Appends (normalised stencil as BF16 [8], label) unless the buffer is full; `count` keeps
 // counting past the capacity so the caller sees how many were offered.  Normalised values are
@@ -59,7 +66,7 @@ __device__ __forceinline__ void emit(const double* w, int lab, uint16_t* X, uint
     mn = fmin(mn, w[k]);
   }
   mean /= 6.0;
-  if (!(mx - mn > HTENO_FLAT_SPREAD * fmax(fabs(mx), fabs(mn)))) return;  // flat (or NaN)
+  if (flat_in_float(w) || !(mx - mn >= 0.0)) return;  // flat, or NaN
   const double inv = 1.0 / (mx - mn + 1e-30);
   const unsigned long long slot = atomicAdd(count, 1ull);
   if (slot >= (unsigned long long)cap) return;

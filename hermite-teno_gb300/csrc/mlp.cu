@@ -24,9 +24,6 @@
 
 #include "fv2d_fused.cuh"
 #include "hteno_internal.h"
-#ifndef HTENO_FLAT_SPREAD
-#define HTENO_FLAT_SPREAD 1e-6  // same flatness rule as the harvest (harvest.cuh)
-#endif
 #include "mlp_internal.cuh"
 
 struct hteno_mlp;
@@ -441,8 +438,8 @@ __global__ void __launch_bounds__(256) k_route_prep(Geo G, const double* __restr
         hi = fmaxf(hi, w[m]);
         lo = fminf(lo, w[m]);
       }
-      if (!(hi - lo > float(HTENO_FLAT_SPREAD) * fmaxf(fabsf(hi), fabsf(lo)))) {
-        byte |= uint8_t(1u << b);  // flat: routed without the network
+      if (hi == lo) {  // flat in float: plain TENO keeps all three candidates; no network needed
+        byte |= uint8_t(1u << b);
         continue;
       }
       mean *= (1.0f / 6.0f);

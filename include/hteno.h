@@ -243,9 +243,9 @@ const char* hteno_mlp_last_error(hteno_mlp* m);
 int hteno_set_router(hteno_solver* s, hteno_mlp* m, float threshold, int audit_every);
 /* stats[6]: audited stencils, routed, misrouted (routed though plain TENO cut a candidate; flat
  * stencils excepted), all-smooth by plain TENO, number of audited steps, and the number of
- * stencils the last classification handed to the network (the others were flat: their spread is
- * below 1e-6 of their magnitude, every candidate gives the same value to float rounding, and
- * they are routed without the network).  Also reports a classifier timeout. */
+ * stencils the last classification handed to the network (the others were flat: six equal float
+ * values, for which plain TENO keeps all three candidates, routed without the network).  Also
+ * reports a classifier timeout. */
 int hteno_router_stats(hteno_solver* s, long long* stats);
 
 /* ---- Tracing: per-kernel CUDA-event timing of hteno_step ---------------------------------- */
