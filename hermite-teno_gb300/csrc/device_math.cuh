@@ -142,7 +142,56 @@ __device__ __forceinline__ T teno_side(const DevConst& C, T p0, T p1, T p2, cons
   return catchnan(p0 * w[0] + p1 * w[1] + p2 * w[2]);
 }
 
-// kind: 0 teno5, 1 teno5i, 2 linear.  u[0..5] -> (u^-_{i+1/2}, u^+_{i+1/2}).
+// The selectable alternatives (Schemes_Lagrange.cpp:358-594, 1265-1294), one side, compute type
+// T: kind 3 weno5JS, 4 weno5Z, 5 weno5N, 6 teno5N, 7 teno5a.  tab: this side's TENO weights per
+// cut-off pattern [8][3]; d: its optimal weights.  The WENO weights are scaled by the smallest
+// denominator so float stays in range.
+template <typename T>
+__device__ __forceinline__ T alt_side(int kind, T p0, T p1, T p2, const T* v, const T (*tab)[3],
+                                      const T* d) {
+  T SI0, SI1, SI2, w0, w1, w2;
+  if (kind == 5 || kind == 6) {
+    SI2 = T(0.1) * fabs(v[0] - T(3.0) * v[1] + T(2.0) * v[2]) + fabs(v[0] - T(2.0) * v[1] + v[2]);
+    SI1 = T(0.1) * fabs(v[3] - v[2]) + fabs(v[1] - T(2.0) * v[2] + v[3]);
+    SI0 = T(0.1) * fabs(v[3] - v[2]) + fabs(v[2] - T(2.0) * v[3] + v[4]);
+    const T x = fabs(v[0] - T(4.0) * v[1] + T(6.0) * v[2] - T(4.0) * v[3] + v[4]);
+    const T e0 = SI0 + T(HTENO_LAG_EPS), e1 = SI1 + T(HTENO_LAG_EPS), e2 = SI2 + T(HTENO_LAG_EPS);
+    if (kind == 5) {
+      const T tau = x * x * sqrt(x);  // |.|^2.5
+      w0 = d[0] * (T(1.0) + tau * Cst<T>::rcp(e0 * e0));
+      w1 = d[1] * (T(1.0) + tau * Cst<T>::rcp(e1 * e1));
+      w2 = d[2] * (T(1.0) + tau * Cst<T>::rcp(e2 * e2));
+    } else {
+      const T tau = x * x;
+      const int pat = teno_pattern(T(1.0) + tau * Cst<T>::rcp(e0 * e0), T(1.0) + tau * Cst<T>::rcp(e1 * e1),
+                                   T(1.0) + tau * Cst<T>::rcp(e2 * e2), T(HTENO_LAG_CT));
+      return catchnan(p0 * tab[pat][0] + p1 * tab[pat][1] + p2 * tab[pat][2]);
+    }
+  } else {
+    lagrange_si(v, SI0, SI1, SI2);
+    if (kind == 3) {
+      const T e0 = T(HTENO_LAG_EPS) + SI0, e1 = T(HTENO_LAG_EPS) + SI1, e2 = T(HTENO_LAG_EPS) + SI2;
+      const T em = fmin(fmin(e0, e1), e2);
+      const T a0 = em * Cst<T>::rcp(e0), a1 = em * Cst<T>::rcp(e1), a2 = em * Cst<T>::rcp(e2);
+      w0 = d[0] * a0 * a0;
+      w1 = d[1] * a1 * a1;
+      w2 = d[2] * a2 * a2;
+    } else if (kind == 4) {
+      const T tau = fabs(SI2 - SI0), ez = Cst<T>::epsz();
+      w0 = d[0] * (T(1.0) + tau * Cst<T>::rcp(SI0 + ez));
+      w1 = d[1] * (T(1.0) + tau * Cst<T>::rcp(SI1 + ez));
+      w2 = d[2] * (T(1.0) + tau * Cst<T>::rcp(SI2 + ez));
+    } else {  // teno5a
+      const T ez = Cst<T>::epsz();
+      const int pat = teno_pattern(Cst<T>::rcp(SI0 + ez), Cst<T>::rcp(SI1 + ez), Cst<T>::rcp(SI2 + ez),
+                                   T(HTENO_LAG_CT));
+      return catchnan(p0 * tab[pat][0] + p1 * tab[pat][1] + p2 * tab[pat][2]);
+    }
+  }
+  return catchnan((p0 * w0 + p1 * w1 + p2 * w2) * Cst<T>::rcp(w0 + w1 + w2));
+}
+
+// kind: 0 teno5, 1 teno5i, 2 linear, 3..7 the alternatives.  u[0..5] -> (u^-, u^+) at i+1/2.
 template <typename T>
 __device__ __forceinline__ void lagrange_recon(const DevConst& C, int kind, const T* u, T& outm,
                                                T& outp) {
@@ -153,6 +202,8 @@ __device__ __forceinline__ void lagrange_recon(const DevConst& C, int kind, cons
   if (kind == 2) {
     const T* w = K::wtab(C, 0, 7);
     outm = p0 * w[0] + p1 * w[1] + p2 * w[2];
+  } else if (kind >= 3) {
+    outm = alt_side(kind, p0, p1, p2, u, reinterpret_cast<const T(*)[3]>(K::wtab(C, 0, 0)), K::wtab(C, 0, 7));
   } else {
     outm = teno_side(C, p0, p1, p2, u, 0, kind == 1);
   }
@@ -162,6 +213,9 @@ __device__ __forceinline__ void lagrange_recon(const DevConst& C, int kind, cons
   if (kind == 2) {
     const T* w = K::wtab(C, 1, 7);
     outp = p0 * w[0] + p1 * w[1] + p2 * w[2];
+  } else if (kind >= 3) {
+    outp = alt_side(kind, p0, p1, p2, u + 1, reinterpret_cast<const T(*)[3]>(K::wtab(C, 1, 0)),
+                    K::wtab(C, 1, 7));
   } else {
     outp = teno_side(C, p0, p1, p2, u + 1, 1, kind == 1);
   }

@@ -269,7 +269,7 @@ int hteno_batch_create(const hteno_config* cfgs, int n, hteno_batch** out) {
     if (c.dims != 2 || c.scheme != HTENO_SCHEME_FV || c.precision != HTENO_PREC_MIXED)
       return HTENO_ERR_UNSUPPORTED;
     if (c.nx < 6 || c.ny < 6 || (long long)c.nx * c.ny > (1ll << 30) || !(c.xr > c.xl) ||
-        !(c.yt > c.yb) || !(c.cfl > 0.0) || !(c.gamma > 1.0) || c.recon < 0 || c.recon > 2 ||
+        !(c.yt > c.yb) || !(c.cfl > 0.0) || !(c.gamma > 1.0) || c.recon < 0 || c.recon > 7 ||
         c.flux < 0 || c.flux > 1 || c.bc < 0 || c.bc > 1)
       return HTENO_ERR_INVALID_ARG;
   }

@@ -198,6 +198,8 @@ int hteno_set_router(hteno_solver* s, hteno_mlp* m, float threshold, int audit_e
   if (!s || !(threshold > 0.f && threshold < 1.f) || audit_every < 0) return HTENO_ERR_INVALID_ARG;
   if (s->cfg.dims != 2 || s->cfg.scheme != HTENO_SCHEME_FV || s->cfg.precision != HTENO_PREC_MIXED)
     return set_error(s, HTENO_ERR_UNSUPPORTED, "learned routing runs on the mixed FV 2D path");
+  if (s->cfg.recon != HTENO_RECON_TENO5 && s->cfg.recon != HTENO_RECON_TENO5I)
+    return set_error(s, HTENO_ERR_UNSUPPORTED, "learned routing predicts TENO cut-offs (teno5, teno5i)");
   cudaStreamSynchronize(s->stream);
   if (!m) {
     s->router = nullptr;

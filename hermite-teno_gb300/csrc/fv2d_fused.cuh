@@ -108,83 +108,77 @@ __device__ __forceinline__ int teno_pat_s(const float* v, bool improved) {
   return teno_pattern(r0, r1, r2, float(HTENO_LAG_CT));
 }
 
-// One side of teno5 / teno5i with the weight table in shared memory (a per-thread pattern
-// would serialise constant-memory reads).
-__device__ __forceinline__ float teno_side_s(float p0, float p1, float p2, const float* v,
-                                             const float (*tab)[3], bool improved) {
-  const float* w = tab[teno_pat_s(v, improved)];
+// A side's 5-cell window of equal float values: the smoothness indicators vanish, all three
+// TENO ratios are equal, and the cut-off keeps every candidate (pattern 7) -- the linear weights,
+// which are therefore taken without evaluating the indicators (the same result, bit for bit).
+__device__ __forceinline__ bool flat5(const float* v) {
+  return v[1] == v[0] && v[2] == v[0] && v[3] == v[0] && v[4] == v[0];
+}
+
+__device__ __forceinline__ float weighted(float p0, float p1, float p2, const float* w) {
   return catchnan(p0 * w[0] + p1 * w[1] + p2 * w[2]);
 }
 
-// Audit counters of the learned router: stencils seen, routed to the linear weights, routed
-// although the plain TENO cut-off would not have kept all three candidates (flat stencils, six
-// equal float values, excepted: their float cut-off bits are rounding noise), all-smooth by TENO.
-struct RouteCount {
-  int seen = 0, routed = 0, misrouted = 0, smooth = 0;
-};
-
-__device__ __forceinline__ bool flat6(const float* u) {
-  bool eq = true;
-#pragma unroll
-  for (int m = 1; m < 6; ++m) eq &= u[m] == u[0];
-  return eq;
-}
-
-// recon_s with routing: a side whose route bit is set takes the optimal linear weights (the TENO
-// result when all three cut-off bits are on) without evaluating the smoothness indicators; when
-// auditing, the plain cut-off is evaluated as well and compared.
-__device__ __forceinline__ void recon_routed(const DevConst& C, int kind, const float (*tab)[8][3],
-                                             const float* u, int route, bool audit, RouteCount& rc,
-                                             float& outm, float& outp) {
-  const bool impr = kind == 1;
-  float p0 = C.f_crj[0][1] * u[2] + C.f_crj[1][1] * u[3] + C.f_crj[2][1] * u[4];
-  float p1 = C.f_crj[0][2] * u[1] + C.f_crj[1][2] * u[2] + C.f_crj[2][2] * u[3];
-  float p2 = C.f_crj[0][3] * u[0] + C.f_crj[1][3] * u[1] + C.f_crj[2][3] * u[2];
-  if (kind == 2 || ((route & 1) && !audit)) {
-    outm = p0 * tab[0][7][0] + p1 * tab[0][7][1] + p2 * tab[0][7][2];
-  } else {
-    const int pat = teno_pat_s(u, impr);
-    const float* w = (route & 1) ? tab[0][7] : tab[0][pat];
-    outm = catchnan(p0 * w[0] + p1 * w[1] + p2 * w[2]);
-    if (audit) {
-      rc.seen += 1;
-      rc.smooth += pat == 7;
-      rc.routed += route & 1;
-      rc.misrouted += (route & 1) && pat != 7 && !flat6(u);
-    }
-  }
-  p0 = C.f_crj[0][0] * u[3] + C.f_crj[1][0] * u[4] + C.f_crj[2][0] * u[5];
-  p1 = C.f_crj[0][1] * u[2] + C.f_crj[1][1] * u[3] + C.f_crj[2][1] * u[4];
-  p2 = C.f_crj[0][2] * u[1] + C.f_crj[1][2] * u[2] + C.f_crj[2][2] * u[3];
-  if (kind == 2 || ((route & 2) && !audit)) {
-    outp = p0 * tab[1][7][0] + p1 * tab[1][7][1] + p2 * tab[1][7][2];
-  } else {
-    const int pat = teno_pat_s(u + 1, impr);
-    const float* w = (route & 2) ? tab[1][7] : tab[1][pat];
-    outp = catchnan(p0 * w[0] + p1 * w[1] + p2 * w[2]);
-    if (audit) {
-      rc.seen += 1;
-      rc.smooth += pat == 7;
-      rc.routed += (route >> 1) & 1;
-      rc.misrouted += (route & 2) && pat != 7 && !flat6(u);
-    }
-  }
-}
-
-// teno5 (Schemes_Lagrange.cpp:481-511), teno5i (:1235-1263) or linear (:1219-1233):
-// u[0..5] -> (u^-_{i+1/2}, u^+_{i+1/2}).
+// teno5 (Schemes_Lagrange.cpp:481-511), teno5i (:1235-1263), linear (:1219-1233) or one of the
+// alternatives: u[0..5] -> (u^-_{i+1/2}, u^+_{i+1/2}).  The weight tables live in shared memory:
+// a per-thread pattern would serialise constant-memory reads.
 __device__ __forceinline__ void recon_s(const DevConst& C, int kind, const float (*tab)[8][3],
                                         const float* u, float& outm, float& outp) {
   float p0 = C.f_crj[0][1] * u[2] + C.f_crj[1][1] * u[3] + C.f_crj[2][1] * u[4];
   float p1 = C.f_crj[0][2] * u[1] + C.f_crj[1][2] * u[2] + C.f_crj[2][2] * u[3];
   float p2 = C.f_crj[0][3] * u[0] + C.f_crj[1][3] * u[1] + C.f_crj[2][3] * u[2];
   if (kind == 2) outm = p0 * tab[0][7][0] + p1 * tab[0][7][1] + p2 * tab[0][7][2];
-  else outm = teno_side_s(p0, p1, p2, u, tab[0], kind == 1);
+  else if (kind >= 3) outm = alt_side(kind, p0, p1, p2, u, tab[0], tab[0][7]);
+  else outm = weighted(p0, p1, p2, tab[0][flat5(u) ? 7 : teno_pat_s(u, kind == 1)]);
   p0 = C.f_crj[0][0] * u[3] + C.f_crj[1][0] * u[4] + C.f_crj[2][0] * u[5];
   p1 = C.f_crj[0][1] * u[2] + C.f_crj[1][1] * u[3] + C.f_crj[2][1] * u[4];
   p2 = C.f_crj[0][2] * u[1] + C.f_crj[1][2] * u[2] + C.f_crj[2][2] * u[3];
   if (kind == 2) outp = p0 * tab[1][7][0] + p1 * tab[1][7][1] + p2 * tab[1][7][2];
-  else outp = teno_side_s(p0, p1, p2, u + 1, tab[1], kind == 1);
+  else if (kind >= 3) outp = alt_side(kind, p0, p1, p2, u + 1, tab[1], tab[1][7]);
+  else outp = weighted(p0, p1, p2, tab[1][flat5(u + 1) ? 7 : teno_pat_s(u + 1, kind == 1)]);
+}
+
+// Audit counters of the learned router: stencils seen, routed to the linear weights, routed
+// although the plain TENO cut-off would not have kept all three candidates, all-smooth by TENO.
+struct RouteCount {
+  int seen = 0, routed = 0, misrouted = 0, smooth = 0;
+};
+
+// recon_s with routing: a side whose route bit is set takes the optimal linear weights (the TENO
+// result when all three cut-off bits are on) without evaluating the smoothness indicators; flat
+// windows take them as in recon_s; when auditing, the plain cut-off is evaluated as well and
+// compared.  TENO kinds only (0, 1).
+__device__ __forceinline__ void recon_routed(const DevConst& C, int kind, const float (*tab)[8][3],
+                                             const float* u, int route, bool audit, RouteCount& rc,
+                                             float& outm, float& outp) {
+  const bool impr = kind == 1;
+#pragma unroll
+  for (int side = 0; side < 2; ++side) {
+    const float* v = u + side;
+    float p0, p1, p2;
+    if (side == 0) {
+      p0 = C.f_crj[0][1] * u[2] + C.f_crj[1][1] * u[3] + C.f_crj[2][1] * u[4];
+      p1 = C.f_crj[0][2] * u[1] + C.f_crj[1][2] * u[2] + C.f_crj[2][2] * u[3];
+      p2 = C.f_crj[0][3] * u[0] + C.f_crj[1][3] * u[1] + C.f_crj[2][3] * u[2];
+    } else {
+      p0 = C.f_crj[0][0] * u[3] + C.f_crj[1][0] * u[4] + C.f_crj[2][0] * u[5];
+      p1 = C.f_crj[0][1] * u[2] + C.f_crj[1][1] * u[3] + C.f_crj[2][1] * u[4];
+      p2 = C.f_crj[0][2] * u[1] + C.f_crj[1][2] * u[2] + C.f_crj[2][2] * u[3];
+    }
+    const bool routed = (route >> side) & 1;
+    const bool flat = flat5(v);
+    int pat = 7;
+    if (!flat && (!routed || audit)) pat = teno_pat_s(v, impr);
+    const float o = weighted(p0, p1, p2, tab[side][(routed || flat) ? 7 : pat]);
+    if (side == 0) outm = o;
+    else outp = o;
+    if (audit) {
+      rc.seen += 1;
+      rc.smooth += pat == 7;
+      rc.routed += routed;
+      rc.misrouted += routed && pat != 7;
+    }
+  }
 }
 
 // Pointers of one stage of one grid.

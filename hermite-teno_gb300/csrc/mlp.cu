@@ -374,10 +374,11 @@ __global__ void __launch_bounds__(128) k_predict(Weights W, const uint16_t* __re
 
 // Learned routing of a mixed FV 2D grid, pass 1: one thread per face (x faces, then y faces)
 // computes the 8 stencils the fused kernel will reconstruct (4 characteristic fields x 2 sides,
-// float, from the double state as the fused kernel sees it).  Flat stencils are routed at once
-// (their route bits form the face's mask byte); the others are appended, normalised and in BF16,
-// to the row list for the network, with (face << 3 | bit) beside each.  Appends are aggregated
-// per block: one atomic per block.
+// float, from the double state as the fused kernel sees it) and clears the face's mask byte.
+// Flat stencils (six equal float values) are left alone: the stage kernel takes the linear
+// weights for flat windows by itself.  The others are appended, normalised and in BF16, to the
+// row list for the network, with (face << 3 | bit) beside each.  Appends are aggregated per
+// block: one atomic per block.
 __global__ void __launch_bounds__(256) k_route_prep(Geo G, const double* __restrict__ q,
                                                     uint8_t* __restrict__ mx, uint8_t* __restrict__ my,
                                                     uint4* __restrict__ rows,
@@ -438,10 +439,7 @@ __global__ void __launch_bounds__(256) k_route_prep(Geo G, const double* __restr
         hi = fmaxf(hi, w[m]);
         lo = fminf(lo, w[m]);
       }
-      if (hi == lo) {  // flat in float: plain TENO keeps all three candidates; no network needed
-        byte |= uint8_t(1u << b);
-        continue;
-      }
+      if (hi == lo) continue;  // flat in float: the stage kernel takes the linear weights itself
       mean *= (1.0f / 6.0f);
       const float inv = 1.0f / (hi - lo);
       uint16_t f[8] = {0, 0, 0, 0, 0, 0, 0, 0};

@@ -118,18 +118,117 @@ __device__ __forceinline__ double teno_side(const DevConst& C, const double* p, 
   return catchnan(dot3v(p, w));
 }
 
-// kind 0 teno5, 1 teno5i, 2 linear (:1219-1233)
+// ---- the selectable alternatives (Schemes_Lagrange.cpp:358-594, 1265-1294), one side each ----
+
+// Cut-off pattern from the exact ratios r_k, whose sixth powers are the reference's raw weights:
+// fast path on (r_k / r_max)^6 with a guard band, the reference's pow-and-divide inside it.
+__device__ __forceinline__ int cutoff_from_r(const double* r, double ct) {
+  const double rm = fmax(fmax(r[0], r[1]), r[2]);
+  const double inv = __drcp_rn(rm);
+  double a[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    double x = r[k] * inv;
+    x = x * x;
+    a[k] = x * x * x;
+  }
+  const double lim = ct * ((a[0] + a[1]) + a[2]);
+  int pat = 0;
+  bool near = false;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    pat |= (a[k] < lim ? 0 : 1) << k;
+    near |= fabs(a[k] - lim) <= 1e-10 * lim;
+  }
+  if (near || !(rm < 1e300)) {  // the reference's arithmetic (also for overflowing ratios)
+    double w[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) w[k] = pow(r[k], 6.0);
+    const double s = (w[0] + w[1]) + w[2];
+    pat = 0;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) pat |= ((w[k] / s) < ct ? 0 : 1) << k;
+  }
+  return pat;
+}
+
+__device__ __forceinline__ double normalised(const double* p, double* w) {
+  const double s = (w[0] + w[1]) + w[2];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) w[k] = w[k] / s;
+  return catchnan(dot3v(p, w));
+}
+
+// weno5N / teno5N indicators (:445-450) on the side's window v[0..4]; returns the 5-point
+// difference |v0 - 4v1 + 6v2 - 4v3 + v4|
+__device__ __forceinline__ double n_indicators(const double* v, double* SI) {
+  SI[2] = 0.1 * fabs(v[0] - 3.0 * v[1] + 2.0 * v[2]) + fabs(v[0] - 2.0 * v[1] + v[2]);
+  SI[1] = 0.1 * fabs(v[3] - v[2]) + fabs(v[1] - 2.0 * v[2] + v[3]);
+  SI[0] = 0.1 * fabs(v[3] - v[2]) + fabs(v[2] - 2.0 * v[3] + v[4]);
+  return fabs(v[0] - 4.0 * v[1] + 6.0 * v[2] - 4.0 * v[3] + v[4]);
+}
+
+// kind 3 weno5JS, 4 weno5Z, 5 weno5N, 6 teno5N, 7 teno5a
+__device__ __forceinline__ double alt_side(const DevConst& C, int kind, const double* p,
+                                           const double* v, int side) {
+  const double* d = side ? C.dkp : C.dkm;
+  double SI[3], w[3];
+  if (kind == 3 || kind == 4 || kind == 7) lagrange_si(v, SI);
+  if (kind == 3) {  // w_k = d_k / (eps + SI_k)^2
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const double e = HTENO_LAG_EPS + SI[k];
+      w[k] = d[k] / (e * e);
+    }
+    return normalised(p, w);
+  }
+  if (kind == 4) {  // tau = |SI_2 - SI_0|, w_k = d_k (1 + tau / (SI_k + epsz))
+    const double tau = fabs(SI[2] - SI[0]);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) w[k] = d[k] * (1.0 + (tau / (SI[k] + HTENO_LAG_EPSZ)));
+    return normalised(p, w);
+  }
+  if (kind == 5) {  // tau = |5-point difference|^2.5, w_k = d_k (1 + tau / (SI_k + eps)^2)
+    const double tau = pow(n_indicators(v, SI), 2.5);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const double e = SI[k] + HTENO_LAG_EPS;
+      w[k] = d[k] * (1.0 + (tau / (e * e)));
+    }
+    return normalised(p, w);
+  }
+  double r[3];
+  if (kind == 6) {  // r_k = 1 + tau / (SI_k + eps)^2, tau = |5-point difference|^2
+    const double x = n_indicators(v, SI);
+    const double tau = x * x;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const double e = SI[k] + HTENO_LAG_EPS;
+      r[k] = 1.0 + tau / (e * e);
+    }
+  } else {  // teno5a: r_k = 1 / (SI_k + epsz)
+#pragma unroll
+    for (int k = 0; k < 3; ++k) r[k] = 1.0 / (SI[k] + HTENO_LAG_EPSZ);
+  }
+  const int pat = cutoff_from_r(r, HTENO_LAG_CT);
+  const double* tw = side ? C.wtab_p[pat] : C.wtab_m[pat];
+  return catchnan(dot3v(p, tw));
+}
+
+// kind 0 teno5, 1 teno5i, 2 linear (:1219-1233), 3..7 the alternatives above
 __device__ __forceinline__ void lagrange_recon(const DevConst& C, int kind, const double* u,
                                                double& outm, double& outp) {
   double p[3];
   p[0] = dot3(C.crj[0][1], C.crj[1][1], C.crj[2][1], u + 2);
   p[1] = dot3(C.crj[0][2], C.crj[1][2], C.crj[2][2], u + 1);
   p[2] = dot3(C.crj[0][3], C.crj[1][3], C.crj[2][3], u + 0);
-  outm = kind == 2 ? dot3v(p, C.dkm) : teno_side(C, p, u, 0, kind == 1);
+  outm = kind == 2 ? dot3v(p, C.dkm) : kind >= 3 ? alt_side(C, kind, p, u, 0)
+                                                 : teno_side(C, p, u, 0, kind == 1);
   p[0] = dot3(C.crj[0][0], C.crj[1][0], C.crj[2][0], u + 3);
   p[1] = dot3(C.crj[0][1], C.crj[1][1], C.crj[2][1], u + 2);
   p[2] = dot3(C.crj[0][2], C.crj[1][2], C.crj[2][2], u + 1);
-  outp = kind == 2 ? dot3v(p, C.dkp) : teno_side(C, p, u + 1, 1, kind == 1);
+  outp = kind == 2 ? dot3v(p, C.dkp) : kind >= 3 ? alt_side(C, kind, p, u + 1, 1)
+                                                 : teno_side(C, p, u + 1, 1, kind == 1);
 }
 
 // weno5JS3PointsQuadrature (Schemes_Lagrange.cpp:1155-1217)

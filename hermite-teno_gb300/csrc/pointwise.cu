@@ -206,7 +206,7 @@ using namespace hteno;
 extern "C" {
 
 int hteno_lagrange_batch(int kind, int precision, const double* u, double* out, long n, void* stream) {
-  HTENO_CHECK_N(n, !u || !out || kind < 0 || kind > 2);
+  HTENO_CHECK_N(n, !u || !out || kind < 0 || kind > 7);
   cudaStream_t st;
   if (prep(stream, &st)) return HTENO_ERR_CUDA;
   if (precision == HTENO_PREC_MIXED)

@@ -173,7 +173,7 @@ int hteno_create(const hteno_config* cfg, hteno_solver** out) {
     return HTENO_ERR_INVALID_ARG;
   if (!(c.xr > c.xl) || (c.dims == 2 && !(c.yt > c.yb))) return HTENO_ERR_INVALID_ARG;
   if (!(c.cfl > 0.0) || !(c.gamma > 1.0)) return HTENO_ERR_INVALID_ARG;
-  if (c.recon < 0 || c.recon > 2 || c.flux < 0 || c.flux > 1 || c.bc < 0 || c.bc > 1 ||
+  if (c.recon < 0 || c.recon > 7 || c.flux < 0 || c.flux > 1 || c.bc < 0 || c.bc > 1 ||
       c.precision < 0 || c.precision > 1)
     return HTENO_ERR_INVALID_ARG;
 

@@ -36,13 +36,20 @@ typedef enum { HTENO_HOST = 0, HTENO_DEVICE = 1 } hteno_where;
 
 typedef enum { HTENO_SCHEME_FV = 0, HTENO_SCHEME_HERMITE = 1 } hteno_scheme;
 
-/* Reconstruction.  FV: Schemes::Lagrange::teno5 / teno5i / linear.
- * Hermite 2D: hteno (the reference's choice).  Hermite 1D: LMPE routing (htenoi on troubled
- * cells, linear elsewhere, FVHermite_System1D.cpp:239-290). */
+/* Reconstruction.  FV: Schemes::Lagrange::teno5 / teno5i / linear, and the reference's other
+ * selectable 5th-order schemes weno5JS, weno5Z, weno5N, teno5N, teno5a
+ * (Schemes_Lagrange.cpp:358-594, 1265-1294).  Hermite 2D: hteno (the reference's choice).
+ * Hermite 1D: LMPE routing (htenoi on troubled cells, linear elsewhere,
+ * FVHermite_System1D.cpp:239-290). */
 typedef enum {
   HTENO_RECON_TENO5 = 0,
   HTENO_RECON_TENO5I = 1,
-  HTENO_RECON_LINEAR = 2
+  HTENO_RECON_LINEAR = 2,
+  HTENO_RECON_WENO5JS = 3,
+  HTENO_RECON_WENO5Z = 4,
+  HTENO_RECON_WENO5N = 5,
+  HTENO_RECON_TENO5N = 6,
+  HTENO_RECON_TENO5A = 7
 } hteno_recon;
 
 typedef enum { HTENO_FLUX_RUSANOV = 0, HTENO_FLUX_HLLC = 1 } hteno_flux;
@@ -121,7 +128,8 @@ const char* hteno_status_string(int status);
 /* ---- Pointwise batch kernels (device pointers), one reference function each ------------- */
 
 /* Schemes::Lagrange::teno5 / teno5i / linear (Schemes_Lagrange.cpp:481-511, 1235-1263,
- * 1219-1233): u[n][6] -> out[n][2] = (u^-_{i+1/2}, u^+_{i+1/2}).  kind: hteno_recon.
+ * 1219-1233) and the alternatives of hteno_recon: u[n][6] -> out[n][2] =
+ * (u^-_{i+1/2}, u^+_{i+1/2}).  kind: hteno_recon.
  * precision: HTENO_PREC_FP64 computes in double, HTENO_PREC_MIXED in float. */
 int hteno_lagrange_batch(int kind, int precision, const double* u, double* out, long n,
                          void* stream);

@@ -178,7 +178,120 @@ inline T teno_side(const T* p, const T* v, const double* d, bool improved) {
   return catchnan(dot3(p, w), T(K.machine_eps));
 }
 
-// kind: 0 teno5, 1 teno5i, 2 linear.  u[0..5] -> out[0] = u^-_{i+1/2}, out[1] = u^+_{i+1/2}
+// The selectable alternatives of Schemes::Lagrange, one side each.  v[0..4] is the side's
+// 5-cell window (the left side's u[0..4], the right side's u[1..5]), as smoothnessMeasure sees it.
+
+// cutOff (:1141-1149) of raw weights w followed by the sigma-weighted optimal weights
+template <typename T>
+inline T cutoff_weighted(const T* p, T* w, const double* d) {
+  const LagrangeCoef& K = lag();
+  T s = (w[0] + w[1]) + w[2];
+  T sig[3];
+  for (int k = 0; k < 3; ++k) {
+    w[k] = w[k] / s;
+    sig[k] = w[k] < T(K.ct) ? T(0.0) : T(1.0);
+  }
+  for (int k = 0; k < 3; ++k) w[k] = sig[k] * T(d[k]);
+  s = (w[0] + w[1]) + w[2];
+  for (int k = 0; k < 3; ++k) w[k] = w[k] / s;
+  return catchnan(dot3(p, w), T(K.machine_eps));
+}
+
+template <typename T>
+inline T normalised(const T* p, T* w) {
+  const LagrangeCoef& K = lag();
+  const T s = (w[0] + w[1]) + w[2];
+  for (int k = 0; k < 3; ++k) w[k] = w[k] / s;
+  return catchnan(dot3(p, w), T(K.machine_eps));
+}
+
+// weno5JS (:358-381): w_k = d_k / (eps + SI_k)^2
+template <typename T>
+inline T weno5js_side(const T* p, const T* v, const double* d) {
+  const LagrangeCoef& K = lag();
+  T SI[3], w[3];
+  lagrange_si(v, SI);
+  for (int k = 0; k < 3; ++k) {
+    const T e = T(K.eps) + SI[k];
+    w[k] = T(d[k]) / (e * e);
+  }
+  return normalised(p, w);
+}
+
+// weno5Z (:383-408): tau = |SI_2 - SI_0|, w_k = d_k (1 + tau / (SI_k + epsz))
+template <typename T>
+inline T weno5z_side(const T* p, const T* v, const double* d) {
+  const LagrangeCoef& K = lag();
+  T SI[3], w[3];
+  lagrange_si(v, SI);
+  const T tau = fabs(SI[2] - SI[0]);
+  for (int k = 0; k < 3; ++k) w[k] = T(d[k]) * (T(1.0) + (tau / (SI[k] + T(K.epsz))));
+  return normalised(p, w);
+}
+
+// The indicators of weno5N / teno5N (:445-450 and :558-563) on the side's window v[0..4]:
+// SI_2 = theta |v0 - 3v1 + 2v2| + |v0 - 2v1 + v2|, SI_1 = theta |v3 - v2| + |v1 - 2v2 + v3|,
+// SI_0 = theta |v3 - v2| + |v2 - 2v3 + v4|; and the 5-point difference v0 - 4v1 + 6v2 - 4v3 + v4.
+template <typename T>
+inline T n_indicators(const T* v, T* SI) {
+  const T theta = T(0.1);
+  SI[2] = theta * fabs(v[0] - T(3.0) * v[1] + T(2.0) * v[2]) + fabs(v[0] - T(2.0) * v[1] + v[2]);
+  SI[1] = theta * fabs(v[3] - v[2]) + fabs(v[1] - T(2.0) * v[2] + v[3]);
+  SI[0] = theta * fabs(v[3] - v[2]) + fabs(v[2] - T(2.0) * v[3] + v[4]);
+  return fabs(v[0] - T(4.0) * v[1] + T(6.0) * v[2] - T(4.0) * v[3] + v[4]);
+}
+
+// weno5N (:440-479): tau = |5-point difference|^2.5, w_k = d_k (1 + tau / (SI_k + eps)^2)
+template <typename T>
+inline T weno5n_side(const T* p, const T* v, const double* d) {
+  const LagrangeCoef& K = lag();
+  T SI[3], w[3];
+  const T tau = pow(n_indicators(v, SI), T(2.5));
+  for (int k = 0; k < 3; ++k) {
+    const T e = SI[k] + T(K.eps);
+    w[k] = T(d[k]) * (T(1.0) + (tau / (e * e)));
+  }
+  return normalised(p, w);
+}
+
+// teno5N (:553-594): tau = |5-point difference|^2, w_k = (1 + tau / (SI_k + eps)^2)^6, cut-off
+template <typename T>
+inline T teno5n_side(const T* p, const T* v, const double* d) {
+  const LagrangeCoef& K = lag();
+  T SI[3], w[3];
+  const T x = n_indicators(v, SI);
+  const T tau = x * x;
+  for (int k = 0; k < 3; ++k) {
+    const T e = SI[k] + T(K.eps);
+    w[k] = pow(T(1.0) + tau / (e * e), T(6));
+  }
+  return cutoff_weighted(p, w, d);
+}
+
+// teno5a (:1265-1294): tau = 1, w_k = (1 / (SI_k + epsz))^6, cut-off
+template <typename T>
+inline T teno5a_side(const T* p, const T* v, const double* d) {
+  const LagrangeCoef& K = lag();
+  T SI[3], w[3];
+  lagrange_si(v, SI);
+  for (int k = 0; k < 3; ++k) w[k] = pow(T(1.0) / (SI[k] + T(K.epsz)), T(6));
+  return cutoff_weighted(p, w, d);
+}
+
+template <typename T>
+inline T lagrange_side(int kind, const T* p, const T* v, const double* d) {
+  switch (kind) {
+    case 3: return weno5js_side(p, v, d);
+    case 4: return weno5z_side(p, v, d);
+    case 5: return weno5n_side(p, v, d);
+    case 6: return teno5n_side(p, v, d);
+    case 7: return teno5a_side(p, v, d);
+    default: return teno_side(p, v, d, kind == 1);
+  }
+}
+
+// kind: 0 teno5, 1 teno5i, 2 linear, 3 weno5JS, 4 weno5Z, 5 weno5N, 6 teno5N, 7 teno5a.
+// u[0..5] -> out[0] = u^-_{i+1/2}, out[1] = u^+_{i+1/2}
 template <typename T>
 inline void lagrange_recon(int kind, const T* u, T* out) {
   const LagrangeCoef& K = lag();
@@ -191,7 +304,7 @@ inline void lagrange_recon(int kind, const T* u, T* out) {
     T d[3] = {T(K.dkm[0]), T(K.dkm[1]), T(K.dkm[2])};
     out[0] = dot3(p, d);
   } else {
-    out[0] = teno_side(p, u + 0, K.dkm, kind == 1);
+    out[0] = lagrange_side(kind, p, u + 0, K.dkm);
   }
   p[0] = dot3c(C + 0, 4, u + 3);
   p[1] = dot3c(C + 1, 4, u + 2);
@@ -200,7 +313,7 @@ inline void lagrange_recon(int kind, const T* u, T* out) {
     T d[3] = {T(K.dkp[0]), T(K.dkp[1]), T(K.dkp[2])};
     out[1] = dot3(p, d);
   } else {
-    out[1] = teno_side(p, u + 1, K.dkp, kind == 1);
+    out[1] = lagrange_side(kind, p, u + 1, K.dkp);
   }
 }
 

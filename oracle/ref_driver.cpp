@@ -83,6 +83,20 @@ void ref_linear5(const double* u, double* out, long n) {
   Schemes::Lagrange L;
   for (long k = 0; k < n; ++k) put<2>(L.linear(vec<6>(u + 6 * k)), out + 2 * k);
 }
+// weno5JS / weno5Z / weno5N / teno5N / teno5a (Schemes_Lagrange.cpp:358-594, 1265-1294)
+void ref_lagrange_alt(int kind, const double* u, double* out, long n) {
+  Schemes::Lagrange L;
+  for (long k = 0; k < n; ++k) {
+    const auto v = vec<6>(u + 6 * k);
+    switch (kind) {
+      case 3: put<2>(L.weno5JS(v), out + 2 * k); break;
+      case 4: put<2>(L.weno5Z(v), out + 2 * k); break;
+      case 5: put<2>(L.weno5N(v), out + 2 * k); break;
+      case 6: put<2>(L.teno5N(v), out + 2 * k); break;
+      default: put<2>(L.teno5a(v), out + 2 * k); break;
+    }
+  }
+}
 void ref_gl3(const double* u, double* out, long n) {
   Schemes::Lagrange L;
   for (long k = 0; k < n; ++k) put<3>(L.weno5JS3PointsQuadrature(vec<5>(u + 5 * k)), out + 3 * k);

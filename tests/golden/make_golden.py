@@ -169,8 +169,23 @@ def solvers():
     np.savez_compressed(HERE / "solvers.npz", **g)
 
 
+def alternatives(rng):
+    """weno5JS, weno5Z, weno5N, teno5N, teno5a (Schemes_Lagrange.cpp:358-594, 1265-1294) on the
+    same kinds of stencils as the pointwise fixtures."""
+    n = 256
+    u6 = stencils(rng, n, 6)
+    g = {"alt_u": u6}
+    REF.ref_lagrange_alt.argtypes = [ctypes.c_int, _D, _D, ctypes.c_long]
+    for kind in (3, 4, 5, 6, 7):
+        out = np.empty((n, 2))
+        REF.ref_lagrange_alt(kind, p(u6), p(out), n)
+        g[f"alt_{kind}"] = out
+    np.savez_compressed(HERE / "alternatives.npz", **g)
+
+
 if __name__ == "__main__":
     pointwise(np.random.default_rng(20261203))
     solvers()
+    alternatives(np.random.default_rng(20261204))
     for f in sorted(HERE.glob("*.npz")):
         print(f.name, f.stat().st_size)

@@ -281,3 +281,23 @@ def test_fv1d_kxrcf_sensor(hteno_lib, cuda):
     want = kxrcf_ref(q, 1.0 / 400)
     assert (got != want).sum() <= 2  # threshold ties aside
     assert 3 <= got.sum() <= 80 and got[:80].sum() == 0  # flags sit at the waves only
+
+
+@pytest.mark.parametrize("recon", [3, 4, 5, 6, 7], ids=["weno5js", "weno5z", "weno5n", "teno5n", "teno5a"])
+def test_fv2d_alternative_reconstructions(hteno_lib, cuda, oracle, recon):
+    """The reference's other selectable schemes through the same solver: the plain path against
+    the oracle (bit for bit; weno5N within 1e-12, its |.|^2.5 going through the device pow), and
+    the mixed path within its bound."""
+    from hteno import ic
+
+    q = ic.four_quadrant(40, 28, 23)
+    want, t_o, n_o = oracle.fv2d_run(q, 15, flux=1, recon=recon)
+    got, t_g, n_g = gpu_run2d(hteno_lib, q, 15, flux=1, recon=recon)
+    assert n_g == n_o == 15
+    if recon == 5:
+        assert rel_linf(got, want) <= TOL
+    else:
+        assert t_g == t_o
+        np.testing.assert_array_equal(got, want)
+    mixed, _, _ = gpu_run2d(hteno_lib, q, 1000, t_final=t_o, flux=1, recon=recon, precision=1)
+    assert np.abs(mixed[0] - want[0]).mean() <= 1e-4

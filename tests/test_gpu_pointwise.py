@@ -138,3 +138,26 @@ def test_ssprk3_bitwise(hteno_lib, cuda, pw):
                                                   out.data_ptr(), q0.numel(), None) == 0
         cuda.cuda.synchronize()
         np.testing.assert_array_equal(out.cpu().numpy(), pw[f"rk_stage{st}"])
+
+
+def test_alternative_reconstructions(hteno_lib, cuda, oracle):
+    """weno5JS, weno5Z, teno5N, teno5a bit for bit against the oracle (itself pinned to the
+    reference's outputs); weno5N within 1e-14, its |.|^2.5 going through the device pow."""
+    from pathlib import Path
+
+    g = dict(np.load(Path(__file__).resolve().parent / "golden" / "alternatives.npz"))
+    rng = np.random.default_rng(8)
+    for u in (g["alt_u"], stencils(rng, 20000, 6)):
+        scale = np.abs(u).max(axis=1, keepdims=True)
+        for kind in (3, 4, 5, 6, 7):
+            got = run_lagrange(hteno_lib, cuda, kind, u)
+            want = oracle.lagrange(kind, u)
+            if kind == 5:
+                close_scaled(got, want, scale, 1e-14)
+            else:
+                np.testing.assert_array_equal(got, want)
+    for kind in (3, 4, 5, 6, 7):  # float versions: close to double on smooth data
+        x = np.arange(6)
+        u = np.ascontiguousarray(np.sin(0.2 + 0.03 * x)[None, :] * np.linspace(0.5, 2, 256)[:, None])
+        np.testing.assert_allclose(run_lagrange(hteno_lib, cuda, kind, u, prec=1), oracle.lagrange(kind, u),
+                                   rtol=5e-6, atol=5e-6)

@@ -37,6 +37,13 @@ def test_lagrange_golden(oracle, pw):
         same(oracle.lagrange(kind, pw["lag_u"]), pw[f"lag_{name}"])
 
 
+def test_alternative_reconstructions_golden(oracle):
+    """weno5JS, weno5Z, weno5N, teno5N, teno5a: the oracle reproduces the reference's outputs."""
+    g = dict(np.load(GOLD / "alternatives.npz"))
+    for kind in (3, 4, 5, 6, 7):
+        same(oracle.lagrange(kind, g["alt_u"]), g[f"alt_{kind}"])
+
+
 def test_gl3_golden(oracle, pw):
     same(oracle.gl3(pw["gl3_u"]), pw["gl3_out"])
 
