@@ -51,6 +51,7 @@ def parse():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--start-step", type=int, default=100)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
@@ -96,6 +97,7 @@ def allreduce_max(torch, world, x):
 
 def config_block(args, world):
     return {"workload": WORKLOAD, "nx": NX, "ny": NY, "recon": "teno5", "flux": "hllc",
+            "timed_from_step": max(args.warmup, args.start_step),
             "bc": "zero-gradient", "cfl": 0.4, "gamma": 1.4, "seed": SEED,
             "parallelism": f"replicas{world}" if world > 1 else "single-gpu",
             "l2": "working set ~0.45 GB per GPU > 129 MB L2 (no flush needed)"}
@@ -244,6 +246,22 @@ def batch_path(hteno, torch, stream, steps, world):
                     "as one CUDA graph; FP32 reconstruction/fluxes, FP64 state"}
 
 
+def kernel_shares(hteno, solver, steps):
+    """Per-kernel share of `steps` more steps, with CUDA events around every launch."""
+    import ctypes
+
+    lib = hteno.lib()
+    lib.hteno_enable_kernel_timing(solver.h, 1)
+    solver.step(steps)
+    kt = (hteno.KernelTime * 32)()
+    cnt = ctypes.c_int()
+    lib.hteno_kernel_timing(solver.h, kt, 32, ctypes.byref(cnt))
+    lib.hteno_enable_kernel_timing(solver.h, 0)
+    rows = [(kt[k].name.decode(), kt[k].ms) for k in range(cnt.value) if kt[k].launches]
+    tot = sum(ms for _, ms in rows) or 1.0
+    return {name: round(ms / tot, 4) for name, ms in rows}
+
+
 def hermite_path(hteno, torch, stream, steps, ref_steps, world, n=2048):
     """Hermite-WENO 2D (FVHermite::System2D) on n x n: 32 seeded Gaussian density blobs on
     rho = 1, p = 1, a Mach-2 shock entering from x = 0, moments by face differences; mixed
@@ -278,6 +296,8 @@ def hermite_path(hteno, torch, stream, steps, ref_steps, world, n=2048):
             name = "fp64" if prec == hteno.PREC_FP64 else "fp32_mixed"
             out[name] = {"value": n * n * k * world / (ms / 1e3) / 1e6, "unit": UNIT,
                          "ms_per_step": ms / k, "steps": k}
+            if prec == hteno.PREC_MIXED:  # where a mixed step spends its time (separate run)
+                out[name]["kernel_shares"] = kernel_shares(hteno, s, 2)
             if prec == hteno.PREC_FP64:
                 ref = (s.time()[0], s.get_state())
             else:
@@ -355,6 +375,7 @@ def learned_path(hteno, torch, stream, args, world, n=4096):
             s.sync()
             ms = ev0.elapsed_time(ev1)
             st = s.router_stats() if router is not None else None
+            shares = kernel_shares(hteno, s, 2)
             # accuracy: the same arm from the initial state to the FP64 arm's time
             s.set_state(q)
             s.step(1 << 20, t_ref)
@@ -365,9 +386,12 @@ def learned_path(hteno, torch, stream, args, world, n=4096):
              "ms_per_step": ms / args.c5_steps, "steps": args.c5_steps,
              "speedup_vs_fp64": (ms64 / args.c5_fp64_steps) / (ms / args.c5_steps),
              "l1_rho_vs_fp64": l1, "linf_rho_vs_fp64": linf, "shock_shift_cells": shift,
-             "t_compared": t_ref}
+             "t_compared": t_ref, "kernel_shares": shares}
         if st is not None:
+            nonflat_smooth = max(1, st["smooth"] - st["flat"])
             d["router"] = {"audited_stencils": st["seen"], "routed_fraction": st["routed"] / max(1, st["seen"]),
+                           "flat_fraction": st["flat"] / max(1, st["seen"]),
+                           "routed_of_nonflat_smooth": st["routed"] / nonflat_smooth,
                            "network_rows_last_step": st["network_rows"],
                            "misrouted_of_routed": st["misrouted"] / max(1, st["routed"]),
                            "plain_teno_smooth_fraction": st["smooth"] / max(1, st["seen"]),
@@ -426,7 +450,7 @@ def mixed_path(hteno, torch, q, stream, args, t_end, ref_state, ms_plain, world)
     with hteno.Solver(cfg) as s:
         s.set_stream(stream.cuda_stream)
         s.set_state(q)
-        s.step_async(args.warmup)
+        s.step_async(max(args.warmup, args.start_step))
         s.sync()
         ev0 = torch.cuda.Event(enable_timing=True)
         ev1 = torch.cuda.Event(enable_timing=True)
@@ -464,9 +488,12 @@ def run_gpu(args):
     solver.set_state(q)
     launches = solver.launches_per_step()
 
-    # warm-up
-    solver.step_async(args.warmup)
+    # warm-up: W steps, and on to the start step of the timed region (the middle of the
+    # configuration's 200-step run, so the timed steps see its typical wave pattern rather than
+    # the nearly uniform first steps, where constant windows shortcut the reconstruction)
+    solver.step_async(max(args.warmup, args.start_step))
     solver.sync()
+    start_state = solver.get_state()
 
     # timed region: K steps, device-resident, CUDA events on the solver's stream
     lib.hteno_enable_kernel_timing(solver.h, 1)
@@ -527,7 +554,7 @@ def run_gpu(args):
     # advances one step and reads the state back
     e2e = None
     if not args.no_e2e:
-        hq = torch.from_numpy(q).pin_memory()
+        hq = torch.from_numpy(start_state).pin_memory()
         hout = torch.empty_like(hq).pin_memory()
         e2e_steps = max(1, args.steps)
         barrier(torch, world)

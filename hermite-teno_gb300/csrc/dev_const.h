@@ -11,6 +11,9 @@ struct DevConst {
   double gp[3][3], gm[3][3];          // crjgp3L / crjgm3L
   double linwp[3], linwm[3], linw0p[3], linw0m[3], sumw0p, sumw0m;
   double gl3w[3];                     // Gauss-Legendre weights / 2 (FV_System2D.cpp:28)
+  // normalised GL3 weights when every smoothness indicator is zero (constant data): the sets
+  // linwp, linw0p, linw0m, linwm divided by (eps + 0)^2 and normalised, in that order
+  double gl3flat[4][3];
   double wtab_m[8][3], wtab_p[8][3];  // TENO5 weights per cut-off pattern (dkm / dkp)
   double dkm[3], dkp[3];
   // Schemes::Hermite (Schemes_Hermite.cpp:5-92, grid-size independent part)

@@ -66,6 +66,18 @@ void fill_dev_const(DevConst* c) {
   c->linwm[0] = (2882.0 * sq15 + 1179.0) / den;
   c->linwm[1] = (9672.0 * sq15 - 6448.0) / den;
   c->linwm[2] = (3166.0 * sq15 - 5211.0) / den;
+  {
+    // weights of weno5JS3PointsQuadrature when all three indicators vanish, with the device's
+    // operations: s = (eps + 0)^2, w_k = lw_k / s, normalised by the left-to-right sum
+    const double e = 1e-6 + 0.0, s2 = e * e;
+    const double* sets[4] = {c->linwp, c->linw0p, c->linw0m, c->linwm};
+    for (int m = 0; m < 4; ++m) {
+      double w[3];
+      for (int k = 0; k < 3; ++k) w[k] = sets[m][k] / s2;
+      const double sum = (w[0] + w[1]) + w[2];
+      for (int k = 0; k < 3; ++k) c->gl3flat[m][k] = w[k] / sum;
+    }
+  }
   c->gl3w[0] = 5.0 / 9.0 / 2.0;
   c->gl3w[1] = 8.0 / 9.0 / 2.0;
   c->gl3w[2] = 5.0 / 9.0 / 2.0;

@@ -14,14 +14,14 @@ std::mutex g_mu;
 
 #include "common_kernels.cuh"
 
-template <int TX, int TY, int NT, bool ROUTE>
+template <int TX, int TY, int NT>
 __global__ void __launch_bounds__(NT) k_fused(Geo G, int stage, fused::StageArgs a) {
   if (a.st && a.st->done) return;
   extern __shared__ __align__(16) unsigned char smem[];
   auto& S = *reinterpret_cast<fused::Smem<TX, TY>*>(smem);
   int bad = 0;
-  const double ms = fused::tile_stage<TX, TY, NT, ROUTE>(c_dev, G, blockIdx.x * TX, blockIdx.y * TY,
-                                                         stage, a, S, bad);
+  const double ms = fused::tile_stage<TX, TY, NT>(c_dev, G, blockIdx.x * TX, blockIdx.y * TY,
+                                                  stage, a, S, bad);
   if (stage == 3) {
     block_max_to(ms, &a.st->maxbits);
     if (bad) atomicOr(&a.st->status, bad);
@@ -47,31 +47,23 @@ struct Variant {
   size_t smem;
   const char* name;
   void (*launch)(cudaStream_t, const Geo&, int, const fused::StageArgs&);
-  void (*launch_routed)(cudaStream_t, const Geo&, int, const fused::StageArgs&);
   cudaError_t (*prepare)();
 };
 
-template <int TX, int TY, int NT, bool ROUTE>
+template <int TX, int TY, int NT>
 void launch_v(cudaStream_t cs, const Geo& G, int stage, const fused::StageArgs& a) {
   const dim3 grid(unsigned((G.nx + TX - 1) / TX), unsigned((G.ny + TY - 1) / TY));
-  k_fused<TX, TY, NT, ROUTE><<<grid, NT, fused::smem_bytes<TX, TY>(), cs>>>(G, stage, a);
+  k_fused<TX, TY, NT><<<grid, NT, fused::smem_bytes<TX, TY>(), cs>>>(G, stage, a);
 }
 
 template <int TX, int TY, int NT>
 cudaError_t prepare_v() {
-  cudaError_t e = cudaFuncSetAttribute(k_fused<TX, TY, NT, false>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       int(fused::smem_bytes<TX, TY>()));
-  if (e != cudaSuccess) return e;
-  return cudaFuncSetAttribute(k_fused<TX, TY, NT, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  return cudaFuncSetAttribute(k_fused<TX, TY, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                               int(fused::smem_bytes<TX, TY>()));
 }
 
-#define HTENO_VARIANT(TX, TY, NT)                                                                \
-  {                                                                                              \
-    TX, TY, NT, fused::smem_bytes<TX, TY>(), "fused_" #TX "x" #TY "_" #NT,                       \
-        launch_v<TX, TY, NT, false>, launch_v<TX, TY, NT, true>, prepare_v<TX, TY, NT>           \
-  }
+#define HTENO_VARIANT(TX, TY, NT) \
+  { TX, TY, NT, fused::smem_bytes<TX, TY>(), "fused_" #TX "x" #TY "_" #NT, launch_v<TX, TY, NT>, prepare_v<TX, TY, NT> }
 
 const Variant kVariants[] = {
     HTENO_VARIANT(32, 16, 256), HTENO_VARIANT(32, 8, 256),  HTENO_VARIANT(16, 16, 256),
@@ -99,8 +91,7 @@ void launch_stage(hteno_solver* s, const Geo& G, int stage, const fused::StageAr
   const int kind = trace_kind(s, stage == 2 || stage == 3 ? "fused_s23" : "fused_s1", bytes,
                               (kFacesFlops + fluxf) * nf + kUpdateFlops * nc);
   trace_begin(s, kind);
-  if (a.mx) V.launch_routed(s->stream, G, stage, a);
-  else V.launch(s->stream, G, stage, a);
+  V.launch(s->stream, G, stage, a);
   trace_end(s);
 }
 
@@ -164,7 +155,7 @@ void fv2d_fused_step(hteno_solver* s, const Geo& G, double* qc) {
     const int kc = trace_kind(s, "classify", 0.0, 0.0);
     trace_begin(s, kc);
     mlp_classify(s->router, G, s->q, s->route_x, s->route_y, s->router_thr, s->route_rows,
-                 s->route_info, s->audit + 4, s->route_cap, s->stream);
+                 s->route_info, s->audit + 5, s->route_cap, s->stream);
     trace_end(s);
     const bool aud = s->audit_every > 0 && s->router_steps % s->audit_every == 0;
     for (fused::StageArgs* a : {&a1, &a2, &a3}) {
@@ -212,12 +203,12 @@ int hteno_set_router(hteno_solver* s, hteno_mlp* m, float threshold, int audit_e
     s->route_cap = long(std::min<size_t>(8 * (bx + by), size_t(64) << 20));
     cudaError_t e = cudaMalloc(&s->route_x, (bx + 3) & ~size_t(3));
     if (e == cudaSuccess) e = cudaMalloc(&s->route_y, (by + 3) & ~size_t(3));
-    if (e == cudaSuccess) e = cudaMalloc(&s->audit, 5 * sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMalloc(&s->audit, 6 * sizeof(unsigned long long));
     if (e == cudaSuccess) e = cudaMalloc(&s->route_rows, size_t(s->route_cap) * sizeof(uint4));
     if (e == cudaSuccess) e = cudaMalloc(&s->route_info, size_t(s->route_cap) * sizeof(unsigned long long));
     if (e != cudaSuccess) return cuda_error(s, e, "route masks");
   }
-  cudaMemset(s->audit, 0, 5 * sizeof(unsigned long long));
+  cudaMemset(s->audit, 0, 6 * sizeof(unsigned long long));
   s->router = m;
   s->router_thr = threshold;
   s->audit_every = audit_every;
@@ -230,13 +221,13 @@ int hteno_set_router(hteno_solver* s, hteno_mlp* m, float threshold, int audit_e
 int hteno_router_stats(hteno_solver* s, long long* stats) {
   if (!s || !stats) return HTENO_ERR_INVALID_ARG;
   if (!s->router || !s->audit) return set_error(s, HTENO_ERR_UNSUPPORTED, "no router set");
-  unsigned long long h[5] = {0, 0, 0, 0, 0};
+  unsigned long long h[6] = {0, 0, 0, 0, 0, 0};
   cudaError_t e = cudaMemcpyAsync(h, s->audit, sizeof(h), cudaMemcpyDeviceToHost, s->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
   if (e != cudaSuccess) return cuda_error(s, e, "router stats");
-  for (int k = 0; k < 4; ++k) stats[k] = (long long)h[k];
-  stats[4] = s->audits;
-  stats[5] = (long long)h[4];
+  for (int k = 0; k < 5; ++k) stats[k] = (long long)h[k];
+  stats[5] = s->audits;
+  stats[6] = (long long)h[5];
   const int rc = mlp_status(s->router, s->stream);
   return rc == HTENO_OK ? HTENO_OK : set_error(s, rc, "classifier tensor-core wait timed out");
 }

@@ -119,66 +119,45 @@ __device__ __forceinline__ float weighted(float p0, float p1, float p2, const fl
   return catchnan(p0 * w[0] + p1 * w[1] + p2 * w[2]);
 }
 
-// teno5 (Schemes_Lagrange.cpp:481-511), teno5i (:1235-1263), linear (:1219-1233) or one of the
-// alternatives: u[0..5] -> (u^-_{i+1/2}, u^+_{i+1/2}).  The weight tables live in shared memory:
-// a per-thread pattern would serialise constant-memory reads.
-__device__ __forceinline__ void recon_s(const DevConst& C, int kind, const float (*tab)[8][3],
-                                        const float* u, float& outm, float& outp) {
-  float p0 = C.f_crj[0][1] * u[2] + C.f_crj[1][1] * u[3] + C.f_crj[2][1] * u[4];
-  float p1 = C.f_crj[0][2] * u[1] + C.f_crj[1][2] * u[2] + C.f_crj[2][2] * u[3];
-  float p2 = C.f_crj[0][3] * u[0] + C.f_crj[1][3] * u[1] + C.f_crj[2][3] * u[2];
-  if (kind == 2) outm = p0 * tab[0][7][0] + p1 * tab[0][7][1] + p2 * tab[0][7][2];
-  else if (kind >= 3) outm = alt_side(kind, p0, p1, p2, u, tab[0], tab[0][7]);
-  else outm = weighted(p0, p1, p2, tab[0][flat5(u) ? 7 : teno_pat_s(u, kind == 1)]);
-  p0 = C.f_crj[0][0] * u[3] + C.f_crj[1][0] * u[4] + C.f_crj[2][0] * u[5];
-  p1 = C.f_crj[0][1] * u[2] + C.f_crj[1][1] * u[3] + C.f_crj[2][1] * u[4];
-  p2 = C.f_crj[0][2] * u[1] + C.f_crj[1][2] * u[2] + C.f_crj[2][2] * u[3];
-  if (kind == 2) outp = p0 * tab[1][7][0] + p1 * tab[1][7][1] + p2 * tab[1][7][2];
-  else if (kind >= 3) outp = alt_side(kind, p0, p1, p2, u + 1, tab[1], tab[1][7]);
-  else outp = weighted(p0, p1, p2, tab[1][flat5(u + 1) ? 7 : teno_pat_s(u + 1, kind == 1)]);
-}
-
 // Audit counters of the learned router: stencils seen, routed to the linear weights, routed
-// although the plain TENO cut-off would not have kept all three candidates, all-smooth by TENO.
+// although the plain TENO cut-off would not have kept all three candidates, all-smooth by TENO,
+// flat windows.
 struct RouteCount {
-  int seen = 0, routed = 0, misrouted = 0, smooth = 0;
+  int seen = 0, routed = 0, misrouted = 0, smooth = 0, flat = 0;
 };
 
-// recon_s with routing: a side whose route bit is set takes the optimal linear weights (the TENO
-// result when all three cut-off bits are on) without evaluating the smoothness indicators; flat
-// windows take them as in recon_s; when auditing, the plain cut-off is evaluated as well and
-// compared.  TENO kinds only (0, 1).
-__device__ __forceinline__ void recon_routed(const DevConst& C, int kind, const float (*tab)[8][3],
-                                             const float* u, int route, bool audit, RouteCount& rc,
-                                             float& outm, float& outp) {
-  const bool impr = kind == 1;
-#pragma unroll
-  for (int side = 0; side < 2; ++side) {
-    const float* v = u + side;
-    float p0, p1, p2;
-    if (side == 0) {
-      p0 = C.f_crj[0][1] * u[2] + C.f_crj[1][1] * u[3] + C.f_crj[2][1] * u[4];
-      p1 = C.f_crj[0][2] * u[1] + C.f_crj[1][2] * u[2] + C.f_crj[2][2] * u[3];
-      p2 = C.f_crj[0][3] * u[0] + C.f_crj[1][3] * u[1] + C.f_crj[2][3] * u[2];
-    } else {
-      p0 = C.f_crj[0][0] * u[3] + C.f_crj[1][0] * u[4] + C.f_crj[2][0] * u[5];
-      p1 = C.f_crj[0][1] * u[2] + C.f_crj[1][1] * u[3] + C.f_crj[2][1] * u[4];
-      p2 = C.f_crj[0][2] * u[1] + C.f_crj[1][2] * u[2] + C.f_crj[2][2] * u[3];
-    }
-    const bool routed = (route >> side) & 1;
-    const bool flat = flat5(v);
-    int pat = 7;
-    if (!flat && (!routed || audit)) pat = teno_pat_s(v, impr);
-    const float o = weighted(p0, p1, p2, tab[side][(routed || flat) ? 7 : pat]);
-    if (side == 0) outm = o;
-    else outp = o;
-    if (audit) {
-      rc.seen += 1;
-      rc.smooth += pat == 7;
-      rc.routed += routed;
-      rc.misrouted += routed && pat != 7;
-    }
+// One side of teno5 (Schemes_Lagrange.cpp:481-511), teno5i (:1235-1263), linear (:1219-1233) or
+// an alternative, u[0..5] -> u^-_{i+1/2} (side 0) or u^+_{i+1/2} (side 1).  With the route bit
+// set (learned routing, TENO kinds) the side takes the linear weights without evaluating the
+// indicators; when auditing, the plain cut-off is evaluated as well and counted.  The weight
+// tables live in shared memory: a per-thread pattern would serialise constant-memory reads.
+__device__ __forceinline__ float side_value(const DevConst& C, int kind, const float (*tab)[8][3],
+                                            const float* u, int side, bool routed, bool audit,
+                                            RouteCount& rc) {
+  float p0, p1, p2;
+  if (side == 0) {
+    p0 = C.f_crj[0][1] * u[2] + C.f_crj[1][1] * u[3] + C.f_crj[2][1] * u[4];
+    p1 = C.f_crj[0][2] * u[1] + C.f_crj[1][2] * u[2] + C.f_crj[2][2] * u[3];
+    p2 = C.f_crj[0][3] * u[0] + C.f_crj[1][3] * u[1] + C.f_crj[2][3] * u[2];
+  } else {
+    p0 = C.f_crj[0][0] * u[3] + C.f_crj[1][0] * u[4] + C.f_crj[2][0] * u[5];
+    p1 = C.f_crj[0][1] * u[2] + C.f_crj[1][1] * u[3] + C.f_crj[2][1] * u[4];
+    p2 = C.f_crj[0][2] * u[1] + C.f_crj[1][2] * u[2] + C.f_crj[2][2] * u[3];
   }
+  const float* v = u + side;
+  if (kind == 2) return p0 * tab[side][7][0] + p1 * tab[side][7][1] + p2 * tab[side][7][2];
+  if (kind >= 3) return alt_side(kind, p0, p1, p2, v, tab[side], tab[side][7]);
+  const bool flat = flat5(v);
+  int pat = 7;
+  if (!flat && (!routed || audit)) pat = teno_pat_s(v, kind == 1);
+  if (audit) {
+    rc.seen += 1;
+    rc.smooth += pat == 7;
+    rc.flat += flat;
+    rc.routed += routed;
+    rc.misrouted += routed && pat != 7;
+  }
+  return weighted(p0, p1, p2, tab[side][(routed || flat) ? 7 : pat]);
 }
 
 // Pointers of one stage of one grid.
@@ -187,23 +166,26 @@ struct StageArgs {
   const double* qbase;  // step-start state (stages 2, 3), read pointwise
   double* qout;         // output state (stages 1-3) or residual (stage 0)
   StepState* st;        // dt, health flags, max wave speed; null for stage 0
-  // learned routing (ROUTE kernels): per x face [ny][nx+1] and y face [ny+1][nx] one byte, bit
+  // learned routing (when mx is set): per x face [ny][nx+1] and y face [ny+1][nx] one byte, bit
   // 2r (2r+1) = left (right) side of characteristic field r takes the linear weights
   const uint8_t* mx = nullptr;
   const uint8_t* my = nullptr;
-  unsigned long long* audit = nullptr;  // [4] RouteCount sums when auditing this stage
+  unsigned long long* audit = nullptr;  // [5] RouteCount sums when auditing this stage
 };
 
 // The tile at (i0, j0) of grid G.  Every thread of the block must call it (barriers inside).
 // Returns this thread's max wave speed over the cells it updated (stage 3) and ORs health flags
 // into *bad.
-template <int TX, int TY, int NT, bool ROUTE = false>
+template <int TX, int TY, int NT>
 __device__ __forceinline__ double tile_stage(const DevConst& C, const Geo& G, int i0, int j0,
                                              int stage, const StageArgs& a, Smem<TX, TY>& S,
                                              int& bad) {
   typedef Shape<TX, TY> Sh;
   RouteCount rc;
-  const bool audit = ROUTE && a.audit != nullptr;
+  // routing is a run-time switch (uniform per launch): the same machine code serves the plain and
+  // the routed runs, so a router that routes nothing reproduces the plain run bit for bit
+  const bool route_on = a.mx != nullptr;
+  const bool audit = route_on && a.audit != nullptr;
   const size_t nc = size_t(G.nx) * G.ny;
   const float g1 = float(G.g1);
   const int tid = threadIdx.x;
@@ -250,26 +232,18 @@ __device__ __forceinline__ double tile_stage(const DevConst& C, const Geo& G, in
 #pragma unroll
       for (int r = 0; r < 4; ++r) ch[r][m] = cc[r];
     }
-    if constexpr (ROUTE) {
+    int route = 0;
+    bool own = false;
+    if (route_on) {
       const int gface = min(i0 + f, G.nx);
-      const int route = a.mx[size_t(cmap(j0 - 2 + rr, G.ny, G.bc)) * (G.nx + 1) + gface];
-      const bool own = audit && rr >= 2 && rr < TY + 2 && j0 + rr - 2 < G.ny && i0 + f <= G.nx &&
-                       (f < TX || i0 + f == G.nx);
+      route = a.mx[size_t(cmap(j0 - 2 + rr, G.ny, G.bc)) * (G.nx + 1) + gface];
+      own = audit && rr >= 2 && rr < TY + 2 && j0 + rr - 2 < G.ny && i0 + f <= G.nx &&
+            (f < TX || i0 + f == G.nx);
+    }
 #pragma unroll
-      for (int r = 0; r < 4; ++r) {
-        float lo, hi;
-        recon_routed(C, G.recon, S.wtab, ch[r], (route >> (2 * r)) & 3, own, rc, lo, hi);
-        S.c[r][it] = lo;
-        S.c[4 + r][it] = hi;
-      }
-    } else {
-#pragma unroll
-      for (int r = 0; r < 4; ++r) {
-        float lo, hi;
-        recon_s(C, G.recon, S.wtab, ch[r], lo, hi);
-        S.c[r][it] = lo;
-        S.c[4 + r][it] = hi;
-      }
+    for (int r = 0; r < 4; ++r) {
+      S.c[r][it] = side_value(C, G.recon, S.wtab, ch[r], 0, (route >> (2 * r)) & 1, own, rc);
+      S.c[4 + r][it] = side_value(C, G.recon, S.wtab, ch[r], 1, (route >> (2 * r + 1)) & 1, own, rc);
     }
   }
   __syncthreads();
@@ -326,26 +300,18 @@ __device__ __forceinline__ double tile_stage(const DevConst& C, const Geo& G, in
 #pragma unroll
       for (int r = 0; r < 4; ++r) ch[r][m] = cv[r];
     }
-    if constexpr (ROUTE) {
+    int route = 0;
+    bool own = false;
+    if (route_on) {
       const int gface = min(j0 + gg, G.ny);
-      const int route = a.my[size_t(gface) * G.nx + cmap(i0 - 2 + cc, G.nx, G.bc)];
-      const bool own = audit && cc >= 2 && cc < TX + 2 && i0 + cc - 2 < G.nx && j0 + gg <= G.ny &&
-                       (gg < TY || j0 + gg == G.ny);
+      route = a.my[size_t(gface) * G.nx + cmap(i0 - 2 + cc, G.nx, G.bc)];
+      own = audit && cc >= 2 && cc < TX + 2 && i0 + cc - 2 < G.nx && j0 + gg <= G.ny &&
+            (gg < TY || j0 + gg == G.ny);
+    }
 #pragma unroll
-      for (int r = 0; r < 4; ++r) {
-        float lo, hi;
-        recon_routed(C, G.recon, S.wtab, ch[r], (route >> (2 * r)) & 3, own, rc, lo, hi);
-        S.c[r][it] = lo;
-        S.c[4 + r][it] = hi;
-      }
-    } else {
-#pragma unroll
-      for (int r = 0; r < 4; ++r) {
-        float lo, hi;
-        recon_s(C, G.recon, S.wtab, ch[r], lo, hi);
-        S.c[r][it] = lo;
-        S.c[4 + r][it] = hi;
-      }
+    for (int r = 0; r < 4; ++r) {
+      S.c[r][it] = side_value(C, G.recon, S.wtab, ch[r], 0, (route >> (2 * r)) & 1, own, rc);
+      S.c[4 + r][it] = side_value(C, G.recon, S.wtab, ch[r], 1, (route >> (2 * r + 1)) & 1, own, rc);
     }
   }
   __syncthreads();
@@ -422,15 +388,13 @@ __device__ __forceinline__ double tile_stage(const DevConst& C, const Geo& G, in
       msf = fmaxf(msf, m);
     }
   }
-  if constexpr (ROUTE) {
-    if (audit) {
-      int v[4] = {rc.seen, rc.routed, rc.misrouted, rc.smooth};
+  if (audit) {
+    int v[5] = {rc.seen, rc.routed, rc.misrouted, rc.smooth, rc.flat};
 #pragma unroll
-      for (int k = 0; k < 4; ++k) {
+    for (int k = 0; k < 5; ++k) {
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
-        if ((threadIdx.x & 31) == 0 && v[k]) atomicAdd(a.audit + k, (unsigned long long)v[k]);
-      }
+      for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
+      if ((threadIdx.x & 31) == 0 && v[k]) atomicAdd(a.audit + k, (unsigned long long)v[k]);
     }
   }
   return f2d(msf);

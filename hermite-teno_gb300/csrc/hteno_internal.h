@@ -76,7 +76,7 @@ struct hteno_solver {
   long router_steps = 0;
   uint8_t* route_x = nullptr;
   uint8_t* route_y = nullptr;
-  unsigned long long* audit = nullptr;  // [4]: seen, routed, misrouted, smooth; [4]: rows asked
+  unsigned long long* audit = nullptr;  // [6]: seen, routed, misrouted, smooth, flat; rows asked
   long audits = 0;
   uint4* route_rows = nullptr;             // non-flat stencils handed to the network
   unsigned long long* route_info = nullptr;

@@ -102,6 +102,10 @@ __device__ __forceinline__ int cutoff_pattern(const double* SI, double tau, doub
 // One side of teno5 (:481-511) / teno5i (:1235-1263) given the candidates p and stencil v.
 __device__ __forceinline__ double teno_side(const DevConst& C, const double* p, const double* v,
                                             int side, bool improved) {
+  // A constant window: every indicator is exactly zero, the three ratios are equal and the
+  // cut-off keeps all candidates (pattern 7) -- decided without evaluating them, same bits.
+  if (v[1] == v[0] && v[2] == v[0] && v[3] == v[0] && v[4] == v[0])
+    return catchnan(dot3v(p, side ? C.wtab_p[7] : C.wtab_m[7]));
   double SI[3];
   lagrange_si(v, SI);
   double tau;
@@ -240,6 +244,28 @@ __device__ __forceinline__ void gl3(const DevConst& C, const double* u, double* 
   cg[1] = u[1] - 2.0 * u[2] + u[3];
   bg[2] = 3.0 * u[2] - 4.0 * u[3] + u[4];
   cg[2] = u[2] - 2.0 * u[3] + u[4];
+  if (bg[0] == 0.0 && bg[1] == 0.0 && bg[2] == 0.0 && cg[0] == 0.0 && cg[1] == 0.0 && cg[2] == 0.0) {
+    // every indicator is zero: the normalised weights are the constants gl3flat, which the host
+    // computed with these same operations -- the same bits without the 24 divisions
+    double p[3];
+    p[0] = dot3(C.gp[0][0], C.gp[1][0], C.gp[2][0], u + 0);
+    p[1] = dot3(C.gp[0][1], C.gp[1][1], C.gp[2][1], u + 1);
+    p[2] = dot3(C.gp[0][2], C.gp[1][2], C.gp[2][2], u + 2);
+    out[0] = dot3v(p, C.gl3flat[0]);
+    p[0] = (-u[0] + 2.0 * u[1] + 23.0 * u[2]) / 24.0;
+    p[1] = (-u[1] + 26.0 * u[2] - u[3]) / 24.0;
+    p[2] = (23.0 * u[2] + 2.0 * u[3] - u[4]) / 24.0;
+    double c = C.sumw0p * dot3v(p, C.gl3flat[1]);
+    c = c - C.sumw0m * dot3v(p, C.gl3flat[2]);
+    out[1] = c;
+    p[0] = dot3(C.gm[0][0], C.gm[1][0], C.gm[2][0], u + 0);
+    p[1] = dot3(C.gm[0][1], C.gm[1][1], C.gm[2][1], u + 1);
+    p[2] = dot3(C.gm[0][2], C.gm[1][2], C.gm[2][2], u + 2);
+    out[2] = dot3v(p, C.gl3flat[3]);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) out[k] = catchnan(out[k]);
+    return;
+  }
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
     const double si = 0.25 * (bg[k] * bg[k]) + (13.0 / 12.0) * (cg[k] * cg[k]);

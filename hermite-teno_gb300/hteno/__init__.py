@@ -254,10 +254,10 @@ class Solver:
                                       int(audit_every)), self.h)
 
     def router_stats(self) -> dict:
-        a = (ctypes.c_longlong * 6)()
+        a = (ctypes.c_longlong * 7)()
         _check(lib().hteno_router_stats(self.h, a), self.h)
-        return {"seen": a[0], "routed": a[1], "misrouted": a[2], "smooth": a[3], "audits": a[4],
-                "network_rows": a[5]}
+        return {"seen": a[0], "routed": a[1], "misrouted": a[2], "smooth": a[3], "flat": a[4],
+                "audits": a[5], "network_rows": a[6]}
 
     def residual(self, q_dev, rhs_dev) -> None:
         _check(lib().hteno_residual(self.h, _ptr(q_dev)[0], _ptr(rhs_dev)[0]), self.h)

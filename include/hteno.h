@@ -249,11 +249,11 @@ const char* hteno_mlp_last_error(hteno_mlp* m);
  * cut-off of every stencil and count the routing errors.  m = NULL switches routing off; the
  * classifier must outlive its use by the solver. */
 int hteno_set_router(hteno_solver* s, hteno_mlp* m, float threshold, int audit_every);
-/* stats[6]: audited stencils, routed, misrouted (routed though plain TENO cut a candidate; flat
- * stencils excepted), all-smooth by plain TENO, number of audited steps, and the number of
- * stencils the last classification handed to the network (the others were flat: six equal float
- * values, for which plain TENO keeps all three candidates, routed without the network).  Also
- * reports a classifier timeout. */
+/* stats[7]: audited stencils, routed, misrouted (routed though plain TENO cut a candidate),
+ * all-smooth by plain TENO, flat (a window of equal float values: the stage kernel takes the
+ * linear weights for it without the network or the indicators -- plain TENO keeps all three
+ * candidates there), number of audited steps, and the number of stencils the last
+ * classification handed to the network.  Also reports a classifier timeout. */
 int hteno_router_stats(hteno_solver* s, long long* stats);
 
 /* ---- Tracing: per-kernel CUDA-event timing of hteno_step ---------------------------------- */
