@@ -94,10 +94,12 @@ constexpr size_t smem_bytes() {
   return sizeof(Smem<TX, TY>);
 }
 
-// Cut-off pattern of one side of teno5 / teno5i (float).
+// Cut-off pattern of one side of teno5 / teno5i (float).  With all three indicators exactly zero
+// (constant data) the three ratios are equal and the pattern is 7 whatever tau is.
 __device__ __forceinline__ int teno_pat_s(const float* v, bool improved) {
   float SI0, SI1, SI2;
   lagrange_si(v, SI0, SI1, SI2);
+  if (SI0 == 0.f && SI1 == 0.f && SI2 == 0.f) return 7;
   float tau;
   if (!improved) tau = fabsf(lagrange_b35(v) - (SI0 + SI2 + 4.0f * SI1) * (1.0f / 6.0f));
   else tau = fmaxf(fmaxf(SI0, SI1), SI2);
@@ -108,9 +110,8 @@ __device__ __forceinline__ int teno_pat_s(const float* v, bool improved) {
   return teno_pattern(r0, r1, r2, float(HTENO_LAG_CT));
 }
 
-// A side's 5-cell window of equal float values: the smoothness indicators vanish, all three
-// TENO ratios are equal, and the cut-off keeps every candidate (pattern 7) -- the linear weights,
-// which are therefore taken without evaluating the indicators (the same result, bit for bit).
+// A side's 5-cell window of equal float values, counted by the audit (the classifier hands such
+// stencils to nobody).
 __device__ __forceinline__ bool flat5(const float* v) {
   return v[1] == v[0] && v[2] == v[0] && v[3] == v[0] && v[4] == v[0];
 }
@@ -147,17 +148,16 @@ __device__ __forceinline__ float side_value(const DevConst& C, int kind, const f
   const float* v = u + side;
   if (kind == 2) return p0 * tab[side][7][0] + p1 * tab[side][7][1] + p2 * tab[side][7][2];
   if (kind >= 3) return alt_side(kind, p0, p1, p2, v, tab[side], tab[side][7]);
-  const bool flat = flat5(v);
   int pat = 7;
-  if (!flat && (!routed || audit)) pat = teno_pat_s(v, kind == 1);
+  if (!routed || audit) pat = teno_pat_s(v, kind == 1);
   if (audit) {
     rc.seen += 1;
     rc.smooth += pat == 7;
-    rc.flat += flat;
+    rc.flat += flat5(v);
     rc.routed += routed;
     rc.misrouted += routed && pat != 7;
   }
-  return weighted(p0, p1, p2, tab[side][(routed || flat) ? 7 : pat]);
+  return weighted(p0, p1, p2, tab[side][routed ? 7 : pat]);
 }
 
 // Pointers of one stage of one grid.

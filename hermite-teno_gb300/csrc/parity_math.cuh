@@ -102,12 +102,14 @@ __device__ __forceinline__ int cutoff_pattern(const double* SI, double tau, doub
 // One side of teno5 (:481-511) / teno5i (:1235-1263) given the candidates p and stencil v.
 __device__ __forceinline__ double teno_side(const DevConst& C, const double* p, const double* v,
                                             int side, bool improved) {
-  // A constant window: every indicator is exactly zero, the three ratios are equal and the
-  // cut-off keeps all candidates (pattern 7) -- decided without evaluating them, same bits.
-  if (v[1] == v[0] && v[2] == v[0] && v[3] == v[0] && v[4] == v[0])
-    return catchnan(dot3v(p, side ? C.wtab_p[7] : C.wtab_m[7]));
   double SI[3];
   lagrange_si(v, SI);
+  // All three indicators exactly zero (constant data): the three ratios 1 + tau/(0 + epsz) are
+  // equal whatever tau is, and the cut-off keeps all candidates (pattern 7) -- decided without
+  // tau, same bits.  (Equal values alone do not suffice: 3u - 4u + u can leave a rounding
+  // residue in one indicator.)
+  if (SI[0] == 0.0 && SI[1] == 0.0 && SI[2] == 0.0)
+    return catchnan(dot3v(p, side ? C.wtab_p[7] : C.wtab_m[7]));
   double tau;
   if (!improved) {
     const double b35 = lagrange_b35(v);
