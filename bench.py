@@ -64,6 +64,7 @@ def parse():
     ap.add_argument("--c5-steps", type=int, default=20)
     ap.add_argument("--c5-fp64-steps", type=int, default=3)
     ap.add_argument("--c5-epochs", type=int, default=10)
+    ap.add_argument("--c5-audit-every", type=int, default=10)
     ap.add_argument("--batch-steps", type=int, default=100)
     return ap.parse_args()
 
@@ -361,7 +362,7 @@ def learned_path(hteno, torch, stream, args, world, n=4096):
         with hteno.Solver(cfg32) as s:
             s.set_stream(stream.cuda_stream)
             if router is not None:
-                s.set_router(router, 0.9, 50)
+                s.set_router(router, 0.9, args.c5_audit_every)
             s.set_state(q)
             s.step_async(2)  # warm-up
             s.sync()
@@ -395,7 +396,8 @@ def learned_path(hteno, torch, stream, args, world, n=4096):
                            "network_rows_last_step": st["network_rows"],
                            "misrouted_of_routed": st["misrouted"] / max(1, st["routed"]),
                            "plain_teno_smooth_fraction": st["smooth"] / max(1, st["seen"]),
-                           "audited_steps": st["audits"], "threshold": 0.9, "audit_every": 50}
+                           "audited_steps": st["audits"], "threshold": 0.9,
+                           "audit_every": args.c5_audit_every}
         out[name] = d
     m.close()
     out["learned_vs_fp32_plain"] = out["fp32_plain"]["ms_per_step"] / out["fp32_learned"]["ms_per_step"]
