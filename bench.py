@@ -316,7 +316,8 @@ def learned_path(hteno, torch, stream, args, world, n=4096):
     """The learned-routing workload: 4096 x 4096 seeded four-quadrant data, TENO5 + HLLC.
     The classifier trains on rows the plain FP64 solver records from runs with fresh seeds of the
     1024^2 four-quadrant problem and the 400-cell Sod tube.  Three arms run from the same
-    state: plain FP64, FP32 (mixed) and FP32 + learned routing with an audit every 50 steps.
+    state: plain FP64, FP32 (mixed) and FP32 + learned routing with a plain-TENO audit every
+    `c5_audit_every` steps (50 in the configuration's 500-step run, 10 for the short default).
     The mixed arms are timed over `c5_steps`; the FP64 arm over `c5_fp64_steps`.  Densities are
     compared at the FP64 arm's final time."""
     from hteno import ic, learned
