@@ -44,12 +44,69 @@ __global__ void kp_prim(Geo G, const double* __restrict__ q, double* __restrict_
   if (do_max) block_max_to(ms, &st->maxbits);
 }
 
+// ---- uniform regions ---------------------------------------------------------------------------
+// deep[k] = 1 when the 7 x 7 block of cells centred on cell k (boundary-mapped as every stencil
+// maps it) holds one state, bit for bit, and that state is tame: density and pressure positive
+// and within [2^-64, 2^64], Mach number at most 8.  Every input of the two x fluxes and of the two
+// y fluxes of cell k then comes from identical cells, so each pair is computed from identical
+// data, and the pair's difference -- the cell's residual -- is exactly +0 as long as the flux is
+// finite.  The bounds make it so: reconstructing identical values through the characteristic
+// basis (condition ~ Mach^2) returns the state to a relative 2^-40, positive, and no product of
+// the face or flux arithmetic leaves the double range.  The stage skips the faces only such cells
+// use and gives such cells a zero residual: the results are the same bits as the full stage.
+__device__ __forceinline__ int cmap_any(int i, int n, int bc) {  // any offset (tiles past the edge)
+  if (bc == HTENO_BC_PERIODIC) {
+    i %= n;
+    return i < 0 ? i + n : i;
+  }
+  return min(max(i, 0), n - 1);
+}
+
+__global__ void __launch_bounds__(256) kp_deep(Geo G, const double* __restrict__ q,
+                                               uint8_t* __restrict__ deep, const StepState* st) {
+  if (st && st->done) return;
+  constexpr int TX = 32, TY = 8, W = TX + 6, H = TY + 6;
+  __shared__ unsigned long long key[4][H][W];
+  const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY;
+  const size_t nc = size_t(G.nx) * G.ny;
+  for (int it = threadIdx.x; it < W * H; it += blockDim.x) {
+    const int y = it / W, x = it - y * W;
+    const size_t k = size_t(cmap_any(j0 - 3 + y, G.ny, G.bc)) * G.nx + cmap_any(i0 - 3 + x, G.nx, G.bc);
+#pragma unroll
+    for (int v = 0; v < 4; ++v)
+      key[v][y][x] = static_cast<unsigned long long>(__double_as_longlong(q[v * nc + k]));
+  }
+  __syncthreads();
+  const int tx = threadIdx.x % TX, ty = threadIdx.x / TX;
+  const int gi = i0 + tx, gj = j0 + ty;
+  if (gi >= G.nx || gj >= G.ny) return;
+  const unsigned long long c0 = key[0][ty + 3][tx + 3], c1 = key[1][ty + 3][tx + 3];
+  const unsigned long long c2 = key[2][ty + 3][tx + 3], c3 = key[3][ty + 3][tx + 3];
+  const double qc[4] = {__longlong_as_double(static_cast<long long>(c0)),
+                        __longlong_as_double(static_cast<long long>(c1)),
+                        __longlong_as_double(static_cast<long long>(c2)),
+                        __longlong_as_double(static_cast<long long>(c3))};
+  double w[4];
+  par::primitive(G.g1, qc, w);
+  constexpr double lo = 0x1p-64, hi = 0x1p64;
+  bool u = w[0] >= lo && w[0] <= hi && w[3] >= lo && w[3] <= hi &&
+           w[1] * w[1] + w[2] * w[2] <= 64.0 * (G.gamma * w[3] / w[0]);
+#pragma unroll
+  for (int dy = 0; dy < 7; ++dy)
+#pragma unroll
+    for (int dx = 0; dx < 7; ++dx)
+      u &= key[0][ty + dy][tx + dx] == c0 && key[1][ty + dy][tx + dx] == c1 &&
+           key[2][ty + dy][tx + dx] == c2 && key[3][ty + dy][tx + dx] == c3;
+  deep[size_t(gj) * G.nx + gi] = u ? 1 : 0;
+}
+
 template <int DIR>
 __global__ void __launch_bounds__(kFaceThreads) kp_faces(Geo G, const double* __restrict__ q,
                                                          const double* __restrict__ prim,
                                                          double* __restrict__ fc,
                                                          double* __restrict__ froe,
-                                                         const StepState* st) {
+                                                         const StepState* st,
+                                                         const uint8_t* __restrict__ deep = nullptr) {
   if (st && st->done) return;
   const int nf = DIR == 1 ? G.nx + 1 : G.ny + 1;
   const int nt = DIR == 1 ? G.ny : G.nx;
@@ -64,6 +121,20 @@ __global__ void __launch_bounds__(kFaceThreads) kp_faces(Geo G, const double* __
     const int m = bmap(s, ns, G.bc);
     return DIR == 1 ? size_t(t) * G.nx + m : size_t(m) * G.nx + t;
   };
+  if (deep) {
+    // no flux face computed this stage reads this face: those are the faces (f, t + m), |m| <= 2,
+    // whose two cells are not both deep
+    const int a = bmap(f - 1, ns, G.bc), b = bmap(f, ns, G.bc);
+    bool skip = true;
+#pragma unroll
+    for (int m = -2; m <= 2; ++m) {
+      const int tt = bmap(t + m, nt, G.bc);
+      const size_t ka = DIR == 1 ? size_t(tt) * G.nx + a : size_t(a) * G.nx + tt;
+      const size_t kb = DIR == 1 ? size_t(tt) * G.nx + b : size_t(b) * G.nx + tt;
+      skip = skip && deep[ka] && deep[kb];
+    }
+    if (skip) return;
+  }
   const size_t ca = cell(f - 1), cb = cell(f);
   const par::Eig E = par::eig(G.g1, DIR, prim[3 * nc + ca], prim[ca], prim[nc + ca],
                               prim[2 * nc + ca], prim[3 * nc + cb], prim[cb], prim[nc + cb],
@@ -139,7 +210,8 @@ template <int DIR>
 __global__ void __launch_bounds__(kFaceThreads) kp_flux(Geo G, const double* __restrict__ fc,
                                                         const double* __restrict__ froe,
                                                         double* __restrict__ F,
-                                                        const StepState* st) {
+                                                        const StepState* st,
+                                                        const uint8_t* __restrict__ deep = nullptr) {
   if (st && st->done) return;
   const int nf = DIR == 1 ? G.nx + 1 : G.ny + 1;
   const int nt = DIR == 1 ? G.ny : G.nx;
@@ -148,6 +220,13 @@ __global__ void __launch_bounds__(kFaceThreads) kp_flux(Geo G, const double* __r
   int f, t;
   if (DIR == 1) { f = int(idx % nf); t = int(idx / nf); }
   else { t = int(idx % nt); f = int(idx / nt); }
+  if (deep) {  // both cells deep: neither reads this flux
+    const int ns = DIR == 1 ? G.nx : G.ny;
+    const int a = bmap(f - 1, ns, G.bc), b = bmap(f, ns, G.bc);
+    const size_t ka = DIR == 1 ? size_t(t) * G.nx + a : size_t(a) * G.nx + t;
+    const size_t kb = DIR == 1 ? size_t(t) * G.nx + b : size_t(b) * G.nx + t;
+    if (deep[ka] && deep[kb]) return;
+  }
   const size_t nface = size_t(nf) * nt;
   size_t nb[5];
 #pragma unroll
@@ -199,7 +278,8 @@ __global__ void __launch_bounds__(kFaceThreads) kp_flux(Geo G, const double* __r
 __global__ void kp_update(Geo G, int stage, const double* __restrict__ fx,
                           const double* __restrict__ fy, double* __restrict__ q,
                           double* __restrict__ q0, double* __restrict__ prim,
-                          double* __restrict__ out, StepState* st) {
+                          double* __restrict__ out, StepState* st,
+                          const uint8_t* __restrict__ deep = nullptr) {
   if (st && st->done) return;
   const size_t nc = size_t(G.nx) * G.ny;
   const size_t k = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
@@ -209,11 +289,13 @@ __global__ void kp_update(Geo G, int stage, const double* __restrict__ fx,
     const int i = int(k % G.nx), j = int(k / G.nx);
     const size_t nxf = size_t(G.nx + 1) * G.ny, nyf = size_t(G.ny + 1) * G.nx;
     const size_t ox = size_t(j) * (G.nx + 1) + i, oy = size_t(j) * G.nx + i;
-    double rhs[4];
+    double rhs[4] = {0.0, 0.0, 0.0, 0.0};  // a deep cell's flux pairs are equal: residual +0
+    if (!(deep && deep[k])) {
 #pragma unroll
-    for (int v = 0; v < 4; ++v)
-      rhs[v] = ((fx[v * nxf + ox] - fx[v * nxf + ox + 1]) * G.dy +
-                (fy[v * nyf + oy] - fy[v * nyf + oy + G.nx]) * G.dx) / G.area + 0.0;
+      for (int v = 0; v < 4; ++v)
+        rhs[v] = ((fx[v * nxf + ox] - fx[v * nxf + ox + 1]) * G.dy +
+                  (fy[v * nyf + oy] - fy[v * nyf + oy + G.nx]) * G.dx) / G.area + 0.0;
+    }
     if (stage == 0) {
 #pragma unroll
       for (int v = 0; v < 4; ++v) out[v * nc + k] = rhs[v];
@@ -253,6 +335,10 @@ __global__ void kp_update(Geo G, int stage, const double* __restrict__ fx,
 int fv2d_fp64_setup(hteno_solver* s) {
   if (upload_const(c_dev, &g_mask, &g_mu) != cudaSuccess)
     return set_error(s, HTENO_ERR_CUDA, "constant upload failed");
+  if (s->cfg.precision == HTENO_PREC_FP64 && !s->deep) {
+    const cudaError_t e = cudaMalloc(&s->deep, size_t(s->cfg.nx) * s->cfg.ny);
+    if (e != cudaSuccess) return cuda_error(s, e, "uniform-region flags");
+  }
   return HTENO_OK;
 }
 
@@ -275,26 +361,34 @@ void fv2d_fp64_stage(hteno_solver* s, const Geo& G, const Work<double>& W, int s
   const int kx = trace_kind(s, "flux_x", double(nxf) * 19 * 8, fluxf * nxf);
   const int ky = trace_kind(s, "flux_y", double(nyf) * 19 * 8, fluxf * nyf);
   const int ku = trace_kind(s, "update", ncd * 128 + double(nxf + nyf) * 4 * 8, kUpdateFlops * ncd);
+  // uniform regions (stepping only): the faces only deep cells use are skipped
+  const uint8_t* deep = stage > 0 ? s->deep : nullptr;
+  if (deep) {
+    const int ku0 = trace_kind(s, "uniform", ncd * 32, 0.0);
+    trace_begin(s, ku0);
+    kp_deep<<<dim3(unsigned((nx + 31) / 32), unsigned((ny + 7) / 8)), 256, 0, cs>>>(G, q, s->deep, st);
+    trace_end(s);
+  }
   trace_begin(s, kf_x);
   kp_faces<1><<<unsigned((nxf + kFaceThreads - 1) / kFaceThreads), kFaceThreads, 0, cs>>>(
-      G, q, W.prim, W.xc, W.xroe, st);
+      G, q, W.prim, W.xc, W.xroe, st, deep);
   trace_end(s);
   trace_begin(s, kf_y);
   kp_faces<2><<<unsigned((nyf + kFaceThreads - 1) / kFaceThreads), kFaceThreads, 0, cs>>>(
-      G, q, W.prim, W.yc, W.yroe, st);
+      G, q, W.prim, W.yc, W.yroe, st, deep);
   trace_end(s);
   trace_begin(s, kx);
   kp_flux<1><<<unsigned((nxf + kFaceThreads - 1) / kFaceThreads), kFaceThreads, 0, cs>>>(
-      G, W.xc, W.xroe, W.fx, st);
+      G, W.xc, W.xroe, W.fx, st, deep);
   trace_end(s);
   trace_begin(s, ky);
   kp_flux<2><<<unsigned((nyf + kFaceThreads - 1) / kFaceThreads), kFaceThreads, 0, cs>>>(
-      G, W.yc, W.yroe, W.fy, st);
+      G, W.yc, W.yroe, W.fy, st, deep);
   trace_end(s);
   const size_t nc = size_t(nx) * ny;
   trace_begin(s, ku);
   kp_update<<<unsigned((nc + 255) / 256), 256, 0, cs>>>(G, stage, W.fx, W.fy, s->q, s->q0,
-                                                       W.prim, out, st);
+                                                       W.prim, out, st, deep);
   trace_end(s);
 }
 

@@ -105,6 +105,7 @@ void release(hteno_solver* s) {
   cudaFree(s->route_y);
   cudaFree(s->audit);
   cudaFree(s->route_rows);
+  cudaFree(s->deep);
   cudaFree(s->route_info);
   cudaFree(s->q);
   cudaFree(s->q0);

@@ -128,6 +128,41 @@ def test_fv2d_edge_sizes_and_time_clipping(hteno_lib, cuda, oracle):
             np.testing.assert_array_equal(got, want)
 
 
+def blob_field(nx, ny, scale=1.0, mach=0.3, p_bg=1.0):
+    """A dense, high-pressure disc in a uniform stream: most cells sit in bitwise-uniform 7 x 7
+    blocks, which the plain path gives a zero residual without computing their faces."""
+    from hteno import ic
+
+    x = (np.arange(nx) + 0.5) / nx
+    y = (np.arange(ny) + 0.5) / ny
+    X, Y = np.meshgrid(x, y)
+    disc = (X - 0.45) ** 2 + (Y - 0.5) ** 2 < 0.12 ** 2
+    u = mach * np.sqrt(1.4) + 0 * X
+    return np.ascontiguousarray(ic.conservative2(scale * (1.0 + disc), u, -0.2 * u, scale * (p_bg + 2.0 * disc)))
+
+
+UNIFORM_CASES = {
+    "stream": dict(q=lambda: blob_field(96, 72), flux=1, bc=0),
+    "stream-rusanov-periodic": dict(q=lambda: blob_field(96, 72), flux=0, bc=1),
+    "tiny-density": dict(q=lambda: blob_field(96, 72, scale=1e-22), flux=1, bc=0),  # below 2^-64
+    "hypersonic": dict(q=lambda: blob_field(96, 72, mach=12.0), flux=1, bc=0),  # Mach above 8
+    "negative-pressure": dict(q=lambda: blob_field(48, 40, p_bg=-1.0), flux=1, bc=0, steps=2),
+}
+
+
+@pytest.mark.parametrize("case", list(UNIFORM_CASES))
+def test_fv2d_uniform_regions_exact(hteno_lib, cuda, oracle, case):
+    """The plain path skips the faces that only cells of bitwise-uniform, tame 7 x 7 blocks use;
+    the result is the full computation's bits, whether or not a case qualifies (states outside
+    the tame bounds, and nonphysical ones whose fluxes are NaN, take the full path)."""
+    c = dict(UNIFORM_CASES[case])
+    q, steps = c.pop("q")(), c.pop("steps", 30)
+    want, t_o, n_o = oracle.fv2d_run(q, steps, **c)
+    got, t_g, n_g = gpu_run2d(hteno_lib, q, steps, **c)
+    assert n_g == n_o and (t_g == t_o or (np.isnan(t_g) and np.isnan(t_o)))
+    np.testing.assert_array_equal(got, want)
+
+
 def test_fv2d_constant_state_is_steady(hteno_lib, cuda):
     q = np.ascontiguousarray(np.broadcast_to(np.array([1.3, 0.2, -0.4, 2.7])[:, None, None], (4, 16, 20)).copy())
     got, _, _ = gpu_run2d(hteno_lib, q, 5, flux=1)
