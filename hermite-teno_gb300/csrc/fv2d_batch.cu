@@ -47,6 +47,7 @@ __global__ void __launch_bounds__(NT) k_batch_stage(const BInst* __restrict__ in
     else if (stage == 1) a = fused::StageArgs{I.q, nullptr, I.q1, I.st};
     else if (stage == 2) a = fused::StageArgs{I.q1, I.q, I.q2, I.st};
     else a = fused::StageArgs{I.q2, I.q, I.q, I.st};
+    a.skip_uniform = stage != 0;  // stage 0 only times tile shapes: the full work
     int bad = 0;
     const double ms = fused::tile_stage<TX, TY, NT>(c_dev, I.G, job.y, job.z, stage, a, S, bad);
     if (stage == 3) {

@@ -362,7 +362,7 @@ void fv2d_fp64_stage(hteno_solver* s, const Geo& G, const Work<double>& W, int s
   const int ky = trace_kind(s, "flux_y", double(nyf) * 19 * 8, fluxf * nyf);
   const int ku = trace_kind(s, "update", ncd * 128 + double(nxf + nyf) * 4 * 8, kUpdateFlops * ncd);
   // uniform regions (stepping only): the faces only deep cells use are skipped
-  const uint8_t* deep = stage > 0 ? s->deep : nullptr;
+  const uint8_t* deep = stage > 0 && s->uniform_skip ? s->deep : nullptr;
   if (deep) {
     const int ku0 = trace_kind(s, "uniform", ncd * 32, 0.0);
     trace_begin(s, ku0);

@@ -121,6 +121,7 @@ int fv2d_fused_prepare(hteno_solver* s, const Geo& G, double* scratch) {
   if (cudaEventCreate(&a) != cudaSuccess || cudaEventCreate(&b) != cudaSuccess)
     return set_error(s, HTENO_ERR_CUDA, "tuner events");
   fused::StageArgs args{s->q, nullptr, scratch, nullptr};
+  args.skip_uniform = false;  // time the full work, not the (mostly uniform) initial state
   int best = 0;
   float best_ms = 3.4e38f;
   for (int v = 0; v < kNumVariants; ++v) {
@@ -151,6 +152,7 @@ int fv2d_fused_prepare(hteno_solver* s, const Geo& G, double* scratch) {
 void fv2d_fused_step(hteno_solver* s, const Geo& G, double* qc) {
   fused::StageArgs a1{s->q, nullptr, s->q0, s->dstate}, a2{s->q0, s->q, qc, s->dstate},
       a3{qc, s->q, s->q, s->dstate};
+  a1.skip_uniform = a2.skip_uniform = a3.skip_uniform = s->uniform_skip;
   if (s->router) {
     const int kc = trace_kind(s, "classify", 0.0, 0.0);
     trace_begin(s, kc);
@@ -172,7 +174,9 @@ void fv2d_fused_step(hteno_solver* s, const Geo& G, double* qc) {
 }
 
 void fv2d_fused_residual(hteno_solver* s, const Geo& G, const double* q, double* rhs) {
-  launch_stage(s, G, 0, fused::StageArgs{q, nullptr, rhs, nullptr});
+  fused::StageArgs a{q, nullptr, rhs, nullptr};
+  a.skip_uniform = s->uniform_skip;
+  launch_stage(s, G, 0, a);
 }
 
 const char* fv2d_fused_variant_name(int v) {

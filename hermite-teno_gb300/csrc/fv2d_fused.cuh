@@ -171,7 +171,20 @@ struct StageArgs {
   const uint8_t* mx = nullptr;
   const uint8_t* my = nullptr;
   unsigned long long* audit = nullptr;  // [5] RouteCount sums when auditing this stage
+  bool skip_uniform = true;  // tiles of one tame float state get their (exactly zero) residual directly
 };
+
+// A float state whose fluxes stay finite through the characteristic round trip: density and
+// pressure in [2^-16, 2^16], Mach number at most 8 (the round trip's condition is ~ Mach^2, so
+// the reconstructed state keeps a relative 2^-12 of float precision and stays positive, and no
+// product of the face or flux arithmetic leaves the float range).
+__device__ __forceinline__ bool tame_state(float r, float mx, float my, float e, float g1, float gamma) {
+  const float ir = __frcp_rn(r);
+  const float u = mx * ir, v = my * ir;
+  const float p = (e - 0.5f * (mx * u + my * v)) * g1;
+  constexpr float lo = 0x1p-16f, hi = 0x1p16f;
+  return r >= lo && r <= hi && p >= lo && p <= hi && u * u + v * v <= 64.0f * (gamma * p * ir);
+}
 
 // The tile at (i0, j0) of grid G.  Every thread of the block must call it (barriers inside).
 // Returns this thread's max wave speed over the cells it updated (stage 3) and ORs health flags
@@ -215,6 +228,25 @@ __device__ __forceinline__ double tile_stage(const DevConst& C, const Geo& G, in
   }
   __syncthreads();
 
+  // Uniform tile: the tile and its 3-cell halo hold one tame float state, bit for bit.  Every flux
+  // of every cell of the tile is then computed from identical inputs, each pair's difference is
+  // +0, and so is the residual: phases B-E are skipped, the same bits result.  (Not while
+  // auditing a router: the audit counts every stencil.)
+  bool flat = false;
+  if (a.skip_uniform && !audit) {
+    const unsigned b0 = __float_as_uint(S.q[0][0][0]), b1 = __float_as_uint(S.q[1][0][0]);
+    const unsigned b2 = __float_as_uint(S.q[2][0][0]), b3 = __float_as_uint(S.q[3][0][0]);
+    bool same = true;
+    for (int it = tid; it < Sh::W * Sh::H; it += NT) {
+      const int y = it / Sh::W, x = it - y * Sh::W;
+      same = same && __float_as_uint(S.q[0][y][x]) == b0 && __float_as_uint(S.q[1][y][x]) == b1 &&
+             __float_as_uint(S.q[2][y][x]) == b2 && __float_as_uint(S.q[3][y][x]) == b3;
+    }
+    flat = __syncthreads_and(same) &&
+           tame_state(S.q[0][0][0], S.q[1][0][0], S.q[2][0][0], S.q[3][0][0], g1, float(G.gamma));
+  }
+
+  if (!flat) {
   // B: x faces, characteristic reconstruction
   for (int it = tid; it < Sh::XN; it += NT) {
     const int rr = it / Sh::XF, f = it - rr * Sh::XF;
@@ -349,6 +381,7 @@ __device__ __forceinline__ double tile_stage(const DevConst& C, const Geo& G, in
     for (int v = 0; v < 4; ++v) S.fy[v][gg][col] = acc[v];
   }
   __syncthreads();
+  }  // !flat
 
   // F: residual and SSP-RK3 stage in double
   float msf = 0.f;
@@ -363,9 +396,12 @@ __device__ __forceinline__ double tile_stage(const DevConst& C, const Geo& G, in
 #pragma unroll
     for (int v = 0; v < 4; ++v) {
       // float flux differences are exact in double, so the update stays conservative
-      const double dfx = f2d(S.fx[v][y][x]) - f2d(S.fx[v][y][x + 1]);
-      const double dfy = f2d(S.fy[v][y][x]) - f2d(S.fy[v][y + 1][x]);
-      const double rhs = fma(dfx, rdx, dfy * rdy);
+      double rhs = 0.0;
+      if (!flat) {
+        const double dfx = f2d(S.fx[v][y][x]) - f2d(S.fx[v][y][x + 1]);
+        const double dfy = f2d(S.fy[v][y][x]) - f2d(S.fy[v][y + 1][x]);
+        rhs = fma(dfx, rdx, dfy * rdy);
+      }
       if (stage == 0) {
         a.qout[v * nc + k] = rhs;
       } else {

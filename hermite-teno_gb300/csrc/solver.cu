@@ -1,6 +1,7 @@
 // Solver handles and the C-ABI around the scheme back ends (include/hteno.h).
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 
@@ -187,6 +188,9 @@ int hteno_create(const hteno_config* cfg, hteno_solver** out) {
   s->dx = (c.xr - c.xl) / c.nx;
   s->dy = c.dims == 2 ? (c.yt - c.yb) / c.ny : 1.0;
   cudaGetDevice(&s->device);
+  // HTENO_UNIFORM_SKIP=0 computes uniform regions in full (a check that skipping them is exact)
+  const char* us = std::getenv("HTENO_UNIFORM_SKIP");
+  s->uniform_skip = !(us && us[0] == '0');
 
   auto fail = [&](int code) {
     release(s);

@@ -94,6 +94,49 @@ def test_mixed_tile_shapes_agree_bitwise(hteno_lib, cuda):
         np.testing.assert_array_equal(o, outs[0])
 
 
+def blob_field(nx, ny, scale=1.0, mach=0.3):
+    """A dense, high-pressure disc in a uniform stream: most tiles are uniform."""
+    from hteno import ic
+
+    x = (np.arange(nx) + 0.5) / nx
+    y = (np.arange(ny) + 0.5) / ny
+    X, Y = np.meshgrid(x, y)
+    disc = (X - 0.45) ** 2 + (Y - 0.5) ** 2 < 0.12 ** 2
+    u = mach * np.sqrt(1.4) + 0 * X
+    return np.ascontiguousarray(ic.conservative2(scale * (1.0 + disc), u, -0.2 * u, scale * (1.0 + 2.0 * disc)))
+
+
+def four_quadrant(nx, ny, seed):
+    from hteno import ic
+
+    return ic.four_quadrant(nx, ny, seed)
+
+
+UNIFORM_CASES = {
+    "four-quadrant": (lambda: four_quadrant(150, 110, 3), dict(flux=1)),
+    "stream-periodic": (lambda: blob_field(160, 96), dict(flux=0, bc=1)),
+    "tiny-density": (lambda: blob_field(160, 96, scale=1e-6), dict(flux=1)),  # below 2^-16
+    "hypersonic": (lambda: blob_field(160, 96, mach=12.0), dict(flux=1)),  # Mach above 8
+}
+
+
+@pytest.mark.parametrize("case", list(UNIFORM_CASES))
+def test_mixed_uniform_tiles_exact(hteno_lib, cuda, case):
+    """Tiles whose cells and halo hold one tame float state take their residual (exactly +0)
+    without computing faces; HTENO_UNIFORM_SKIP=0 computes them in full: the same bits.  (The
+    batch path runs the same tile code; it matches the single-grid path bit for bit.)"""
+    make, kw = UNIFORM_CASES[case]
+    q = make()
+    try:
+        os.environ["HTENO_UNIFORM_SKIP"] = "0"
+        full, t_full, n_full, _ = run(hteno_lib, q, 40, precision=1, **kw)
+    finally:
+        os.environ.pop("HTENO_UNIFORM_SKIP", None)
+    got, t_got, n_got, _ = run(hteno_lib, q, 40, precision=1, **kw)
+    assert n_got == n_full and t_got == t_full
+    np.testing.assert_array_equal(got, full)
+
+
 def test_mixed_periodic_conservation(hteno_lib, cuda):
     q = periodic_box(128, 96)
     got, _, _, _ = run(hteno_lib, q, 60, flux=1, bc=1, precision=1)
