@@ -1,6 +1,6 @@
 // FVHermite::System2D on the GPU (FVHermite_System2D.cpp:393-819): cell averages u and first
 // moments v = du/dx, w = du/dy.  Per stage:
-//   limit_x / limit_y : hermiteLimiter on v along x and on w along y.  The reference updates in
+//   limit             : hermiteLimiter on v along x and on w along y.  The reference updates in
 //                       place while sweeping (limitDerivatives, :393-427), i.e. a Gauss-Seidel
 //                       sweep: one thread per (row, field) resp. (column, field) walks the line.
 //   prim              : primitives of u
@@ -34,10 +34,10 @@ int hermite2d_setup(hteno_solver* s) {
 int hermite2d_prepare(hteno_solver* s) {
   const GeoH G = geo_of(s);
   const size_t nc = size_t(G.nx) * G.ny;
-  if (s->cfg.precision == HTENO_PREC_MIXED)
-    kh_prim<<<unsigned((nc + 255) / 256), 256, 0, s->stream>>>(G, s->q, carve_h<float>(s->work, G.nx, G.ny).prim,
-                                                              s->dstate, 1);
-  else
+  if (s->cfg.precision == HTENO_PREC_MIXED) {
+    const WorkH<float> W = carve_h<float>(s->work, G.nx, G.ny);
+    kh_prim_f<<<unsigned((nc + 255) / 256), 256, 0, s->stream>>>(G, s->q, W.qt, W.primt, s->dstate);
+  } else
     hermite2d_fp64_prim(s, G);
   return cuda_error(s, cudaGetLastError(), "kh_prim");
 }

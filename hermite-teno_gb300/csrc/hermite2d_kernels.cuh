@@ -8,6 +8,7 @@
 
 #include "hermite_math.cuh"
 #include "hteno_internal.h"
+#include "mixed_conv.cuh"
 #include "parity_math.cuh"
 
 namespace hteno {
@@ -18,7 +19,21 @@ constexpr int kHFluxThreads = 64;
 struct GeoH {
   int nx, ny;
   double dx, dy, area, gamma, g1, g3;  // g3 = gamma - 3 as the reference computes it
+  double rdx, rdy;                     // 1/dx, 1/dy (mixed-precision update)
 };
+
+// Loads of the double state into the compute type and back: for float on the integer pipes
+// (mix::d2f / f2d), for double the identity.
+template <typename T>
+__device__ __forceinline__ T from_d(double x) {
+  if constexpr (std::is_same<T, float>::value) return mix::d2f(x);
+  else return x;
+}
+template <typename T>
+__device__ __forceinline__ double to_d(T x) {
+  if constexpr (std::is_same<T, float>::value) return mix::f2d(x);
+  else return x;
+}
 
 template <typename T>
 struct WorkH {
@@ -31,12 +46,20 @@ struct WorkH {
   T* yroe;        // [7][ny+1][nx]
   T* fx;          // [12][ny][nx+1]: kind (0 u, 1 moment along the sweep, 2 cross moment) x field
   T* fy;          // [12][ny+1][nx]
+  // the state as the face kernels read it, in the compute type: for double the state arrays
+  // themselves (set by the launcher); for float copies written by the kernels that produce the
+  // state (update, limiter), so each cell is converted once per stage, not once per stencil use
+  T* qt;          // [4][nc]
+  T* vt;          // [4][nc] limited moments
+  T* wt;
+  T* primt;       // [4][nc] u, v, h, sqrt|rho|
 };
 
 template <typename T>
 size_t work_bytes_h(int nx, int ny) {
   const size_t nc = size_t(nx) * ny, nxf = size_t(nx + 1) * ny, nyf = size_t(ny + 1) * nx;
-  return 12 * nc * sizeof(double) + (24 + 7 + 12) * (nxf + nyf) * sizeof(T) + 256 * 12;
+  const size_t copies = std::is_same<T, float>::value ? 16 * nc * sizeof(float) + 256 * 4 : 0;
+  return 12 * nc * sizeof(double) + (24 + 7 + 12) * (nxf + nyf) * sizeof(T) + 256 * 12 + copies;
 }
 
 template <typename T>
@@ -58,6 +81,14 @@ WorkH<T> carve_h(void* base, int nx, int ny) {
   w.yroe = reinterpret_cast<T*>(take(7 * nyf * sizeof(T)));
   w.fx = reinterpret_cast<T*>(take(12 * nxf * sizeof(T)));
   w.fy = reinterpret_cast<T*>(take(12 * nyf * sizeof(T)));
+  w.qt = nullptr;
+  w.vt = w.wt = w.primt = nullptr;
+  if constexpr (std::is_same<T, float>::value) {
+    w.qt = reinterpret_cast<T*>(take(4 * nc * sizeof(T)));
+    w.vt = reinterpret_cast<T*>(take(4 * nc * sizeof(T)));
+    w.wt = reinterpret_cast<T*>(take(4 * nc * sizeof(T)));
+    w.primt = reinterpret_cast<T*>(take(4 * nc * sizeof(T)));
+  }
   return w;
 }
 
@@ -105,48 +136,269 @@ __global__ void kh_prim(GeoH G, const double* __restrict__ q, double* __restrict
   if (do_max) block_max_to(ms, &st->maxbits);
 }
 
-// Gauss-Seidel hermiteLimiter sweep.  DIR 1: line = row j, field e, walks i and updates v;
-// DIR 2: line = column i, field e, walks j and updates w.  The neighbour beyond the last cell is
-// the zero-gradient ghost, which holds the pre-sweep value.
-template <typename T, int DIR>
-__global__ void kh_limit(GeoH G, HermiteK<T> K, const double* __restrict__ q, double* d,
-                         const StepState* st) {
-  if (st->done) return;
-  const int nl = DIR == 1 ? G.ny : G.nx;  // number of lines
-  const int n = DIR == 1 ? G.nx : G.ny;   // length of a line
-  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= 4 * nl) return;
-  const int line = idx % nl, e = idx / nl;
+// Mixed precision, after a new state: the float copies of the state and of its primitives that
+// the face kernels read, and the first dt's max wave speed.
+__global__ void kh_prim_f(GeoH G, const double* __restrict__ q, float* __restrict__ qt,
+                          float* __restrict__ primt, StepState* st) {
   const size_t nc = size_t(G.nx) * G.ny;
-  const size_t stride = DIR == 1 ? 1 : size_t(G.nx);
-  const size_t base = size_t(e) * nc + (DIR == 1 ? size_t(line) * G.nx : size_t(line));
-  T um = T(q[base]), u0 = um, up;
-  T dm = T(d[base]);                       // ghost before the first cell: old value of cell 0
-  T dcur = dm;
-  for (int s = 0; s < n; ++s) {
-    const size_t o = base + size_t(s) * stride;
-    const size_t on = base + size_t(s + 1 < n ? s + 1 : n - 1) * stride;
-    up = T(q[on]);
-    const T dn = T(d[on]);                 // not yet updated (or the ghost = old last value)
-    T uu[3] = {um, u0, up};
-    T dd[3] = {dm, dcur, dn};
-    T lim;
-    if constexpr (std::is_same<T, double>::value) lim = par::hermite_limiter(K, uu, dd);
-    else lim = hermite_limiter(K, uu, dd);
-    d[o] = double(lim);
-    dm = lim;
-    um = u0;
-    u0 = up;
-    dcur = dn;
+  const size_t k = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+  double ms = 0.0;
+  if (k < nc) {
+    double qq[4] = {q[k], q[nc + k], q[2 * nc + k], q[3 * nc + k]};
+    double u, v, p, h, sr;
+    cell_prim(G.g1, qq, u, v, p, h, sr);
+#pragma unroll
+    for (int e = 0; e < 4; ++e) qt[e * nc + k] = mix::d2f(qq[e]);
+    primt[k] = mix::d2f(u);
+    primt[nc + k] = mix::d2f(v);
+    primt[2 * nc + k] = mix::d2f(h);
+    primt[3 * nc + k] = mix::d2f(sr);
+    ms = cell_max_speed(G.gamma, qq[0], u, v, p);
+  }
+  block_max_to(ms, &st->maxbits);
+}
+
+// Gauss-Seidel hermiteLimiter sweeps of both directions in one launch.  Blocks [0, nbx): x lines
+// (line = row j of field e, walks i, updates v); blocks [nbx, ...): y lines (column i, walks j,
+// updates w).  The two directions touch different arrays, so they run side by side.  The
+// neighbour beyond the last cell is the zero-gradient ghost, which holds the pre-sweep value; the
+// one before the first cell is the first cell (old value).
+//
+// Each block takes 32 lines of one field.  The sweep itself is sequential along a line (each cell
+// reads its left neighbour's limited value), so one thread walks each line; the block stages the
+// lines through shared memory in chunks of kLimChunk cells with coalesced loads and stores (along
+// the rows for x lines, across the columns for y lines), keeping the global-memory latency off
+// the sweep's dependency chain.
+constexpr int kLimLines = 32, kLimChunk = 64, kLimThreads = 128;
+
+template <typename T>
+__global__ void __launch_bounds__(kLimThreads) kh_limit(GeoH G, HermiteK<T> K,
+                                                        const double* __restrict__ q,
+                                                        double* __restrict__ v,
+                                                        double* __restrict__ w, int nbx,
+                                                        const StepState* st) {
+  if (st->done) return;
+  constexpr int L = kLimLines, C = kLimChunk;
+  __shared__ double sq[C + 1][L + 1];
+  __shared__ double sd[C + 1][L + 1];
+  const bool xd = int(blockIdx.x) < nbx;
+  const int b = xd ? int(blockIdx.x) : int(blockIdx.x) - nbx;
+  const int nl = xd ? G.ny : G.nx;  // number of lines
+  const int n = xd ? G.nx : G.ny;   // length of a line
+  const int nlb = (nl + L - 1) / L;
+  const int e = b / nlb, l0 = (b - e * nlb) * L;
+  double* __restrict__ d = xd ? v : w;
+  const size_t nc = size_t(G.nx) * G.ny;
+  auto at = [&](int l, int s) -> size_t {
+    return size_t(e) * nc + (xd ? size_t(l) * G.nx + s : size_t(s) * G.nx + l);
+  };
+  const int tid = threadIdx.x;
+  const bool sweeper = tid < L && l0 + tid < nl;
+  T um = T(0), u0 = T(0), dm = T(0), dcur = T(0);
+  if (sweeper) {
+    um = from_d<T>(q[at(l0 + tid, 0)]);
+    u0 = um;
+    dm = from_d<T>(d[at(l0 + tid, 0)]);
+    dcur = dm;
+  }
+  for (int c0 = 0; c0 < n; c0 += C) {
+    const int cnt = min(C, n - c0);
+    // cells c0 .. c0 + cnt of each line (the last is the look-ahead, clamped to the line's end);
+    // every d value read here is a pre-sweep value: the sweep has written cells < c0 only
+    for (int it = tid; it < (cnt + 1) * L; it += kLimThreads) {
+      int l, k;
+      if (xd) { k = it % (cnt + 1); l = it / (cnt + 1); }
+      else { l = it % L; k = it / L; }
+      if (l0 + l < nl) {
+        const size_t o = at(l0 + l, min(c0 + k, n - 1));
+        sq[k][l] = q[o];
+        sd[k][l] = d[o];
+      }
+    }
+    __syncthreads();
+    if (sweeper) {
+      for (int k = 0; k < cnt; ++k) {
+        const T up = from_d<T>(sq[k + 1][tid]);
+        const T dn = from_d<T>(sd[k + 1][tid]);  // not yet limited (or the ghost = pre-sweep last value)
+        T uu[3] = {um, u0, up};
+        T dd[3] = {dm, dcur, dn};
+        T lim;
+        if constexpr (std::is_same<T, double>::value) lim = par::hermite_limiter(K, uu, dd);
+        else lim = hermite_limiter(K, uu, dd);
+        sd[k][tid] = to_d<T>(lim);
+        dm = lim;
+        um = u0;
+        u0 = up;
+        dcur = dn;
+      }
+    }
+    __syncthreads();
+    for (int it = tid; it < cnt * L; it += kLimThreads) {
+      int l, k;
+      if (xd) { k = it % cnt; l = it / cnt; }
+      else { l = it % L; k = it / L; }
+      if (l0 + l < nl) d[at(l0 + l, c0 + k)] = sd[k][l];
+    }
+    __syncthreads();
+  }
+}
+
+// Mixed precision: the same sweeps with the float limiter restated so that the part that waits
+// for the left neighbour's limited value d0 is short.  hermiteLimiter's result is
+//   lim = [w0 (p0/lw0 - Q) + w1 p1 + w2 p2] / (w0 + w1 + w2),  w_k = lw_k (1 + tau / (s_k + eps))
+// where only p0 = P - d0/4 and s0 = |(a ud0 + B) ud0 + C|/6720 (ud0 = d0 dif, the smoothness
+// measure fullPointsSI expanded in ud0) depend on d0.  Every other quantity of a cell is computed
+// by all threads of the block in parallel, before the sweep: B, C, s1, s2, E = P/lw0 - Q,
+// M = lw1 r1 + lw2 r2, L = lw1 p1 + lw2 p2, N = lw1 r1 p1 + lw2 r2 p2 with r_k = 1/(s_k + eps).
+// The sweep then evaluates, per cell,
+//   tau = (|s0 - s1| + |s0 - s2|)^2 / 4,  w0 = lw0 (1 + tau / (s0 + eps)),
+//   lim = (w0 (E - d0 / (4 lw0)) + L + tau N) / (w0 + lw1 + lw2 + tau M).
+constexpr int kLimChunkF = 32;
+
+__global__ void __launch_bounds__(kLimThreads, 4) kh_limit_f(GeoH G, HermiteK<float> K,
+                                                          const double* __restrict__ q,
+                                                          double* __restrict__ v,
+                                                          double* __restrict__ w,
+                                                          float* __restrict__ vt,
+                                                          float* __restrict__ wt, int nbx,
+                                                          const StepState* st) {
+  if (st->done) return;
+  constexpr int L = kLimLines, C = kLimChunkF;
+  constexpr float lw0 = 1.0f - 2e-5f, lw1 = 1e-5f, lw2 = 1e-5f, eps = float(HTENO_LAG_EPS);
+  __shared__ float pre[8][C][L + 1];
+  __shared__ union {
+    struct {
+      float u[C + 2][L + 1];  // cells c0 - 1 .. c0 + cnt (clamped)
+      float d[C][L + 1];      // pre-sweep d of cells c0 + 1 .. c0 + cnt (clamped)
+    } in;
+    double out[C][L + 1];     // limited values of cells c0 .. c0 + cnt - 1
+  } S;
+  __shared__ float outf[C][L + 1];  // the same in float
+  const bool xd = int(blockIdx.x) < nbx;
+  const int b = xd ? int(blockIdx.x) : int(blockIdx.x) - nbx;
+  const int nl = xd ? G.ny : G.nx;
+  const int n = xd ? G.nx : G.ny;
+  const int nlb = (nl + L - 1) / L;
+  const int e = b / nlb, l0 = (b - e * nlb) * L;
+  double* __restrict__ d = xd ? v : w;
+  float* __restrict__ dt = xd ? vt : wt;
+  const size_t nc = size_t(G.nx) * G.ny;
+  auto at = [&](int l, int s) -> size_t {
+    return size_t(e) * nc + (xd ? size_t(l) * G.nx + s : size_t(s) * G.nx + l);
+  };
+  const int tid = threadIdx.x;
+  const bool sweeper = tid < L && l0 + tid < nl;
+  const float dif = K.dif, rdif = K.rdif;
+  float d0 = sweeper ? mix::d2f(d[at(l0 + tid, 0)]) : 0.f;  // ghost before the first cell
+  // Staging slots of this thread (element tid + 128 j of the chunk's line-major or cell-major
+  // block).  x lines: consecutive threads take consecutive cells of a row; y lines: consecutive
+  // threads take consecutive lines (columns) of a cell row; both coalesce.  u: cells c0 - 1 ..
+  // c0 + cnt of the chunk (row k = 0 .. cnt + 1); d: pre-sweep d of cells c0 + 1 .. c0 + cnt
+  // (row k = 0 .. cnt - 1).  The next chunk's values are loaded into registers while this
+  // chunk is processed.
+  constexpr int NU = ((C + 2) * L + kLimThreads - 1) / kLimThreads, ND = C * L / kLimThreads;
+  auto slot_u = [&](int j, int& l, int& k) {
+    const int el = tid + kLimThreads * j;
+    if (xd) { l = el / (C + 2); k = el - l * (C + 2); }
+    else { l = el % L; k = el / L; }
+  };
+  auto slot_d = [&](int j, int& l, int& k) {
+    const int el = tid + kLimThreads * j;
+    if (xd) { l = el / C; k = el % C; }
+    else { l = el % L; k = el / L; }
+  };
+  double bu[NU], bd[ND];
+  auto fetch = [&](int c) {
+    const int m = min(C, n - c);
+#pragma unroll
+    for (int j = 0; j < NU; ++j) {
+      int l, k;
+      slot_u(j, l, k);
+      bu[j] = (l < L && l0 + l < nl && k < m + 2) ? q[at(l0 + l, min(max(c - 1 + k, 0), n - 1))] : 0.0;
+    }
+#pragma unroll
+    for (int j = 0; j < ND; ++j) {
+      int l, k;
+      slot_d(j, l, k);
+      bd[j] = (l < L && l0 + l < nl && k < m) ? d[at(l0 + l, min(c + 1 + k, n - 1))] : 0.0;
+    }
+  };
+  fetch(0);
+  for (int c0 = 0; c0 < n; c0 += C) {
+    const int cnt = min(C, n - c0);
+#pragma unroll
+    for (int j = 0; j < NU; ++j) {
+      int l, k;
+      slot_u(j, l, k);
+      if (l < L && k < cnt + 2) S.in.u[k][l] = mix::d2f(bu[j]);
+    }
+#pragma unroll
+    for (int j = 0; j < ND; ++j) {
+      int l, k;
+      slot_d(j, l, k);
+      if (l < L && k < cnt) S.in.d[k][l] = mix::d2f(bd[j]);
+    }
+    if (c0 + C < n) fetch(c0 + C);  // in flight during the precompute and the sweep
+    __syncthreads();
+    for (int it = tid; it < cnt * L; it += kLimThreads) {
+      const int l = it % L, k = it / L;
+      const float u0 = S.in.u[k][l], u1 = S.in.u[k + 1][l], u2 = S.in.u[k + 2][l];
+      const float ud2 = S.in.d[k][l] * dif;
+      const float p1 = (u1 - u0) * rdif, p2 = (u2 - u1) * rdif;
+      const float s1 = (u0 - u1) * (u0 - u1), s2 = (u1 - u2) * (u1 - u2);
+      const float r1 = 1.0f / (s1 + eps), r2 = 1.0f / (s2 + eps);
+      constexpr float k6720 = 1.0f / 6720.0f;
+      const float B = (1029270.0f * u2 - 2129184.0f * u1 + 1099914.0f * u0 - 494958.0f * ud2) * k6720;
+      const float Cc = ((-1029270.0f * u0 + 2129184.0f * u1 - 1099914.0f * u2 + 281121.0f * ud2) * ud2 +
+                        (1099445.0f * u2 - 4317056.0f * u1 + 2118166.0f * u0) * u2 +
+                        4317056.0f * (u1 - u0) * u1 + 1099445.0f * u0 * u0) * k6720;
+      const float P = 0.75f * (u2 - u0) * rdif - 0.25f * S.in.d[k][l];
+      pre[0][k][l] = B;
+      pre[1][k][l] = Cc;
+      pre[2][k][l] = s1;
+      pre[3][k][l] = s2;
+      pre[4][k][l] = P * (1.0f / lw0) - ((lw1 / lw0) * p1 + (lw2 / lw0) * p2);
+      pre[5][k][l] = lw1 * r1 + lw2 * r2;
+      pre[6][k][l] = lw1 * p1 + lw2 * p2;
+      pre[7][k][l] = lw1 * r1 * p1 + lw2 * r2 * p2;
+    }
+    __syncthreads();  // the staged inputs are consumed: S.out may overwrite them
+    if (sweeper) {
+      constexpr float a = 281121.0f / 6720.0f, c4 = 0.25f / lw0;
+      for (int k = 0; k < cnt; ++k) {
+        const float ud0 = d0 * dif;
+        const float s0 = fabsf(fmaf(fmaf(a, ud0, pre[0][k][tid]), ud0, pre[1][k][tid]));
+        const float t = fabsf(s0 - pre[2][k][tid]) + fabsf(s0 - pre[3][k][tid]);
+        const float tau = 0.25f * t * t;
+        const float w0 = lw0 * fmaf(tau, __fdividef(1.0f, s0 + eps), 1.0f);
+        const float num = fmaf(w0, fmaf(-c4, d0, pre[4][k][tid]), fmaf(tau, pre[7][k][tid], pre[6][k][tid]));
+        const float den = w0 + fmaf(tau, pre[5][k][tid], lw1 + lw2);
+        d0 = __fdividef(num, den);
+        S.out[k][tid] = mix::f2d(d0);
+        outf[k][tid] = d0;
+      }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < ND; ++j) {
+      int l, k;
+      slot_d(j, l, k);
+      if (l < L && l0 + l < nl && k < cnt) {
+        const size_t o = at(l0 + l, c0 + k);
+        d[o] = S.out[k][l];
+        dt[o] = outf[k][l];
+      }
+    }
+    __syncthreads();
   }
 }
 
 template <typename T, int DIR>
 __global__ void __launch_bounds__(kHFaceThreads) kh_faces(GeoH G, HermiteK<T> K,
-                                                         const double* __restrict__ q,
-                                                         const double* __restrict__ v,
-                                                         const double* __restrict__ w,
-                                                         const double* __restrict__ prim,
+                                                         const T* __restrict__ q,
+                                                         const T* __restrict__ v,
+                                                         const T* __restrict__ w,
+                                                         const T* __restrict__ prim,
                                                          T* __restrict__ fc, T* __restrict__ froe,
                                                          const StepState* st) {
   if (st && st->done) return;
@@ -163,8 +415,8 @@ __global__ void __launch_bounds__(kHFaceThreads) kh_faces(GeoH G, HermiteK<T> K,
     const int m = bmap(s, ns, HTENO_BC_ZEROGRAD);
     return DIR == 1 ? size_t(t) * G.nx + m : size_t(m) * G.nx + t;
   };
-  const double* mn = DIR == 1 ? v : w;  // moment along the sweep (HTENO)
-  const double* mt = DIR == 1 ? w : v;  // cross moment (TENO5)
+  const T* mn = DIR == 1 ? v : w;  // moment along the sweep (HTENO)
+  const T* mt = DIR == 1 ? w : v;  // cross moment (TENO5)
   const size_t ca = cell(f - 1), cb = cell(f);
   const size_t nface = size_t(nf) * nt;
   const size_t o = DIR == 1 ? size_t(t) * nf + f : size_t(f) * nt + t;
@@ -217,16 +469,15 @@ __global__ void __launch_bounds__(kHFaceThreads) kh_faces(GeoH G, HermiteK<T> K,
     froe[6 * nface + o] = E.b1;
     return;
   }
-  const Roe2<T> R = roe2<T>(T(G.g1), T(prim[3 * nc + ca]), T(prim[ca]), T(prim[nc + ca]),
-                            T(prim[2 * nc + ca]), T(prim[3 * nc + cb]), T(prim[cb]),
-                            T(prim[nc + cb]), T(prim[2 * nc + cb]));
+  const Roe2<T> R = roe2<T>(T(G.g1), prim[3 * nc + ca], prim[ca], prim[nc + ca], prim[2 * nc + ca],
+                            prim[3 * nc + cb], prim[cb], prim[nc + cb], prim[2 * nc + cb]);
   {
     T A[4][4], B[4][4];
 #pragma unroll
     for (int m = 0; m < 4; ++m) {
       const size_t c = cell(f - 2 + m);
-      T a4[4] = {T(q[c]), T(q[nc + c]), T(q[2 * nc + c]), T(q[3 * nc + c])};
-      T b4[4] = {T(mn[c]), T(mn[nc + c]), T(mn[2 * nc + c]), T(mn[3 * nc + c])};
+      T a4[4] = {q[c], q[nc + c], q[2 * nc + c], q[3 * nc + c]};
+      T b4[4] = {mn[c], mn[nc + c], mn[2 * nc + c], mn[3 * nc + c]};
       T ca4[4], cb4[4];
       roe_left(R, DIR, a4, ca4);
       roe_left(R, DIR, b4, cb4);
@@ -251,7 +502,7 @@ __global__ void __launch_bounds__(kHFaceThreads) kh_faces(GeoH G, HermiteK<T> K,
 #pragma unroll
     for (int m = 0; m < 6; ++m) {
       const size_t c = cell(f - 3 + m);
-      T c4[4] = {T(mt[c]), T(mt[nc + c]), T(mt[2 * nc + c]), T(mt[3 * nc + c])};
+      T c4[4] = {mt[c], mt[nc + c], mt[2 * nc + c], mt[3 * nc + c]};
       T cc[4];
       roe_left(R, DIR, c4, cc);
 #pragma unroll
@@ -384,7 +635,8 @@ __global__ void kh_update(GeoH G, int stage, const T* __restrict__ fx, const T* 
                           double* __restrict__ v, double* __restrict__ v0,
                           double* __restrict__ vs, double* __restrict__ w,
                           double* __restrict__ w0, double* __restrict__ ws,
-                          double* __restrict__ prim, StepState* st) {
+                          double* __restrict__ prim, float* __restrict__ qt,
+                          float* __restrict__ primt, StepState* st) {
   if (st->done) return;
   const size_t nc = size_t(G.nx) * G.ny;
   const size_t k = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
@@ -396,43 +648,92 @@ __global__ void kh_update(GeoH G, int stage, const T* __restrict__ fx, const T* 
     const size_t ox = size_t(j) * (G.nx + 1) + i, oy = size_t(j) * G.nx + i;
     const double dt = st->dt;
     double qn[4];
+    if constexpr (std::is_same<T, float>::value) {
+      // mixed precision: float flux differences are exact in double; RK stage with FMAs; the
+      // conversions on the integer pipes; primitives with a refined float reciprocal of rho
+      auto rhs = [&](int kx, int ky, int e) {
+        const double dfx = mix::f2d(fx[(kx + e) * nxf + ox]) - mix::f2d(fx[(kx + e) * nxf + ox + 1]);
+        const double dfy = mix::f2d(fy[(ky + e) * nyf + oy]) - mix::f2d(fy[(ky + e) * nyf + oy + G.nx]);
+        return fma(dfx, G.rdx, dfy * G.rdy);
+      };
 #pragma unroll
-    for (int e = 0; e < 4; ++e) {
-      // kinds: x-sweep (0 u, 1 v, 2 w), y-sweep (0 u, 1 w, 2 v)
-      const double ru = ((double(fx[(0 + e) * nxf + ox]) - double(fx[(0 + e) * nxf + ox + 1])) * G.dy +
-                         (double(fy[(0 + e) * nyf + oy]) - double(fy[(0 + e) * nyf + oy + G.nx])) * G.dx) / G.area + 0.0;
-      const double rv = ((double(fx[(4 + e) * nxf + ox]) - double(fx[(4 + e) * nxf + ox + 1])) * G.dy +
-                         (double(fy[(8 + e) * nyf + oy]) - double(fy[(8 + e) * nyf + oy + G.nx])) * G.dx) / G.area + 0.0;
-      const double rw = ((double(fx[(8 + e) * nxf + ox]) - double(fx[(8 + e) * nxf + ox + 1])) * G.dy +
-                         (double(fy[(4 + e) * nyf + oy]) - double(fy[(4 + e) * nyf + oy + G.nx])) * G.dx) / G.area + 0.0;
-      const size_t c = size_t(e) * nc + k;
-      double bq, bv, bw, cq = q[c], cv, cw;
-      if (stage == 1) {
-        bq = cq; bv = v[c]; bw = w[c];   // save() after the first rhs: limited moments
-        q0[c] = bq; v0[c] = bv; w0[c] = bw;
-        cv = bv; cw = bw;
-      } else {
-        bq = q0[c]; bv = v0[c]; bw = w0[c];
-        cv = vs[c]; cw = ws[c];          // unlimited stage values (cell.v1 / cell.v2)
+      for (int e = 0; e < 4; ++e) {
+        const double ru = rhs(0, 0, e), rv = rhs(4, 8, e), rw = rhs(8, 4, e);
+        const size_t c = size_t(e) * nc + k;
+        double bq, bv, bw, cq = q[c], cv, cw;
+        if (stage == 1) {
+          bq = cq; bv = v[c]; bw = w[c];
+          q0[c] = bq; v0[c] = bv; w0[c] = bw;
+          cv = bv; cw = bw;
+        } else {
+          bq = q0[c]; bv = v0[c]; bw = w0[c];
+          cv = vs[c]; cw = ws[c];
+        }
+        qn[e] = mix::rk_stage(bq, cq, ru, dt, stage);
+        const double nv = mix::rk_stage(bv, cv, rv, dt, stage);
+        const double nw = mix::rk_stage(bw, cw, rw, dt, stage);
+        q[c] = qn[e];
+        qt[c] = mix::d2f(qn[e]);
+        v[c] = nv;
+        vs[c] = nv;
+        w[c] = nw;
+        ws[c] = nw;
       }
-      qn[e] = ssprk3(bq, cq, ru, dt, stage);
-      const double nv = ssprk3(bv, cv, rv, dt, stage);
-      const double nw = ssprk3(bw, cw, rw, dt, stage);
-      q[c] = qn[e];
-      v[c] = nv;
-      vs[c] = nv;
-      w[c] = nw;
-      ws[c] = nw;
+      const float fr = mix::d2f(qn[0]);
+      double ir = mix::f2d(__frcp_rn(fr));
+      ir = fma(ir, fma(-qn[0], ir, 1.0), ir);
+      const double u = qn[1] * ir, vv = qn[2] * ir;
+      const double p = (qn[3] - 0.5 * (qn[1] * u + qn[2] * vv)) * G.g1;
+      primt[k] = mix::d2f(u);
+      primt[nc + k] = mix::d2f(vv);
+      primt[2 * nc + k] = mix::d2f((qn[3] + p) * ir);
+      primt[3 * nc + k] = sqrtf(fabsf(fr));
+      if (stage == 3) {
+        const float fu = mix::d2f(u), fv = mix::d2f(vv);
+        const float cs = sqrtf(fabsf(float(G.gamma) * mix::d2f(p) / fr));
+        ms = mix::f2d(fmaxf(fmaxf(fu - cs, fabsf(fu + cs)), fmaxf(fv - cs, fabsf(fv + cs))));
+      }
+      bad = (isnan(qn[0]) || isnan(qn[1]) || isnan(qn[2]) || isnan(qn[3]) || isnan(p)) ? 1 : 0;
+      bad |= (qn[0] <= 0.0 || p <= 0.0) ? 2 : 0;
+    } else {
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        // kinds: x-sweep (0 u, 1 v, 2 w), y-sweep (0 u, 1 w, 2 v)
+        const double ru = ((double(fx[(0 + e) * nxf + ox]) - double(fx[(0 + e) * nxf + ox + 1])) * G.dy +
+                           (double(fy[(0 + e) * nyf + oy]) - double(fy[(0 + e) * nyf + oy + G.nx])) * G.dx) / G.area + 0.0;
+        const double rv = ((double(fx[(4 + e) * nxf + ox]) - double(fx[(4 + e) * nxf + ox + 1])) * G.dy +
+                           (double(fy[(8 + e) * nyf + oy]) - double(fy[(8 + e) * nyf + oy + G.nx])) * G.dx) / G.area + 0.0;
+        const double rw = ((double(fx[(8 + e) * nxf + ox]) - double(fx[(8 + e) * nxf + ox + 1])) * G.dy +
+                           (double(fy[(4 + e) * nyf + oy]) - double(fy[(4 + e) * nyf + oy + G.nx])) * G.dx) / G.area + 0.0;
+        const size_t c = size_t(e) * nc + k;
+        double bq, bv, bw, cq = q[c], cv, cw;
+        if (stage == 1) {
+          bq = cq; bv = v[c]; bw = w[c];   // save() after the first rhs: limited moments
+          q0[c] = bq; v0[c] = bv; w0[c] = bw;
+          cv = bv; cw = bw;
+        } else {
+          bq = q0[c]; bv = v0[c]; bw = w0[c];
+          cv = vs[c]; cw = ws[c];          // unlimited stage values (cell.v1 / cell.v2)
+        }
+        qn[e] = ssprk3(bq, cq, ru, dt, stage);
+        const double nv = ssprk3(bv, cv, rv, dt, stage);
+        const double nw = ssprk3(bw, cw, rw, dt, stage);
+        q[c] = qn[e];
+        v[c] = nv;
+        vs[c] = nv;
+        w[c] = nw;
+        ws[c] = nw;
+      }
+      double u, vv, p, h, sr;
+      cell_prim(G.g1, qn, u, vv, p, h, sr);
+      prim[k] = u;
+      prim[nc + k] = vv;
+      prim[2 * nc + k] = h;
+      prim[3 * nc + k] = sr;
+      if (stage == 3) ms = cell_max_speed(G.gamma, qn[0], u, vv, p);
+      bad = (isnan(qn[0]) || isnan(qn[1]) || isnan(qn[2]) || isnan(qn[3])) ? 1 : 0;
+      bad |= (qn[0] <= 0.0 || p <= 0.0) ? 2 : 0;
     }
-    double u, vv, p, h, sr;
-    cell_prim(G.g1, qn, u, vv, p, h, sr);
-    prim[k] = u;
-    prim[nc + k] = vv;
-    prim[2 * nc + k] = h;
-    prim[3 * nc + k] = sr;
-    if (stage == 3) ms = cell_max_speed(G.gamma, qn[0], u, vv, p);
-    bad = (isnan(qn[0]) || isnan(qn[1]) || isnan(qn[2]) || isnan(qn[3])) ? 1 : 0;
-    bad |= (qn[0] <= 0.0 || p <= 0.0) ? 2 : 0;
   }
   if (stage == 3) block_max_to(ms, &st->maxbits);
   if (bad) atomicOr(&st->status, bad);
@@ -448,20 +749,28 @@ GeoH geo_of(const hteno_solver* s) {
   G.gamma = s->cfg.gamma;
   G.g1 = s->cfg.gamma - 1.0;
   G.g3 = s->cfg.gamma - 3.0;
+  G.rdx = 1.0 / s->dx;
+  G.rdy = 1.0 / s->dy;
   return G;
 }
 
 template <typename T>
 void launch_step(hteno_solver* s, const GeoH& G) {
   cudaStream_t cs = s->stream;
-  const WorkH<T> W = carve_h<T>(s->work, G.nx, G.ny);
+  WorkH<T> W = carve_h<T>(s->work, G.nx, G.ny);
+  if constexpr (std::is_same<T, double>::value) {
+    W.qt = s->q;
+    W.vt = s->v;
+    W.wt = s->w;
+    W.primt = W.prim;
+  }
   const HermiteK<T> K = make_hermite_k<T>(s->dx);  // setGridSize(dx) for both directions
   const int nx = G.nx, ny = G.ny;
   const long nxf = long(nx + 1) * ny, nyf = long(ny + 1) * nx;
   const size_t nc = size_t(nx) * ny;
   const double ncd = double(nc);
-  const int k_lx = trace_kind(s, "h_limit_x", ncd * 4 * 8 * 3, 0);
-  const int k_ly = trace_kind(s, "h_limit_y", ncd * 4 * 8 * 3, 0);
+  const int k_l = trace_kind(s, "h_limit", ncd * 4 * 8 * 6, 0);
+  const int nbx = 4 * ((ny + kLimLines - 1) / kLimLines), nby = 4 * ((nx + kLimLines - 1) / kLimLines);
   const int k_fx = trace_kind(s, "h_faces_x", ncd * 128 + double(nxf) * 31 * sizeof(T), 0);
   const int k_fy = trace_kind(s, "h_faces_y", ncd * 128 + double(nyf) * 31 * sizeof(T), 0);
   const int k_x = trace_kind(s, "h_flux_x", double(nxf) * 43 * sizeof(T), 0);
@@ -469,19 +778,20 @@ void launch_step(hteno_solver* s, const GeoH& G) {
   const int k_u = trace_kind(s, "h_update", ncd * 8 * 40 + double(nxf + nyf) * 12 * sizeof(T), 0);
   k_begin_step<<<1, 1, 0, cs>>>(s->dstate);
   for (int stage = 1; stage <= 3; ++stage) {
-    trace_begin(s, k_lx);
-    kh_limit<T, 1><<<unsigned((4 * ny + 63) / 64), 64, 0, cs>>>(G, K, s->q, s->v, s->dstate);
-    trace_end(s);
-    trace_begin(s, k_ly);
-    kh_limit<T, 2><<<unsigned((4 * nx + 63) / 64), 64, 0, cs>>>(G, K, s->q, s->w, s->dstate);
+    trace_begin(s, k_l);
+    if constexpr (std::is_same<T, float>::value)
+      kh_limit_f<<<unsigned(nbx + nby), kLimThreads, 0, cs>>>(G, K, s->q, s->v, s->w, W.vt, W.wt, nbx,
+                                                               s->dstate);
+    else
+      kh_limit<T><<<unsigned(nbx + nby), kLimThreads, 0, cs>>>(G, K, s->q, s->v, s->w, nbx, s->dstate);
     trace_end(s);
     trace_begin(s, k_fx);
     kh_faces<T, 1><<<unsigned((nxf + kHFaceThreads - 1) / kHFaceThreads), kHFaceThreads, 0, cs>>>(
-        G, K, s->q, s->v, s->w, W.prim, W.xc, W.xroe, s->dstate);
+        G, K, W.qt, W.vt, W.wt, W.primt, W.xc, W.xroe, s->dstate);
     trace_end(s);
     trace_begin(s, k_fy);
     kh_faces<T, 2><<<unsigned((nyf + kHFaceThreads - 1) / kHFaceThreads), kHFaceThreads, 0, cs>>>(
-        G, K, s->q, s->v, s->w, W.prim, W.yc, W.yroe, s->dstate);
+        G, K, W.qt, W.vt, W.wt, W.primt, W.yc, W.yroe, s->dstate);
     trace_end(s);
     trace_begin(s, k_x);
     kh_flux<T, 1><<<unsigned((nxf + kHFluxThreads - 1) / kHFluxThreads), kHFluxThreads, 0, cs>>>(
@@ -492,9 +802,14 @@ void launch_step(hteno_solver* s, const GeoH& G) {
         G, W.yc, W.yroe, W.fy, s->dstate);
     trace_end(s);
     trace_begin(s, k_u);
+    float *qtf = nullptr, *primtf = nullptr;
+    if constexpr (std::is_same<T, float>::value) {
+      qtf = W.qt;
+      primtf = W.primt;
+    }
     kh_update<T><<<unsigned((nc + 255) / 256), 256, 0, cs>>>(G, stage, W.fx, W.fy, s->q, s->q0,
                                                             s->v, s->v0, W.vs, s->w, s->w0, W.ws,
-                                                            W.prim, s->dstate);
+                                                            W.prim, qtf, primtf, s->dstate);
     trace_end(s);
   }
   k_end_step<<<1, 1, 0, cs>>>(s->dstate);

@@ -62,6 +62,24 @@ def test_hermite2d_matches_oracle_bitwise(hteno_lib, cuda, oracle):
         np.testing.assert_array_equal(a, b)
 
 
+def test_hermite2d_limiter_chunks_bitwise(hteno_lib, cuda, oracle):
+    """Lines longer than the limiter's shared-memory chunk (64 cells) and line counts that are not
+    multiples of its 32-line blocks: the chunked Gauss-Seidel sweep reproduces the oracle's."""
+    from hteno import ic
+
+    q = ic.gaussian_blobs_shock(150, 97, 4)
+    rng = np.random.default_rng(11)
+    v = np.ascontiguousarray(rng.normal(size=q.shape) * 0.2)
+    w = np.ascontiguousarray(rng.normal(size=q.shape) * 0.2)
+    qo, vo, wo, to, no = oracle.hermite2d_run(q, v, w, 3)
+    qg, vg, wg, tg, ng = run2(hteno_lib, q, v, w, 3)
+    assert ng == no and tg == to
+    for a, b in ((qg, qo), (vg, vo), (wg, wo)):
+        np.testing.assert_array_equal(a, b)
+    qm, _, _, _, _ = run2(hteno_lib, q, v, w, 3, precision=1)
+    assert np.abs(qm[0] - qo[0]).mean() <= 1e-4
+
+
 def test_hermite2d_mixed_precision_error(hteno_lib, cuda, oracle):
     from hteno import ic
 
