@@ -45,6 +45,41 @@ def four_quadrant(nx: int, ny: int, seed: int, gamma: float = 1.4):
     return np.ascontiguousarray(conservative2(w[..., 0], w[..., 1], w[..., 2], w[..., 3], gamma))
 
 
+def cell_centres(nx: int, ny: int, xl: float, xr: float, yb: float, yt: float):
+    """Cell centres as FV::System2D places them (FV_System2D.cpp:37-38): X, Y [ny][nx]."""
+    dx, dy = (xr - xl) / nx, (yt - yb) / ny
+    x = (np.arange(nx) + 0.5) * dx + xl
+    y = (np.arange(ny) + 0.5) * dy + yb
+    return np.meshgrid(x, y)
+
+
+def rayleigh_taylor(nx: int, ny: int, xl: float = 0.0, xr: float = 0.25, yb: float = 0.0,
+                    yt: float = 1.0, gamma: float = 1.4):
+    """conservativeOfTaylorIns2D (Equations_Euler2D.cpp:619-635) at the cell centres: density 2
+    below y = 0.5 and 1 above, hydrostatic-like pressure, a cos(8 pi x) vertical velocity
+    perturbation.  Boundary HTENO_BC_TAYLOR (TaylorInstBc) holds the bottom / top states."""
+    X, Y = cell_centres(nx, ny, xl, xr, yb, yt)
+    low = Y < 0.5
+    rho = np.where(low, 2.0, 1.0)
+    p = np.where(low, 1.0 + 2.0 * Y, Y + 1.5)
+    v = -0.025 * np.sqrt(gamma * p / rho) * np.cos(8.0 * (4.0 * np.arctan(1.0)) * X)
+    return np.ascontiguousarray(conservative2(rho, 0.0 * X, v, p, gamma))
+
+
+def double_mach(nx: int, ny: int, xl: float = 0.0, xr: float = 4.0, yb: float = 0.0,
+                yt: float = 1.0, gamma: float = 1.4):
+    """conservativeOfDoubleMach2D (Equations_Euler2D.cpp:637-655) at the cell centres: a Mach-10
+    shock at 60 degrees through x = 1/6 on the wall.  Boundary HTENO_BC_DOUBLE_MACH
+    (doubleMachBc)."""
+    X, Y = cell_centres(nx, ny, xl, xr, yb, yt)
+    post = X < 1.0 / 6.0 + Y / np.sqrt(3.0)
+    rho = np.where(post, 8.0, 1.4)
+    u = np.where(post, 8.25 * 0.5 * np.sqrt(3.0), 0.0)
+    v = np.where(post, -8.25 * 0.5, 0.0)
+    p = np.where(post, 116.5, 1.0)
+    return np.ascontiguousarray(conservative2(rho, u, v, p, gamma))
+
+
 def sod(nx: int, xl: float = 0.0, xr: float = 1.0, gamma: float = 1.4):
     """Conserved state [3][nx] of Sod's shock tube (sodShock, Equations_Euler1D.cpp:317-332)."""
     x = xl + (np.arange(nx) + 0.5) * (xr - xl) / nx

@@ -946,7 +946,7 @@ inline T ssprk3(T q0, T qn, T rhs, T dt, int stage) {
 // =============================================================================================
 // Solvers
 // =============================================================================================
-enum Bc { BC_ZEROGRAD = 0, BC_PERIODIC = 1 };
+enum Bc { BC_ZEROGRAD = 0, BC_PERIODIC = 1, BC_TAYLOR = 2, BC_DOUBLE_MACH = 3 };
 enum Flux { FLUX_RUSANOV = 0, FLUX_HLLC = 1 };
 enum Recon { RECON_TENO5 = 0, RECON_TENO5I = 1, RECON_LINEAR = 2 };
 
@@ -961,6 +961,10 @@ inline int bcmap(int i, int n, int bc) {
 struct FV2D {
   int nx, ny, bc, flux, recon;
   double dx, dy, area, cfl, gamma, t = 0.0, dt = 0.0;
+  double x0, y0;                                // xl, yb (cell centres for the ghost rules)
+  double qb[4], qu[4], qpost[4], qpre[4];       // fixed ghost states (TaylorInstBc, doubleMachBc)
+  double ctan, c16, s3;                         // tan(pi/6), 1/6, sqrt(3) as the reference computes them
+  std::vector<double> gxl, gxr, gyl, gyr;       // face values of the 2 + 2 ghost face rows [4][4][...]
   std::vector<double> q, q0, q1, rhsu;          // [4][ny][nx]
   std::vector<double> w, sr, h;                 // primitives [4][ny][nx], sqrt(rho), enthalpy
   std::vector<double> xl, xr, yl, yr;           // characteristic face values [4][...]
@@ -973,13 +977,70 @@ struct FV2D {
     dx = (xr0 - xl0) / nx;
     dy = (yt - yb) / ny;
     area = dx * dy;
+    x0 = xl0;
+    y0 = yb;
+    Euler2<double> E(gamma);
+    const double wb[4] = {2.0, 0.0, 0.0, 1.0}, wu[4] = {1.0, 0.0, 0.0, 2.5};  // :169-172
+    E.conservative(wb, qb);
+    E.conservative(wu, qu);
+    s3 = std::sqrt(3.0);
+    c16 = 1.0 / 6.0;
+    const double wpost[4] = {8.0, 8.25 * 0.5 * s3, -8.25 * 0.5, 116.5};  // Equations_Euler2D.cpp:637-655
+    const double wpre[4] = {1.4, 0.0, 0.0, 1.0};
+    E.conservative(wpost, qpost);
+    E.conservative(wpre, qpre);
+    const double pi = 4.0 * std::atan(1.0);  // doubleMachBc :189-190
+    ctan = std::tan(pi / 6.0);
     const size_t n = size_t(nx) * ny;
     q.assign(4 * n, 0.0); q0 = q; q1 = q; rhsu = q; w = q;
     sr.assign(n, 0.0); h = sr;
     const size_t nxf = size_t(nx + 1) * ny, nyf = size_t(nx) * (ny + 1);
     xl.assign(4 * nxf, 0.0); xr = xl; fx = xl; xR.assign(16 * nxf, 0.0); xL = xR;
     yl.assign(4 * nyf, 0.0); yr = yl; fy = yl; yR.assign(16 * nyf, 0.0); yL = yR;
+    gxl.assign(16 * size_t(nx + 1), 0.0); gxr = gxl;
+    gyl.assign(16 * size_t(ny + 1), 0.0); gyr = gyl;
   }
+
+  // State of cell (i, j), -6 <= i < nx + 6, -6 <= j < ny + 6, ghosts as the reference fills them.
+  // Zero-gradient and periodic ghosts copy interior cells (an index map).  TaylorInstBc
+  // (:154-182): x ghosts of interior rows mirror the row with the x momentum negated; the ghost
+  // rows (all columns) hold the fixed bottom / top states.  doubleMachBc (:184-224): below the
+  // first interior row, columns with x <= 1/6 hold conservativeOfDoubleMach2D at the ghost's
+  // centre and the others mirror the column with the y momentum negated; above the last row,
+  // the state of interior cell (0, 6) where x < 1/6 + tan(pi/6) (y + (1 + m) dy + 20 t) and of
+  // cell (nx - 7, 6) elsewhere; the x ghosts of every row copy the row's first / last column.
+  void ghost(int i, int j, double* out) const {
+    auto cp = [&](const double* src) { for (int v = 0; v < 4; ++v) out[v] = src[v]; };
+    auto ld = [&](int ii, int jj) { for (int v = 0; v < 4; ++v) out[v] = q[c(v, ii, jj)]; };
+    if (bc == BC_TAYLOR) {
+      if (j < 0) return cp(qb);
+      if (j >= ny) return cp(qu);
+      if (i < 0) { ld(-1 - i, j); out[1] = -out[1]; return; }
+      if (i >= nx) { ld(2 * nx - 1 - i, j); out[1] = -out[1]; return; }
+      return ld(i, j);
+    }
+    if (bc == BC_DOUBLE_MACH) {
+      const int ic = i < 0 ? 0 : (i >= nx ? nx - 1 : i);
+      if (j >= 0 && j < ny) return ld(ic, j);
+      const double x = ((double) (ic + 6) - 6.0 + 0.5) * dx + x0;
+      if (j < 0) {
+        if (x <= c16) {
+          const double y = ((double) (j + 6) - 6.0 + 0.5) * dy + y0;
+          const double lim = c16 + y / s3;
+          return cp(x < lim ? qpost : qpre);
+        }
+        ld(ic, -1 - j);
+        out[2] = -out[2];
+        return;
+      }
+      const int m = j - ny;
+      const double ytop = ((double) (ny + 6 - 1) - 6.0 + 0.5) * dy + y0;
+      const double hx = ctan * (ytop + (1.0 + (double) m) * dy + 20.0 * t) + c16;
+      return x < hx ? ld(0, 6) : ld(nx - 7, 6);
+    }
+    ld(bcmap(i, nx, bc), bcmap(j, ny, bc));
+  }
+  bool ghost_rows() const { return bc >= BC_TAYLOR; }
   size_t c(int v, int i, int j) const { return (size_t(v) * ny + j) * nx + i; }
   size_t cm(int v, int i, int j) const { return c(v, bcmap(i, nx, bc), bcmap(j, ny, bc)); }
   // x-face f in [0, nx] lies between cells f-1 and f of row j
@@ -1002,6 +1063,7 @@ struct FV2D {
   }
 
   void faces(int dir) {  // eigen2DEuler + the x/y characteristic sweeps (:265-400)
+    if (ghost_rows()) return faces_ghost(dir);
     Euler2<double> E(gamma);
     const int nf = dir == 1 ? nx + 1 : ny + 1, nt = dir == 1 ? ny : nx;
 #pragma omp parallel for
@@ -1039,6 +1101,63 @@ struct FV2D {
       }
   }
 
+  // The same for boundaries whose ghosts are not copies of interior cells: every state comes
+  // from ghost(), primitives of ghost cells are computed from their states (calcPrimitiveVariable
+  // covers the ghosts), and the face rows -2, -1, nt, nt + 1 that the transverse GL3 reads are
+  // computed too (the reference sweeps every row, :373-400), into gxl/gxr/gyl/gyr.
+  void faces_ghost(int dir) {
+    Euler2<double> E(gamma);
+    const int nf = dir == 1 ? nx + 1 : ny + 1, nt = dir == 1 ? ny : nx;
+#pragma omp parallel for
+    for (int t_ = -2; t_ < nt + 2; ++t_)
+      for (int f = 0; f < nf; ++f) {
+        auto st = [&](int s_, double* qq) { dir == 1 ? ghost(s_, t_, qq) : ghost(t_, s_, qq); };
+        auto pr = [&](int s_, double* ww, double& sr_, double& h_) {
+          double qq[4];
+          st(s_, qq);
+          E.primitive(qq, ww);
+          sr_ = std::sqrt(std::fabs(ww[0]));
+          h_ = (qq[3] + ww[3]) / ww[0];
+        };
+        double wa[4], wb[4], sra, srb, ha, hb, R[16], L[16];
+        pr(f - 1, wa, sra, ha);
+        pr(f, wb, srb, hb);
+        E.roe(dir, wa, sra, ha, wb, srb, hb, R, L);
+        double ch[4][6];
+        for (int m = 0; m < 6; ++m) {
+          double qq[4];
+          st(f - 3 + m, qq);
+          for (int r = 0; r < 4; ++r) {
+            double s = L[4 * r] * qq[0];
+            for (int k = 1; k < 4; ++k) s = s + L[4 * r + k] * qq[k];
+            ch[r][m] = s;
+          }
+        }
+        const bool interior = t_ >= 0 && t_ < nt;
+        const int gr = t_ < 0 ? t_ + 2 : t_ - nt + 2;  // ghost face row 0..3
+        for (int r = 0; r < 4; ++r) {
+          double o[2];
+          lagrange_recon(recon, ch[r], o);
+          if (interior) {
+            const size_t idx = dir == 1 ? xf(r, f, t_) : yf(r, t_, f);
+            (dir == 1 ? xl : yl)[idx] = o[0];
+            (dir == 1 ? xr : yr)[idx] = o[1];
+          } else {
+            const size_t idx = (size_t(gr) * 4 + r) * nf + f;
+            (dir == 1 ? gxl : gyl)[idx] = o[0];
+            (dir == 1 ? gxr : gyr)[idx] = o[1];
+          }
+        }
+        if (!interior) continue;
+        const size_t base = dir == 1 ? xf(0, f, t_) : yf(0, t_, f);
+        const size_t stride = dir == 1 ? size_t(ny) * (nx + 1) : size_t(ny + 1) * nx;
+        for (int k = 0; k < 16; ++k) {
+          (dir == 1 ? xR : yR)[base + k * stride] = R[k];
+          (dir == 1 ? xL : yL)[base + k * stride] = L[k];
+        }
+      }
+  }
+
   void fluxes(int dir) {  // transverse GL3 (:402-423), R back-projection (:425-430), flux (:432-497)
     Euler2<double> E(gamma);
     const int nf = dir == 1 ? nx + 1 : ny + 1, nt = dir == 1 ? ny : nx;
@@ -1054,7 +1173,15 @@ struct FV2D {
         for (int r = 0; r < 4; ++r) {
           double a[5], b[5];
           for (int m = 0; m < 5; ++m) {
-            const int tt = bcmap(t_ - 2 + m, ntr, bc);
+            const int tr = t_ - 2 + m;
+            if (ghost_rows() && (tr < 0 || tr >= ntr)) {
+              const int gr = tr < 0 ? tr + 2 : tr - ntr + 2;
+              const size_t idx = (size_t(gr) * 4 + r) * nf + f;
+              a[m] = (dir == 1 ? gxl : gyl)[idx];
+              b[m] = (dir == 1 ? gxr : gyr)[idx];
+              continue;
+            }
+            const int tt = bcmap(tr, ntr, bc);
             const size_t idx = dir == 1 ? xf(r, f, tt) : yf(r, tt, f);
             a[m] = FL[idx];
             b[m] = FR[idx];

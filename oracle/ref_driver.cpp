@@ -170,6 +170,14 @@ void ref_riemann2d_ic(double gamma, const double* x, const double* y, double* q,
   Equations::Euler2D E(gamma);
   for (long k = 0; k < n; ++k) put<4>(E.conservativeOfRiemann2D(x[k], y[k]), q + 4 * k);
 }
+void ref_taylor_ic(double gamma, const double* x, const double* y, double* q, long n) {
+  Equations::Euler2D E(gamma);
+  for (long k = 0; k < n; ++k) put<4>(E.conservativeOfTaylorIns2D(x[k], y[k]), q + 4 * k);
+}
+void ref_double_mach_ic(double gamma, const double* x, const double* y, double* q, long n) {
+  Equations::Euler2D E(gamma);
+  for (long k = 0; k < n; ++k) put<4>(E.conservativeOfDoubleMach2D(x[k], y[k]), q + 4 * k);
+}
 void ref_sod_ic(double gamma, const double* x, double* q, long n) {
   Equations::Euler1D E(gamma);
   for (long k = 0; k < n; ++k) put<3>(E.conservative(E.sodShock(x[k])), q + 3 * k);

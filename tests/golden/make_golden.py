@@ -6,7 +6,7 @@ through that library and stores inputs and outputs as compressed .npz files.  It
 reference tree (it runs where the reference is mounted) and is committed together with its
 outputs so the fixtures can be regenerated:
 
-    make -C oracle ref && python tests/golden/make_golden.py
+    make -C oracle ref ref_bc && python tests/golden/make_golden.py
 """
 from __future__ import annotations
 
@@ -169,6 +169,30 @@ def solvers():
     np.savez_compressed(HERE / "solvers.npz", **g)
 
 
+def boundaries():
+    """FV::System2D as shipped (TENO5, characteristic Rusanov) with rhs() calling TaylorInstBc()
+    resp. doubleMachBc() (oracle/Makefile target `ref_bc`), from the reference's own initial
+    data at the cell centres."""
+    g = {}
+    t = ctypes.c_double()
+    for name, lib, icfn, (nx, ny, xl, xr, yb, yt), steps in (
+            ("taylor", "libhteno_ref_taylor.so", "ref_taylor_ic", (16, 40, 0.0, 0.25, 0.0, 1.0), 20),
+            ("dmach", "libhteno_ref_dmach.so", "ref_double_mach_ic", (64, 16, 0.0, 4.0, 0.0, 1.0), 20)):
+        R = ctypes.CDLL(str(REPO / "oracle" / "_ref" / lib))
+        X, Y = ic.cell_centres(nx, ny, xl, xr, yb, yt)
+        x, y = np.ascontiguousarray(X.ravel()), np.ascontiguousarray(Y.ravel())
+        q = np.empty(4 * x.size)
+        getattr(R, icfn)(c(GAMMA), p(x), p(y), p(q), ctypes.c_long(x.size))
+        q = np.ascontiguousarray(q.reshape(ny, nx, 4).transpose(2, 0, 1))
+        out = np.empty_like(q)
+        R.ref_fv2d_run.restype = ctypes.c_int
+        n = R.ref_fv2d_run(nx, ny, c(xl), c(xr), c(yb), c(yt), c(0.4), c(GAMMA), c(1e30), steps,
+                           p(q), p(out), ctypes.byref(t))
+        g.update({f"{name}_q0": q, f"{name}_q": out, f"{name}_t": np.array(t.value),
+                  f"{name}_steps": np.array(n), f"{name}_box": np.array([xl, xr, yb, yt])})
+    np.savez_compressed(HERE / "boundaries.npz", **g)
+
+
 def alternatives(rng):
     """weno5JS, weno5Z, weno5N, teno5N, teno5a (Schemes_Lagrange.cpp:358-594, 1265-1294) on the
     same kinds of stencils as the pointwise fixtures."""
@@ -187,5 +211,6 @@ if __name__ == "__main__":
     pointwise(np.random.default_rng(20261203))
     solvers()
     alternatives(np.random.default_rng(20261204))
+    boundaries()
     for f in sorted(HERE.glob("*.npz")):
         print(f.name, f.stat().st_size)

@@ -80,6 +80,24 @@ def test_fv2d_golden(oracle, sv):
     same(np.array(t), sv["fv2d_t"])
 
 
+@pytest.mark.parametrize("name,bc", [("taylor", 2), ("dmach", 3)])
+def test_fv2d_boundaries_golden(oracle, name, bc):
+    """TaylorInstBc and doubleMachBc (reflective walls, fixed and time-dependent ghost states):
+    the oracle against the reference with rhs() switched to those routines, and the project's
+    initial data against the reference's."""
+    from hteno import ic
+
+    g = np.load(GOLD / "boundaries.npz")
+    q0 = g[f"{name}_q0"]
+    xl, xr, yb, yt = g[f"{name}_box"]
+    fn = ic.rayleigh_taylor if name == "taylor" else ic.double_mach
+    np.testing.assert_allclose(fn(q0.shape[2], q0.shape[1]), q0, rtol=1e-15, atol=1e-15)
+    q, t, n = oracle.fv2d_run(q0, int(g[f"{name}_steps"]), xl=xl, xr=xr, yb=yb, yt=yt, bc=bc)
+    assert n == int(g[f"{name}_steps"])
+    same(q, g[f"{name}_q"])
+    same(np.array(t), g[f"{name}_t"])
+
+
 def test_fv1d_golden(oracle, sv):
     q, t, n = oracle.fv1d_run(sv["fv1d_q0"], 100000, t_final=0.2, cfl=0.5, recon=1, flux=0)
     assert n == int(sv["fv1d_steps"])
