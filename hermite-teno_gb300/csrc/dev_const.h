@@ -28,4 +28,10 @@ struct DevConst {
 
 void fill_dev_const(DevConst* c);  // host side, device_consts.cpp
 
+// Fixed states and constants of the TaylorInstBc / doubleMachBc ghost rules (FV_System2D.cpp:
+// 154-224), computed on the host as the reference computes them: q[0] bottom and q[1] top state
+// of TaylorInstBc, q[2] post-shock and q[3] pre-shock state of conservativeOfDoubleMach2D; tan(pi/6)
+// with pi = 4 atan(1); 1/6; sqrt(3).  host side, device_consts.cpp
+void fill_bc_consts(double gamma, double q[4][4], double* ctan, double* c16, double* s3);
+
 }  // namespace hteno

@@ -32,6 +32,25 @@ void to_float(const double (&a)[N], float (&b)[N]) {
 }
 }  // namespace
 
+void fill_bc_consts(double gamma, double q[4][4], double* ctan, double* c16, double* s3) {
+  // Euler2D::conservative (Equations_Euler2D.cpp:28-34)
+  const double g1 = gamma - 1.0;
+  auto cons = [&](double r, double u, double v, double p, double* o) {
+    o[0] = r;
+    o[1] = r * u;
+    o[2] = r * v;
+    o[3] = p / g1 + 0.5 * (o[1] * u + o[2] * v);
+  };
+  cons(2.0, 0.0, 0.0, 1.0, q[0]);  // TaylorInstBc wb, wu (:169-172)
+  cons(1.0, 0.0, 0.0, 2.5, q[1]);
+  *s3 = std::sqrt(3.0);
+  cons(8.0, 8.25 * 0.5 * *s3, -8.25 * 0.5, 116.5, q[2]);  // conservativeOfDoubleMach2D (:637-655)
+  cons(1.4, 0.0, 0.0, 1.0, q[3]);
+  *c16 = 1.0 / 6.0;
+  const double pi = 4.0 * std::atan(1.0);  // doubleMachBc (:189-190)
+  *ctan = std::tan(pi / 6.0);
+}
+
 void fill_dev_const(DevConst* c) {
   const double sq15 = std::sqrt(15.0);
   // crjgp3L / crjgm3L (Schemes_Lagrange.cpp:65-83)

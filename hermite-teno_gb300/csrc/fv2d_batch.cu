@@ -271,7 +271,8 @@ int hteno_batch_create(const hteno_config* cfgs, int n, hteno_batch** out) {
       return HTENO_ERR_UNSUPPORTED;
     if (c.nx < 6 || c.ny < 6 || (long long)c.nx * c.ny > (1ll << 30) || !(c.xr > c.xl) ||
         !(c.yt > c.yb) || !(c.cfl > 0.0) || !(c.gamma > 1.0) || c.recon < 0 || c.recon > 7 ||
-        c.flux < 0 || c.flux > 1 || c.bc < 0 || c.bc > 1)
+        c.flux < 0 || c.flux > 1 || c.bc < 0 || c.bc > 3 ||
+        (c.bc >= HTENO_BC_TAYLOR && (c.nx < 7 || c.ny < 7)))
       return HTENO_ERR_INVALID_ARG;
   }
   hteno_batch* b = new (std::nothrow) hteno_batch();
@@ -315,6 +316,10 @@ int hteno_batch_create(const hteno_config* cfgs, int n, hteno_batch** out) {
     I.G.area = I.G.dx * I.G.dy;
     I.G.gamma = c.gamma;
     I.G.g1 = c.gamma - 1.0;
+    I.G.x0 = c.xl;
+    I.G.y0 = c.yb;
+    I.G.t0 = c.t_init;
+    fill_bc_consts(c.gamma, I.G.bq, &I.G.ctan, &I.G.c16, &I.G.s3);
     const size_t bytes = (4 * b->ncell[i] * sizeof(double) + 255) & ~size_t(255);
     char* base = reinterpret_cast<char*>(b->pool) + off[i];
     I.q = reinterpret_cast<double*>(base);

@@ -9,7 +9,78 @@ namespace hteno {
 struct Geo {
   int nx, ny, bc, recon, flux;
   double dx, dy, area, gamma, g1;
+  // boundaries whose ghosts are not copies of interior cells (HTENO_BC_TAYLOR, _DOUBLE_MACH)
+  double x0, y0;        // xl, yb: cell centres
+  double t0;            // time of a residual evaluation (the stepping kernels read the step state)
+  double bq[4][4];      // fixed ghost states (fill_bc_consts)
+  double ctan, c16, s3;
 };
+
+// State of cell (i, j) with the ghosts FV::System2D fills (6 layers; further cells read as the
+// outermost ghost)
+// (FV_System2D.cpp:114-224).  Zero-gradient and periodic ghosts copy interior cells.
+// TaylorInstBc (:154-182): x ghosts of interior rows mirror the row with the x momentum negated;
+// the ghost rows of every column hold the fixed bottom / top states.  doubleMachBc (:184-224):
+// below the first row, columns with x <= 1/6 hold conservativeOfDoubleMach2D at the ghost's
+// centre, the others mirror the column with the y momentum negated; above the last row, the
+// state of interior cell (0, 6) where x < 1/6 + tan(pi/6) (y_top + (1 + m) dy + 20 t), of cell
+// (nx - 7, 6) elsewhere (m = j - ny); the x ghosts of every row copy its first / last column.
+// Positions are computed with explicitly rounded operations, as the reference's expressions
+// round them, in any translation unit.
+__device__ __forceinline__ void bc_state(const Geo& G, const double* __restrict__ q, int i, int j,
+                                         double t, double* out) {
+  const size_t nc = size_t(G.nx) * G.ny;
+  auto ld = [&](int ii, int jj) {
+    const size_t k = size_t(jj) * G.nx + ii;
+#pragma unroll
+    for (int v = 0; v < 4; ++v) out[v] = q[v * nc + k];
+  };
+  auto cp = [&](const double* s) {
+#pragma unroll
+    for (int v = 0; v < 4; ++v) out[v] = s[v];
+  };
+  if (G.bc >= HTENO_BC_TAYLOR) {  // cells past the ghost layers (tiles overhanging the grid)
+    i = min(max(i, -6), G.nx + 5);
+    j = min(max(j, -6), G.ny + 5);
+  }
+  if (G.bc == HTENO_BC_TAYLOR) {
+    if (j < 0) return cp(G.bq[0]);
+    if (j >= G.ny) return cp(G.bq[1]);
+    if (i < 0) { ld(-1 - i, j); out[1] = -out[1]; return; }
+    if (i >= G.nx) { ld(2 * G.nx - 1 - i, j); out[1] = -out[1]; return; }
+    return ld(i, j);
+  }
+  if (G.bc == HTENO_BC_DOUBLE_MACH) {
+    const int ic = min(max(i, 0), G.nx - 1);
+    if (j >= 0 && j < G.ny) return ld(ic, j);
+    const double x = __dadd_rn(__dmul_rn(__dadd_rn(__dsub_rn(double(ic + 6), 6.0), 0.5), G.dx), G.x0);
+    if (j < 0) {
+      if (x <= G.c16) {
+        const double y = __dadd_rn(__dmul_rn(__dadd_rn(__dsub_rn(double(j + 6), 6.0), 0.5), G.dy), G.y0);
+        return cp(x < __dadd_rn(G.c16, __ddiv_rn(y, G.s3)) ? G.bq[2] : G.bq[3]);
+      }
+      ld(ic, -1 - j);
+      out[2] = -out[2];
+      return;
+    }
+    const double ytop = __dadd_rn(__dmul_rn(__dadd_rn(__dsub_rn(double(G.ny + 5), 6.0), 0.5), G.dy), G.y0);
+    const double span = __dadd_rn(__dadd_rn(ytop, __dmul_rn(__dadd_rn(1.0, double(j - G.ny)), G.dy)),
+                                  __dmul_rn(20.0, t));
+    const double hx = __dadd_rn(__dmul_rn(G.ctan, span), G.c16);
+    return x < hx ? ld(0, 6) : ld(G.nx - 7, 6);
+  }
+  int ii = i, jj = j;
+  if (G.bc == HTENO_BC_PERIODIC) {
+    ii %= G.nx;
+    ii = ii < 0 ? ii + G.nx : ii;
+    jj %= G.ny;
+    jj = jj < 0 ? jj + G.ny : jj;
+  } else {
+    ii = min(max(ii, 0), G.nx - 1);
+    jj = min(max(jj, 0), G.ny - 1);
+  }
+  ld(ii, jj);
+}
 
 // Work buffer: primitives (double) and per-face intermediates (compute type T).
 template <typename T>
@@ -70,6 +141,10 @@ inline Geo geo_of(const hteno_solver* s) {
   G.area = s->dx * s->dy;
   G.gamma = s->cfg.gamma;
   G.g1 = s->cfg.gamma - 1.0;
+  G.x0 = s->cfg.xl;
+  G.y0 = s->cfg.yb;
+  G.t0 = s->hstate ? s->hstate->t : 0.0;
+  fill_bc_consts(s->cfg.gamma, G.bq, &G.ctan, &G.c16, &G.s3);
   return G;
 }
 

@@ -69,12 +69,20 @@ __global__ void __launch_bounds__(256) kp_deep(Geo G, const double* __restrict__
   __shared__ unsigned long long key[4][H][W];
   const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY;
   const size_t nc = size_t(G.nx) * G.ny;
+  const bool ghosts = G.bc >= HTENO_BC_TAYLOR;  // ghosts that are not copies: compare their states
+  const double t = st ? st->t : G.t0;
   for (int it = threadIdx.x; it < W * H; it += blockDim.x) {
     const int y = it / W, x = it - y * W;
-    const size_t k = size_t(cmap_any(j0 - 3 + y, G.ny, G.bc)) * G.nx + cmap_any(i0 - 3 + x, G.nx, G.bc);
+    double qq[4];
+    if (ghosts) {
+      bc_state(G, q, i0 - 3 + x, j0 - 3 + y, t, qq);
+    } else {
+      const size_t k = size_t(cmap_any(j0 - 3 + y, G.ny, G.bc)) * G.nx + cmap_any(i0 - 3 + x, G.nx, G.bc);
 #pragma unroll
-    for (int v = 0; v < 4; ++v)
-      key[v][y][x] = static_cast<unsigned long long>(__double_as_longlong(q[v * nc + k]));
+      for (int v = 0; v < 4; ++v) qq[v] = q[v * nc + k];
+    }
+#pragma unroll
+    for (int v = 0; v < 4; ++v) key[v][y][x] = static_cast<unsigned long long>(__double_as_longlong(qq[v]));
   }
   __syncthreads();
   const int tx = threadIdx.x % TX, ty = threadIdx.x / TX;
@@ -206,12 +214,95 @@ __global__ void __launch_bounds__(kFaceThreads) kp_harvest(Geo G, const double* 
   }
 }
 
+// kp_faces for boundaries whose ghosts are not copies of interior cells (HTENO_BC_TAYLOR,
+// _DOUBLE_MACH): every state comes from bc_state(), the primitives of the two Roe cells are
+// computed from their states (calcPrimitiveVariable covers the ghosts, :231-262), and the face
+// rows -2, -1, nt, nt + 1 that the transverse GL3 reads are computed too (the reference sweeps
+// every row, :373-400), into gfc [4 rows][8][nf].
+template <int DIR>
+__global__ void __launch_bounds__(kFaceThreads) kp_faces_g(Geo G, const double* __restrict__ q,
+                                                           double* __restrict__ fc,
+                                                           double* __restrict__ froe,
+                                                           double* __restrict__ gfc,
+                                                           const StepState* st,
+                                                           const uint8_t* __restrict__ deep) {
+  if (st && st->done) return;
+  const int nf = DIR == 1 ? G.nx + 1 : G.ny + 1;
+  const int nt = DIR == 1 ? G.ny : G.nx;
+  const long idx = blockIdx.x * long(blockDim.x) + threadIdx.x;
+  if (idx >= long(nf) * (nt + 4)) return;
+  int f, t;
+  if (DIR == 1) { f = int(idx % nf); t = int(idx / nf) - 2; }
+  else { t = int(idx % (nt + 4)) - 2; f = int(idx / (nt + 4)); }
+  const int ns = DIR == 1 ? G.nx : G.ny;
+  if (deep) {
+    // the fluxes that read this face value are those of faces (f, t + m), |m| <= 2, of the
+    // interior rows; skipped when every one of them is (both of its cells deep)
+    const int a = min(max(f - 1, 0), ns - 1), b = min(max(f, 0), ns - 1);
+    bool skip = true;
+#pragma unroll
+    for (int m = -2; m <= 2; ++m) {
+      const int tt = t + m;
+      if (tt < 0 || tt >= nt) continue;
+      const size_t ka = DIR == 1 ? size_t(tt) * G.nx + a : size_t(a) * G.nx + tt;
+      const size_t kb = DIR == 1 ? size_t(tt) * G.nx + b : size_t(b) * G.nx + tt;
+      skip = skip && deep[ka] && deep[kb];
+    }
+    if (skip) return;
+  }
+  const double tm = st ? st->t : G.t0;
+  auto state = [&](int s, double* o) {
+    if (DIR == 1) bc_state(G, q, s, t, tm, o);
+    else bc_state(G, q, t, s, tm, o);
+  };
+  double qa[4], qb[4], wa[4], wb[4], ha, hb, sra, srb;
+  state(f - 1, qa);
+  state(f, qb);
+  cell_prim(G.g1, qa, wa, ha, sra);
+  cell_prim(G.g1, qb, wb, hb, srb);
+  const par::Eig E = par::eig(G.g1, DIR, sra, wa[1], wa[2], ha, srb, wb[1], wb[2], hb);
+  double ch[4][6];
+#pragma unroll
+  for (int m = 0; m < 6; ++m) {
+    double qq[4], cc[4];
+    state(f - 3 + m, qq);
+    par::left(E, DIR, qq, cc);
+#pragma unroll
+    for (int r = 0; r < 4; ++r) ch[r][m] = cc[r];
+  }
+  const bool interior = t >= 0 && t < nt;
+  const size_t nface = size_t(nf) * nt;
+  const size_t o = DIR == 1 ? size_t(t) * nf + f : size_t(f) * nt + t;
+  const size_t go = size_t(t < 0 ? t + 2 : t - nt + 2) * 8 * nf + f;
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    double va, vb;
+    par::lagrange_recon(c_dev, G.recon, ch[r], va, vb);
+    if (interior) {
+      fc[r * nface + o] = va;
+      fc[(4 + r) * nface + o] = vb;
+    } else {
+      gfc[go + r * nf] = va;
+      gfc[go + (4 + r) * nf] = vb;
+    }
+  }
+  if (!interior) return;
+  froe[0 * nface + o] = E.vxm;
+  froe[1 * nface + o] = E.vym;
+  froe[2 * nface + o] = E.hm;
+  froe[3 * nface + o] = E.qm;
+  froe[4 * nface + o] = E.cm;
+  froe[5 * nface + o] = E.rcm;
+  froe[6 * nface + o] = E.b1;
+}
+
 template <int DIR>
 __global__ void __launch_bounds__(kFaceThreads) kp_flux(Geo G, const double* __restrict__ fc,
                                                         const double* __restrict__ froe,
                                                         double* __restrict__ F,
                                                         const StepState* st,
-                                                        const uint8_t* __restrict__ deep = nullptr) {
+                                                        const uint8_t* __restrict__ deep = nullptr,
+                                                        const double* __restrict__ gfc = nullptr) {
   if (st && st->done) return;
   const int nf = DIR == 1 ? G.nx + 1 : G.ny + 1;
   const int nt = DIR == 1 ? G.ny : G.nx;
@@ -239,7 +330,13 @@ __global__ void __launch_bounds__(kFaceThreads) kp_flux(Geo G, const double* __r
   for (int r = 0; r < 8; ++r) {
     double u5[5];
 #pragma unroll
-    for (int m = 0; m < 5; ++m) u5[m] = fc[r * nface + nb[m]];
+    for (int m = 0; m < 5; ++m) {
+      const int tr = t - 2 + m;
+      if (gfc && (tr < 0 || tr >= nt))  // a face row of the ghosts (kp_faces_g)
+        u5[m] = gfc[(size_t(tr < 0 ? tr + 2 : tr - nt + 2) * 8 + r) * nf + f];
+      else
+        u5[m] = fc[r * nface + nb[m]];
+    }
     par::gl3(c_dev, u5, g[r]);
   }
   const size_t o = nb[2];
@@ -339,6 +436,11 @@ int fv2d_fp64_setup(hteno_solver* s) {
     const cudaError_t e = cudaMalloc(&s->deep, size_t(s->cfg.nx) * s->cfg.ny);
     if (e != cudaSuccess) return cuda_error(s, e, "uniform-region flags");
   }
+  if (s->cfg.precision == HTENO_PREC_FP64 && s->cfg.bc >= HTENO_BC_TAYLOR && !s->ghost_faces) {
+    const size_t n = size_t(32) * (s->cfg.nx + 1) + size_t(32) * (s->cfg.ny + 1);
+    const cudaError_t e = cudaMalloc(&s->ghost_faces, n * sizeof(double));
+    if (e != cudaSuccess) return cuda_error(s, e, "ghost face rows");
+  }
   return HTENO_OK;
 }
 
@@ -369,21 +471,36 @@ void fv2d_fp64_stage(hteno_solver* s, const Geo& G, const Work<double>& W, int s
     kp_deep<<<dim3(unsigned((nx + 31) / 32), unsigned((ny + 7) / 8)), 256, 0, cs>>>(G, q, s->deep, st);
     trace_end(s);
   }
+  // ghost face rows of the x faces ([4][8][nx + 1]) and of the y faces ([4][8][ny + 1])
+  double* gx = s->ghost_faces;
+  double* gy = gx ? gx + size_t(32) * (nx + 1) : nullptr;
   trace_begin(s, kf_x);
-  kp_faces<1><<<unsigned((nxf + kFaceThreads - 1) / kFaceThreads), kFaceThreads, 0, cs>>>(
-      G, q, W.prim, W.xc, W.xroe, st, deep);
+  if (gx) {
+    const long n = long(nx + 1) * (ny + 4);
+    kp_faces_g<1><<<unsigned((n + kFaceThreads - 1) / kFaceThreads), kFaceThreads, 0, cs>>>(
+        G, q, W.xc, W.xroe, gx, st, deep);
+  } else {
+    kp_faces<1><<<unsigned((nxf + kFaceThreads - 1) / kFaceThreads), kFaceThreads, 0, cs>>>(
+        G, q, W.prim, W.xc, W.xroe, st, deep);
+  }
   trace_end(s);
   trace_begin(s, kf_y);
-  kp_faces<2><<<unsigned((nyf + kFaceThreads - 1) / kFaceThreads), kFaceThreads, 0, cs>>>(
-      G, q, W.prim, W.yc, W.yroe, st, deep);
+  if (gy) {
+    const long n = long(ny + 1) * (nx + 4);
+    kp_faces_g<2><<<unsigned((n + kFaceThreads - 1) / kFaceThreads), kFaceThreads, 0, cs>>>(
+        G, q, W.yc, W.yroe, gy, st, deep);
+  } else {
+    kp_faces<2><<<unsigned((nyf + kFaceThreads - 1) / kFaceThreads), kFaceThreads, 0, cs>>>(
+        G, q, W.prim, W.yc, W.yroe, st, deep);
+  }
   trace_end(s);
   trace_begin(s, kx);
   kp_flux<1><<<unsigned((nxf + kFaceThreads - 1) / kFaceThreads), kFaceThreads, 0, cs>>>(
-      G, W.xc, W.xroe, W.fx, st, deep);
+      G, W.xc, W.xroe, W.fx, st, deep, gx);
   trace_end(s);
   trace_begin(s, ky);
   kp_flux<2><<<unsigned((nyf + kFaceThreads - 1) / kFaceThreads), kFaceThreads, 0, cs>>>(
-      G, W.yc, W.yroe, W.fy, st, deep);
+      G, W.yc, W.yroe, W.fy, st, deep, gy);
   trace_end(s);
   const size_t nc = size_t(nx) * ny;
   trace_begin(s, ku);

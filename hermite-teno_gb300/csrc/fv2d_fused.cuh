@@ -178,13 +178,27 @@ __device__ __forceinline__ double tile_stage(const DevConst& C, const Geo& G, in
     const int side = tid / 24, pat = (tid % 24) / 3, k = tid % 3;
     S.wtab[side][pat][k] = side ? C.f_wtab_p[pat][k] : C.f_wtab_m[pat][k];
   }
-  // A: state and primitives of the tile and its halo
+  // A: state and primitives of the tile and its halo (ghosts as the boundary routine fills them)
+  const bool ghosts = G.bc >= HTENO_BC_TAYLOR;
+  const double tm = a.st ? a.st->t : G.t0;
   for (int it = tid; it < Sh::W * Sh::H; it += NT) {
     const int y = it / Sh::W, x = it - y * Sh::W;
-    const int gi = cmap(i0 - 3 + x, G.nx, G.bc), gj = cmap(j0 - 3 + y, G.ny, G.bc);
-    const size_t k = size_t(gj) * G.nx + gi;
-    const float r = d2f(__ldg(a.qin + k)), mx = d2f(__ldg(a.qin + nc + k));
-    const float my = d2f(__ldg(a.qin + 2 * nc + k)), e = d2f(__ldg(a.qin + 3 * nc + k));
+    float r, mx, my, e;
+    if (ghosts) {
+      double qq[4];
+      bc_state(G, a.qin, i0 - 3 + x, j0 - 3 + y, tm, qq);
+      r = d2f(qq[0]);
+      mx = d2f(qq[1]);
+      my = d2f(qq[2]);
+      e = d2f(qq[3]);
+    } else {
+      const int gi = cmap(i0 - 3 + x, G.nx, G.bc), gj = cmap(j0 - 3 + y, G.ny, G.bc);
+      const size_t k = size_t(gj) * G.nx + gi;
+      r = d2f(__ldg(a.qin + k));
+      mx = d2f(__ldg(a.qin + nc + k));
+      my = d2f(__ldg(a.qin + 2 * nc + k));
+      e = d2f(__ldg(a.qin + 3 * nc + k));
+    }
     S.q[0][y][x] = r;
     S.q[1][y][x] = mx;
     S.q[2][y][x] = my;

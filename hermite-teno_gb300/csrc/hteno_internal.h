@@ -71,6 +71,7 @@ struct hteno_solver {
   int tile_variant = -1;  // mixed FV 2D: tile shape picked by the tuner (-1: not yet)
   uint8_t* deep = nullptr;  // plain FV 2D: cells of uniform 7 x 7 neighbourhoods (per stage)
   bool uniform_skip = true;  // FV 2D: uniform regions take their exactly zero residual directly
+  double* ghost_faces = nullptr;  // plain FV 2D with HTENO_BC_TAYLOR / _DOUBLE_MACH: ghost face rows
   // learned routing (mixed FV 2D): classifier, threshold, audit period, masks, audit sums
   hteno_mlp* router = nullptr;
   float router_thr = 0.9f;

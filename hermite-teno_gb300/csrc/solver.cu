@@ -107,6 +107,7 @@ void release(hteno_solver* s) {
   cudaFree(s->audit);
   cudaFree(s->route_rows);
   cudaFree(s->deep);
+  cudaFree(s->ghost_faces);
   cudaFree(s->route_info);
   cudaFree(s->q);
   cudaFree(s->q0);
@@ -175,7 +176,11 @@ int hteno_create(const hteno_config* cfg, hteno_solver** out) {
     return HTENO_ERR_INVALID_ARG;
   if (!(c.xr > c.xl) || (c.dims == 2 && !(c.yt > c.yb))) return HTENO_ERR_INVALID_ARG;
   if (!(c.cfl > 0.0) || !(c.gamma > 1.0)) return HTENO_ERR_INVALID_ARG;
-  if (c.recon < 0 || c.recon > 7 || c.flux < 0 || c.flux > 1 || c.bc < 0 || c.bc > 1 ||
+  if (c.bc >= HTENO_BC_TAYLOR && c.bc <= HTENO_BC_DOUBLE_MACH &&
+      (c.dims != 2 || c.scheme != HTENO_SCHEME_FV))
+    return HTENO_ERR_UNSUPPORTED;  // the reference's other solvers have no such routines wired
+  if (c.bc >= HTENO_BC_TAYLOR && (c.nx < 7 || c.ny < 7)) return HTENO_ERR_INVALID_ARG;
+  if (c.recon < 0 || c.recon > 7 || c.flux < 0 || c.flux > 1 || c.bc < 0 || c.bc > 3 ||
       c.precision < 0 || c.precision > 1)
     return HTENO_ERR_INVALID_ARG;
 

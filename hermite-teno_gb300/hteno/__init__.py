@@ -23,7 +23,7 @@ SCHEME_FV, SCHEME_HERMITE = 0, 1
 RECON_TENO5, RECON_TENO5I, RECON_LINEAR = 0, 1, 2
 RECON_WENO5JS, RECON_WENO5Z, RECON_WENO5N, RECON_TENO5N, RECON_TENO5A = 3, 4, 5, 6, 7
 FLUX_RUSANOV, FLUX_HLLC = 0, 1
-BC_ZEROGRAD, BC_PERIODIC = 0, 1
+BC_ZEROGRAD, BC_PERIODIC, BC_TAYLOR, BC_DOUBLE_MACH = 0, 1, 2, 3
 PREC_FP64, PREC_MIXED = 0, 1
 
 STATUS = {0: "ok", 1: "invalid argument", 2: "out of device memory", 3: "CUDA error",

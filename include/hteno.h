@@ -53,7 +53,20 @@ typedef enum {
 } hteno_recon;
 
 typedef enum { HTENO_FLUX_RUSANOV = 0, HTENO_FLUX_HLLC = 1 } hteno_flux;
-typedef enum { HTENO_BC_ZEROGRAD = 0, HTENO_BC_PERIODIC = 1 } hteno_bc;
+/* Boundaries: zeroGradBc and periodicBc (FV_System2D.cpp:114-152), and for the FV 2D scheme the
+ * two routines the reference ships beside them in rhs() (:366-368):
+ * HTENO_BC_TAYLOR = TaylorInstBc (:154-182): reflective side walls (x momentum mirrored), fixed
+ *   bottom state (rho, u, v, p) = (2, 0, 0, 1) and top state (1, 0, 0, 2.5) -- the Rayleigh-Taylor
+ *   setup on [0, 0.25] x [0, 1];
+ * HTENO_BC_DOUBLE_MACH = doubleMachBc (:184-224): the double Mach reflection on [0, 4] x [0, 1]
+ *   (post-shock inflow below x <= 1/6, reflective wall beyond it, time-dependent top boundary
+ *   following the Mach-10 shock, zero-gradient sides).  Needs nx, ny >= 7. */
+typedef enum {
+  HTENO_BC_ZEROGRAD = 0,
+  HTENO_BC_PERIODIC = 1,
+  HTENO_BC_TAYLOR = 2,
+  HTENO_BC_DOUBLE_MACH = 3
+} hteno_bc;
 
 /* HTENO_PREC_FP64: everything in double (the plain method).
  * HTENO_PREC_MIXED: reconstruction, smoothness indicators and fluxes in float; RK stage

@@ -45,6 +45,18 @@ def test_invalid_configs_rejected_without_device(hteno_lib):
         assert not handle.value
 
 
+def test_boundary_routines_limited_to_fv2d(hteno_lib):
+    """TaylorInstBc / doubleMachBc exist for FV::System2D only, and read interior cells 6 away
+    from the walls."""
+    h = hteno_lib
+    for kw, want in ((dict(bc=h.BC_TAYLOR, dims=1), 7), (dict(bc=h.BC_DOUBLE_MACH, scheme=h.SCHEME_HERMITE), 7),
+                     (dict(bc=h.BC_DOUBLE_MACH, nx=6), 1), (dict(bc=h.BC_TAYLOR, ny=6), 1)):
+        cfg = h.config(**kw)
+        handle = ctypes.c_void_p()
+        assert h.lib().hteno_create(ctypes.byref(cfg), ctypes.byref(handle)) == want, kw
+        assert not handle.value
+
+
 def test_batch_entry_points_validate_arguments(hteno_lib):
     lib = hteno_lib.lib()
     # negative counts and bad directions are rejected before any launch

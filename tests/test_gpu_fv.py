@@ -163,6 +163,40 @@ def test_fv2d_uniform_regions_exact(hteno_lib, cuda, oracle, case):
     np.testing.assert_array_equal(got, want)
 
 
+@pytest.mark.parametrize("name,bc", [("taylor", 2), ("dmach", 3)])
+def test_fv2d_boundaries_match_reference_golden(hteno_lib, cuda, name, bc):
+    """TaylorInstBc and doubleMachBc (reflective walls, fixed and time-dependent ghost states),
+    against the reference with rhs() switched to those routines (scheme as shipped)."""
+    g = np.load(GOLD / "boundaries.npz")
+    q0 = g[f"{name}_q0"]
+    xl, xr, yb, yt = g[f"{name}_box"]
+    got, t, n = gpu_run2d(hteno_lib, q0, int(g[f"{name}_steps"]), xl=xl, xr=xr, yb=yb, yt=yt, bc=bc)
+    assert n == int(g[f"{name}_steps"]) and t == float(g[f"{name}_t"])
+    np.testing.assert_array_equal(got, g[f"{name}_q"])
+
+
+BOUNDARY_CASES = {
+    "rayleigh-taylor-hllc": (2, "rayleigh_taylor", (40, 150), (0.0, 0.25, 0.0, 1.0), 60, dict(flux=1)),
+    "double-mach-hllc": (3, "double_mach", (160, 41), (0.0, 4.0, 0.0, 1.0), 60, dict(flux=1)),
+    "double-mach-teno5i": (3, "double_mach", (97, 30), (0.0, 4.0, 0.0, 1.0), 40, dict(flux=0, recon=1)),
+}
+
+
+@pytest.mark.parametrize("case", list(BOUNDARY_CASES))
+def test_fv2d_boundaries_match_oracle(hteno_lib, cuda, oracle, case):
+    """The benchmark scheme (HLLC) and teno5i with the two boundary routines: bit for bit against
+    the oracle, on grids that are not multiples of any tile; the uniform-region skipping (on by
+    default) is exact with the ghost states too."""
+    from hteno import ic
+
+    bc, fn, (nx, ny), (xl, xr, yb, yt), steps, kw = BOUNDARY_CASES[case]
+    q = getattr(ic, fn)(nx, ny, xl, xr, yb, yt)
+    want, t_o, n_o = oracle.fv2d_run(q, steps, xl=xl, xr=xr, yb=yb, yt=yt, bc=bc, **kw)
+    got, t_g, n_g = gpu_run2d(hteno_lib, q, steps, xl=xl, xr=xr, yb=yb, yt=yt, bc=bc, **kw)
+    assert n_g == n_o == steps and t_g == t_o
+    np.testing.assert_array_equal(got, want)
+
+
 def test_fv2d_constant_state_is_steady(hteno_lib, cuda):
     q = np.ascontiguousarray(np.broadcast_to(np.array([1.3, 0.2, -0.4, 2.7])[:, None, None], (4, 16, 20)).copy())
     got, _, _ = gpu_run2d(hteno_lib, q, 5, flux=1)

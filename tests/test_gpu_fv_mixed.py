@@ -137,6 +137,35 @@ def test_mixed_uniform_tiles_exact(hteno_lib, cuda, case):
     np.testing.assert_array_equal(got, full)
 
 
+@pytest.mark.parametrize("bc,fn,shape,box", [
+    (2, "rayleigh_taylor", (40, 150), (0.0, 0.25, 0.0, 1.0)),
+    (3, "double_mach", (160, 41), (0.0, 4.0, 0.0, 1.0))])
+def test_mixed_boundaries(hteno_lib, cuda, bc, fn, shape, box):
+    """TaylorInstBc / doubleMachBc on the mixed path: close to FP64 at the same time, the same
+    bits with and without the uniform-tile skipping, and a batch of the grid reproduces it."""
+    from hteno import ic
+
+    xl, xr, yb, yt = box
+    q = getattr(ic, fn)(*shape, xl, xr, yb, yt)
+    kw = dict(flux=1, bc=bc, xl=xl, xr=xr, yb=yb, yt=yt)
+    ref, t_ref, _, _ = run(hteno_lib, q, 40, **kw)
+    got, t_got, _, st = run(hteno_lib, q, 1000, t_final=t_ref, precision=1, **kw)
+    assert t_got == pytest.approx(t_ref, rel=1e-14, abs=0) and st == 0
+    assert np.abs(got[0] - ref[0]).mean() <= 1e-3 * np.abs(ref[0]).mean()
+    try:
+        os.environ["HTENO_UNIFORM_SKIP"] = "0"
+        full, _, _, _ = run(hteno_lib, q, 1000, t_final=t_ref, precision=1, **kw)
+    finally:
+        os.environ.pop("HTENO_UNIFORM_SKIP", None)
+    np.testing.assert_array_equal(got, full)
+    cfg = hteno_lib.config(dims=2, nx=shape[0], ny=shape[1], precision=1, **kw)
+    with hteno_lib.Batch([cfg]) as b:
+        b.set_state(0, q)
+        b.step(10)
+        single, _, _, _ = run(hteno_lib, q, 10, precision=1, **kw)
+        np.testing.assert_array_equal(b.get_state(0), single)
+
+
 def test_mixed_periodic_conservation(hteno_lib, cuda):
     q = periodic_box(128, 96)
     got, _, _, _ = run(hteno_lib, q, 60, flux=1, bc=1, precision=1)
