@@ -60,6 +60,7 @@ def parse():
     ap.add_argument("--no-hermite", action="store_true")
     ap.add_argument("--no-sod", action="store_true")
     ap.add_argument("--hermite-steps", type=int, default=10)
+    ap.add_argument("--hermite-n", type=int, default=2048, help="grid side of the Hermite 2D path")
     ap.add_argument("--no-learned", action="store_true")
     ap.add_argument("--c5-steps", type=int, default=20)
     ap.add_argument("--c5-fp64-steps", type=int, default=3)
@@ -582,7 +583,8 @@ def run_gpu(args):
     if not args.no_sod and rank == 0:
         paths["sod_1d_400"] = sod_path(hteno, torch)
     if not args.no_hermite:
-        paths["hermite_2048"] = hermite_path(hteno, torch, stream, args.hermite_steps, 3, world)
+        paths[f"hermite_{args.hermite_n}"] = hermite_path(hteno, torch, stream, args.hermite_steps, 3, world,
+                                                           n=args.hermite_n)
     if not args.no_learned:
         paths["learned_4096"] = learned_path(hteno, torch, stream, args, world)
     if not args.no_batch:
