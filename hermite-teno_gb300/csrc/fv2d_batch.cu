@@ -32,8 +32,8 @@ struct BInst {
 };
 
 // One launch per stage over every tile of every instance: block b takes jobs b, b + grid, ...
-template <int TX, int TY, int NT>
-__global__ void __launch_bounds__(NT) k_batch_stage(const BInst* __restrict__ inst,
+template <int TX, int TY, int NT, int MINB>
+__global__ void __launch_bounds__(NT, MINB) k_batch_stage(const BInst* __restrict__ inst,
                                                     const int4* __restrict__ jobs, int njobs,
                                                     int stage) {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -111,27 +111,31 @@ struct BVariant {
   cudaError_t (*prepare)(int* blocks_per_sm);
 };
 
-template <int TX, int TY, int NT>
+template <int TX, int TY, int NT, int MINB>
 void blaunch(cudaStream_t cs, int grid, const BInst* inst, const int4* jobs, int njobs, int stage) {
-  k_batch_stage<TX, TY, NT><<<grid, NT, fused::smem_bytes<TX, TY>(), cs>>>(inst, jobs, njobs, stage);
+  k_batch_stage<TX, TY, NT, MINB><<<grid, NT, fused::smem_bytes<TX, TY>(), cs>>>(inst, jobs, njobs, stage);
 }
 
-template <int TX, int TY, int NT>
+template <int TX, int TY, int NT, int MINB>
 cudaError_t bprepare(int* blocks_per_sm) {
-  cudaError_t e = cudaFuncSetAttribute(k_batch_stage<TX, TY, NT>,
+  cudaError_t e = cudaFuncSetAttribute(k_batch_stage<TX, TY, NT, MINB>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        int(fused::smem_bytes<TX, TY>()));
   if (e != cudaSuccess) return e;
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_batch_stage<TX, TY, NT>, NT,
-                                                       fused::smem_bytes<TX, TY>());
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_batch_stage<TX, TY, NT, MINB>,
+                                                       NT, fused::smem_bytes<TX, TY>());
 }
 
-#define HTENO_BVARIANT(TX, TY, NT) \
-  { TX, TY, NT, fused::smem_bytes<TX, TY>(), "batch_" #TX "x" #TY "_" #NT, blaunch<TX, TY, NT>, bprepare<TX, TY, NT> }
+// MINB > 1 would set the register budget of MINB blocks per SM.  None is listed: with reduced
+// budgets the compiler contracted some float expressions of this kernel differently, and every
+// candidate must give the same bits (the tuner's choice must not change results).
+#define HTENO_BVARIANT(TX, TY, NT, MINB)                                                          \
+  { TX, TY, NT, fused::smem_bytes<TX, TY>(), "batch_" #TX "x" #TY "_" #NT "_b" #MINB,              \
+    blaunch<TX, TY, NT, MINB>, bprepare<TX, TY, NT, MINB> }
 
 const BVariant kBVariants[] = {
-    HTENO_BVARIANT(32, 16, 256), HTENO_BVARIANT(32, 8, 256),  HTENO_BVARIANT(16, 16, 256),
-    HTENO_BVARIANT(64, 8, 256),  HTENO_BVARIANT(32, 32, 512), HTENO_BVARIANT(16, 8, 128),
+    HTENO_BVARIANT(32, 16, 256, 1), HTENO_BVARIANT(32, 8, 256, 1),  HTENO_BVARIANT(16, 16, 256, 1),
+    HTENO_BVARIANT(64, 8, 256, 1),  HTENO_BVARIANT(32, 32, 512, 1), HTENO_BVARIANT(16, 8, 128, 1),
 };
 constexpr int kNumBVariants = sizeof(kBVariants) / sizeof(kBVariants[0]);
 

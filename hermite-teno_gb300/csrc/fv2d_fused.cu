@@ -14,8 +14,12 @@ std::mutex g_mu;
 
 #include "common_kernels.cuh"
 
-template <int TX, int TY, int NT>
-__global__ void __launch_bounds__(NT) k_fused(Geo G, int stage, fused::StageArgs a) {
+// MINB > 1 asks the compiler to fit MINB blocks per SM in registers (more warps to hide latency,
+// at the price of a few spills); the tuner keeps whichever shape and register budget runs
+// fastest.  Every variant must give the same bits (tested): budgets of 64 registers (MINB = 4 at
+// 256 threads) did not -- the compiler contracted some float expressions differently there.
+template <int TX, int TY, int NT, int MINB>
+__global__ void __launch_bounds__(NT, MINB) k_fused(Geo G, int stage, fused::StageArgs a) {
   if (a.st && a.st->done) return;
   extern __shared__ __align__(16) unsigned char smem[];
   auto& S = *reinterpret_cast<fused::Smem<TX, TY>*>(smem);
@@ -50,24 +54,26 @@ struct Variant {
   cudaError_t (*prepare)();
 };
 
-template <int TX, int TY, int NT>
+template <int TX, int TY, int NT, int MINB>
 void launch_v(cudaStream_t cs, const Geo& G, int stage, const fused::StageArgs& a) {
   const dim3 grid(unsigned((G.nx + TX - 1) / TX), unsigned((G.ny + TY - 1) / TY));
-  k_fused<TX, TY, NT><<<grid, NT, fused::smem_bytes<TX, TY>(), cs>>>(G, stage, a);
+  k_fused<TX, TY, NT, MINB><<<grid, NT, fused::smem_bytes<TX, TY>(), cs>>>(G, stage, a);
 }
 
-template <int TX, int TY, int NT>
+template <int TX, int TY, int NT, int MINB>
 cudaError_t prepare_v() {
-  return cudaFuncSetAttribute(k_fused<TX, TY, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  return cudaFuncSetAttribute(k_fused<TX, TY, NT, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                               int(fused::smem_bytes<TX, TY>()));
 }
 
-#define HTENO_VARIANT(TX, TY, NT) \
-  { TX, TY, NT, fused::smem_bytes<TX, TY>(), "fused_" #TX "x" #TY "_" #NT, launch_v<TX, TY, NT>, prepare_v<TX, TY, NT> }
+#define HTENO_VARIANT(TX, TY, NT, MINB)                                                           \
+  { TX, TY, NT, fused::smem_bytes<TX, TY>(), "fused_" #TX "x" #TY "_" #NT "_b" #MINB,               \
+    launch_v<TX, TY, NT, MINB>, prepare_v<TX, TY, NT, MINB> }
 
 const Variant kVariants[] = {
-    HTENO_VARIANT(32, 16, 256), HTENO_VARIANT(32, 8, 256),  HTENO_VARIANT(16, 16, 256),
-    HTENO_VARIANT(64, 8, 256),  HTENO_VARIANT(32, 32, 512), HTENO_VARIANT(16, 8, 128),
+    HTENO_VARIANT(32, 16, 256, 1), HTENO_VARIANT(32, 8, 256, 1),  HTENO_VARIANT(16, 16, 256, 1),
+    HTENO_VARIANT(64, 8, 256, 1),  HTENO_VARIANT(32, 32, 512, 1), HTENO_VARIANT(16, 8, 128, 1),
+    HTENO_VARIANT(32, 16, 256, 3), HTENO_VARIANT(64, 8, 256, 3),
 };
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 

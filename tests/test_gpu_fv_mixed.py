@@ -77,17 +77,19 @@ def test_mixed_smooth_flow_is_accurate(hteno_lib, cuda):
     assert np.abs(got - ref).max() <= 1e-5
 
 
-def test_mixed_tile_shapes_agree_bitwise(hteno_lib, cuda):
+@pytest.mark.parametrize("kw", [dict(flux=1), dict(flux=0, recon=1), dict(flux=1, recon=5, bc=1)],
+                         ids=["hllc-teno5", "rusanov-teno5i", "hllc-weno5n-periodic"])
+def test_mixed_tile_shapes_agree_bitwise(hteno_lib, cuda, kw):
     """Every tile shape computes each face from the same data with the same arithmetic, so the
     results are identical; the grid is not a multiple of any tile."""
     from hteno import ic
 
-    q = ic.four_quadrant(70, 45, 5)
+    q = ic.four_quadrant(70, 45, 5) if kw.get("bc", 0) == 0 else periodic_box(70, 45)
     outs = []
     try:
-        for v in range(6):
+        for v in range(8):  # every tile shape and register budget of the tuner
             os.environ["HTENO_FV2D_TILE"] = str(v)
-            outs.append(run(hteno_lib, q, 12, flux=1, precision=1)[0])
+            outs.append(run(hteno_lib, q, 12, precision=1, **kw)[0])
     finally:
         os.environ.pop("HTENO_FV2D_TILE", None)
     for o in outs[1:]:
