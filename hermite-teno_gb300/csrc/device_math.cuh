@@ -72,6 +72,20 @@ template <> struct Cst<float> {
   __device__ static float sqrt_(float x) { return sqrtf(x); }
 };
 
+// a * b + c: an explicit fused multiply-add in float (so every instantiation rounds alike even
+// where the compiler is not allowed to contract); for double the unfused expression, which
+// rounds as written where contraction is off.
+template <typename T>
+__device__ __forceinline__ T mad(T a, T b, T c) {
+  if constexpr (sizeof(T) == 4) return fmaf(a, b, c);
+  else return a * b + c;
+}
+// x0 y0 + x1 y1 + x2 y2, summed left to right
+template <typename T>
+__device__ __forceinline__ T dot3m(T x0, T y0, T x1, T y1, T x2, T y2) {
+  return mad(x2, y2, mad(x1, y1, x0 * y0));
+}
+
 template <typename T>
 __device__ __forceinline__ T catchnan(T x) {  // Schemes_Lagrange.cpp:1151-1153
   return isnan(x) ? T(HTENO_MACHINE_EPS) : x;
@@ -100,24 +114,24 @@ __device__ __forceinline__ int teno_pattern(T r0, T r1, T r2, T ct) {
 // smoothnessMeasure (:1013-1026) + optional fullpointsSmootness (:1029-1034)
 template <typename T>
 __device__ __forceinline__ void lagrange_si(const T* v, T& SI0, T& SI1, T& SI2) {
-  T c0 = v[2] - T(2.0) * v[3] + v[4];
-  T b0 = (T(3.0) * v[2] - T(4.0) * v[3] + v[4]) * T(0.5);
-  T c1 = v[1] - T(2.0) * v[2] + v[3];
+  T c0 = mad(T(-2.0), v[3], v[2]) + v[4];
+  T b0 = (mad(T(-4.0), v[3], T(3.0) * v[2]) + v[4]) * T(0.5);
+  T c1 = mad(T(-2.0), v[2], v[1]) + v[3];
   T b1 = (v[1] - v[3]) * T(0.5);
-  T c2 = v[0] - T(2.0) * v[1] + v[2];
-  T b2 = (v[0] - T(4.0) * v[1] + T(3.0) * v[2]) * T(0.5);
-  SI0 = b0 * b0 + T(HTENO_C1) * c0 * c0;
-  SI1 = b1 * b1 + T(HTENO_C1) * c1 * c1;
-  SI2 = b2 * b2 + T(HTENO_C1) * c2 * c2;
+  T c2 = mad(T(-2.0), v[1], v[0]) + v[2];
+  T b2 = mad(T(3.0), v[2], mad(T(-4.0), v[1], v[0])) * T(0.5);
+  SI0 = mad(T(HTENO_C1) * c0, c0, b0 * b0);
+  SI1 = mad(T(HTENO_C1) * c1, c1, b1 * b1);
+  SI2 = mad(T(HTENO_C1) * c2, c2, b2 * b2);
 }
 template <typename T>
 __device__ __forceinline__ T lagrange_b35(const T* v) {
-  T r = v[4] * (T(6908.0) * v[4] - T(51001.0) * v[3] + T(67923.0) * v[2] - T(38947.0) * v[1] +
-                T(8209.0) * v[0]) +
-        v[3] * (T(104963.0) * v[3] - T(299076.0) * v[2] + T(179098.0) * v[1] -
-                T(38947.0) * v[0]) +
-        v[2] * (T(231153.0) * v[2] - T(299076.0) * v[1] + T(67923.0) * v[0]) +
-        v[1] * (T(104963.0) * v[1] - T(51001.0) * v[0]) + T(6908.0) * v[0] * v[0];
+  const T a4 = mad(T(8209.0), v[0], mad(T(-38947.0), v[1], mad(T(67923.0), v[2],
+                  mad(T(-51001.0), v[3], T(6908.0) * v[4]))));
+  const T a3 = mad(T(-38947.0), v[0], mad(T(179098.0), v[1], mad(T(-299076.0), v[2], T(104963.0) * v[3])));
+  const T a2 = mad(T(67923.0), v[0], mad(T(-299076.0), v[1], T(231153.0) * v[2]));
+  const T a1 = mad(T(-51001.0), v[0], T(104963.0) * v[1]);
+  const T r = mad(T(6908.0) * v[0], v[0], mad(v[1], a1, mad(v[2], a2, mad(v[3], a3, v[4] * a4))));
   return r * T(1.0 / 5040.0);
 }
 
@@ -134,12 +148,12 @@ __device__ __forceinline__ T teno_side(const DevConst& C, T p0, T p1, T p2, cons
     tau = fmax(fmax(SI0, SI1), SI2);
   }
   const T ez = Cst<T>::epsz();
-  T r0 = T(1.0) + tau * Cst<T>::rcp(SI0 + ez);
-  T r1 = T(1.0) + tau * Cst<T>::rcp(SI1 + ez);
-  T r2 = T(1.0) + tau * Cst<T>::rcp(SI2 + ez);
+  T r0 = mad(tau, Cst<T>::rcp(SI0 + ez), T(1.0));
+  T r1 = mad(tau, Cst<T>::rcp(SI1 + ez), T(1.0));
+  T r2 = mad(tau, Cst<T>::rcp(SI2 + ez), T(1.0));
   int pat = teno_pattern(r0, r1, r2, T(HTENO_LAG_CT));
   const T* w = Cst<T>::wtab(C, side, pat);
-  return catchnan(p0 * w[0] + p1 * w[1] + p2 * w[2]);
+  return catchnan(dot3m(p0, w[0], p1, w[1], p2, w[2]));
 }
 
 // The selectable alternatives (Schemes_Lagrange.cpp:358-594, 1265-1294), one side, compute type
@@ -196,23 +210,23 @@ template <typename T>
 __device__ __forceinline__ void lagrange_recon(const DevConst& C, int kind, const T* u, T& outm,
                                                T& outp) {
   typedef Cst<T> K;
-  T p0 = K::crj(C, 0, 1) * u[2] + K::crj(C, 1, 1) * u[3] + K::crj(C, 2, 1) * u[4];
-  T p1 = K::crj(C, 0, 2) * u[1] + K::crj(C, 1, 2) * u[2] + K::crj(C, 2, 2) * u[3];
-  T p2 = K::crj(C, 0, 3) * u[0] + K::crj(C, 1, 3) * u[1] + K::crj(C, 2, 3) * u[2];
+  T p0 = dot3m(K::crj(C, 0, 1), u[2], K::crj(C, 1, 1), u[3], K::crj(C, 2, 1), u[4]);
+  T p1 = dot3m(K::crj(C, 0, 2), u[1], K::crj(C, 1, 2), u[2], K::crj(C, 2, 2), u[3]);
+  T p2 = dot3m(K::crj(C, 0, 3), u[0], K::crj(C, 1, 3), u[1], K::crj(C, 2, 3), u[2]);
   if (kind == 2) {
     const T* w = K::wtab(C, 0, 7);
-    outm = p0 * w[0] + p1 * w[1] + p2 * w[2];
+    outm = dot3m(p0, w[0], p1, w[1], p2, w[2]);
   } else if (kind >= 3) {
     outm = alt_side(kind, p0, p1, p2, u, reinterpret_cast<const T(*)[3]>(K::wtab(C, 0, 0)), K::wtab(C, 0, 7));
   } else {
     outm = teno_side(C, p0, p1, p2, u, 0, kind == 1);
   }
-  p0 = K::crj(C, 0, 0) * u[3] + K::crj(C, 1, 0) * u[4] + K::crj(C, 2, 0) * u[5];
-  p1 = K::crj(C, 0, 1) * u[2] + K::crj(C, 1, 1) * u[3] + K::crj(C, 2, 1) * u[4];
-  p2 = K::crj(C, 0, 2) * u[1] + K::crj(C, 1, 2) * u[2] + K::crj(C, 2, 2) * u[3];
+  p0 = dot3m(K::crj(C, 0, 0), u[3], K::crj(C, 1, 0), u[4], K::crj(C, 2, 0), u[5]);
+  p1 = dot3m(K::crj(C, 0, 1), u[2], K::crj(C, 1, 1), u[3], K::crj(C, 2, 1), u[4]);
+  p2 = dot3m(K::crj(C, 0, 2), u[1], K::crj(C, 1, 2), u[2], K::crj(C, 2, 2), u[3]);
   if (kind == 2) {
     const T* w = K::wtab(C, 1, 7);
-    outp = p0 * w[0] + p1 * w[1] + p2 * w[2];
+    outp = dot3m(p0, w[0], p1, w[1], p2, w[2]);
   } else if (kind >= 3) {
     outp = alt_side(kind, p0, p1, p2, u + 1, reinterpret_cast<const T(*)[3]>(K::wtab(C, 1, 0)),
                     K::wtab(C, 1, 7));
@@ -227,15 +241,15 @@ __device__ __forceinline__ void lagrange_recon(const DevConst& C, int kind, cons
 template <typename T>
 __device__ __forceinline__ void gl3(const DevConst& C, const T* u, T& o0, T& o1, T& o2) {
   typedef Cst<T> K;
-  T bg0 = u[0] - T(4.0) * u[1] + T(3.0) * u[2];
-  T cg0 = u[0] - T(2.0) * u[1] + u[2];
+  T bg0 = mad(T(3.0), u[2], mad(T(-4.0), u[1], u[0]));
+  T cg0 = mad(T(-2.0), u[1], u[0]) + u[2];
   T bg1 = u[1] - u[3];
-  T cg1 = u[1] - T(2.0) * u[2] + u[3];
-  T bg2 = T(3.0) * u[2] - T(4.0) * u[3] + u[4];
-  T cg2 = u[2] - T(2.0) * u[3] + u[4];
-  T s0 = T(HTENO_LAG_EPS) + (T(0.25) * bg0 * bg0 + T(HTENO_C1) * cg0 * cg0);
-  T s1 = T(HTENO_LAG_EPS) + (T(0.25) * bg1 * bg1 + T(HTENO_C1) * cg1 * cg1);
-  T s2 = T(HTENO_LAG_EPS) + (T(0.25) * bg2 * bg2 + T(HTENO_C1) * cg2 * cg2);
+  T cg1 = mad(T(-2.0), u[2], u[1]) + u[3];
+  T bg2 = mad(T(-4.0), u[3], T(3.0) * u[2]) + u[4];
+  T cg2 = mad(T(-2.0), u[3], u[2]) + u[4];
+  T s0 = T(HTENO_LAG_EPS) + mad(T(HTENO_C1) * cg0, cg0, T(0.25) * bg0 * bg0);
+  T s1 = T(HTENO_LAG_EPS) + mad(T(HTENO_C1) * cg1, cg1, T(0.25) * bg1 * bg1);
+  T s2 = T(HTENO_LAG_EPS) + mad(T(HTENO_C1) * cg2, cg2, T(0.25) * bg2 * bg2);
   s0 = s0 * s0; s1 = s1 * s1; s2 = s2 * s2;
   // alpha_k = 1 / s_k, scaled by the smallest s to keep float in range
   T smin = fmin(fmin(s0, s1), s2);
@@ -243,27 +257,27 @@ __device__ __forceinline__ void gl3(const DevConst& C, const T* u, T& o0, T& o1,
 
   const T* lw = K::linwp(C);
   T g0 = lw[0] * a0, g1 = lw[1] * a1, g2 = lw[2] * a2;
-  T q0 = K::gp(C, 0, 0) * u[0] + K::gp(C, 1, 0) * u[1] + K::gp(C, 2, 0) * u[2];
-  T q1 = K::gp(C, 0, 1) * u[1] + K::gp(C, 1, 1) * u[2] + K::gp(C, 2, 1) * u[3];
-  T q2 = K::gp(C, 0, 2) * u[2] + K::gp(C, 1, 2) * u[3] + K::gp(C, 2, 2) * u[4];
-  o0 = catchnan((q0 * g0 + q1 * g1 + q2 * g2) * K::rcp(g0 + g1 + g2));
+  T q0 = dot3m(K::gp(C, 0, 0), u[0], K::gp(C, 1, 0), u[1], K::gp(C, 2, 0), u[2]);
+  T q1 = dot3m(K::gp(C, 0, 1), u[1], K::gp(C, 1, 1), u[2], K::gp(C, 2, 1), u[3]);
+  T q2 = dot3m(K::gp(C, 0, 2), u[2], K::gp(C, 1, 2), u[3], K::gp(C, 2, 2), u[4]);
+  o0 = catchnan(dot3m(q0, g0, q1, g1, q2, g2) * K::rcp(g0 + g1 + g2));
 
-  q0 = (-u[0] + T(2.0) * u[1] + T(23.0) * u[2]) * T(1.0 / 24.0);
-  q1 = (-u[1] + T(26.0) * u[2] - u[3]) * T(1.0 / 24.0);
-  q2 = (T(23.0) * u[2] + T(2.0) * u[3] - u[4]) * T(1.0 / 24.0);
+  q0 = mad(T(23.0), u[2], mad(T(2.0), u[1], -u[0])) * T(1.0 / 24.0);
+  q1 = (mad(T(26.0), u[2], -u[1]) - u[3]) * T(1.0 / 24.0);
+  q2 = (mad(T(2.0), u[3], T(23.0) * u[2]) - u[4]) * T(1.0 / 24.0);
   lw = K::linw0p(C);
   g0 = lw[0] * a0; g1 = lw[1] * a1; g2 = lw[2] * a2;
-  T c = K::sumw0p(C) * ((q0 * g0 + q1 * g1 + q2 * g2) * K::rcp(g0 + g1 + g2));
+  T c = K::sumw0p(C) * (dot3m(q0, g0, q1, g1, q2, g2) * K::rcp(g0 + g1 + g2));
   lw = K::linw0m(C);
   g0 = lw[0] * a0; g1 = lw[1] * a1; g2 = lw[2] * a2;
-  o1 = catchnan(c - K::sumw0m(C) * ((q0 * g0 + q1 * g1 + q2 * g2) * K::rcp(g0 + g1 + g2)));
+  o1 = catchnan(c - K::sumw0m(C) * (dot3m(q0, g0, q1, g1, q2, g2) * K::rcp(g0 + g1 + g2)));
 
   lw = K::linwm(C);
   g0 = lw[0] * a0; g1 = lw[1] * a1; g2 = lw[2] * a2;
-  q0 = K::gm(C, 0, 0) * u[0] + K::gm(C, 1, 0) * u[1] + K::gm(C, 2, 0) * u[2];
-  q1 = K::gm(C, 0, 1) * u[1] + K::gm(C, 1, 1) * u[2] + K::gm(C, 2, 1) * u[3];
-  q2 = K::gm(C, 0, 2) * u[2] + K::gm(C, 1, 2) * u[3] + K::gm(C, 2, 2) * u[4];
-  o2 = catchnan((q0 * g0 + q1 * g1 + q2 * g2) * K::rcp(g0 + g1 + g2));
+  q0 = dot3m(K::gm(C, 0, 0), u[0], K::gm(C, 1, 0), u[1], K::gm(C, 2, 0), u[2]);
+  q1 = dot3m(K::gm(C, 0, 1), u[1], K::gm(C, 1, 1), u[2], K::gm(C, 2, 1), u[3]);
+  q2 = dot3m(K::gm(C, 0, 2), u[2], K::gm(C, 1, 2), u[3], K::gm(C, 2, 2), u[4]);
+  o2 = catchnan(dot3m(q0, g0, q1, g1, q2, g2) * K::rcp(g0 + g1 + g2));
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -283,10 +297,10 @@ __device__ __forceinline__ Roe2<T> roe2(T g1, T ra, T ua, T va, T ha, T rb, T ub
   Roe2<T> s;
   T t0 = ra / (ra + rb);
   T t1 = T(1.0) - t0;
-  s.vxm = t0 * ua + t1 * ub;
-  s.vym = t0 * va + t1 * vb;
-  s.hm = t0 * ha + t1 * hb;
-  s.qm = T(0.5) * (s.vxm * s.vxm + s.vym * s.vym);
+  s.vxm = mad(t1, ub, t0 * ua);
+  s.vym = mad(t1, vb, t0 * va);
+  s.hm = mad(t1, hb, t0 * ha);
+  s.qm = T(0.5) * mad(s.vym, s.vym, s.vxm * s.vxm);
   s.cm = Cst<T>::sqrt_(fabs(g1 * (s.hm - s.qm)));
   s.rcm = T(1.0) / s.cm;
   s.b1 = g1 * s.rcm * s.rcm;
@@ -300,10 +314,10 @@ __device__ __forceinline__ void roe_left(const Roe2<T>& s, int dir, const T* q, 
   const T b2 = s.qm * s.b1, s0 = vn * s.rcm, s1 = s.b1 * vn, t2 = T(0.5) * s.b1;
   const T qn = dir == 1 ? q[1] : q[2], qt = dir == 1 ? q[2] : q[1];
   // row 0: 0.5(b2 + s0), -0.5(s1 + rcm) [normal], -t2 vt [tangential], t2
-  c[0] = T(0.5) * (b2 + s0) * q[0] + T(-0.5) * (s1 + s.rcm) * qn + (-t2 * vt) * qt + t2 * q[3];
-  c[1] = -vt * q[0] + qt;
-  c[2] = (T(1.0) - b2) * q[0] + s1 * qn + (s.b1 * vt) * qt + (-s.b1) * q[3];
-  c[3] = T(0.5) * (b2 - s0) * q[0] + T(-0.5) * (s1 - s.rcm) * qn + (-t2 * vt) * qt + t2 * q[3];
+  c[0] = mad(t2, q[3], mad(-t2 * vt, qt, mad(T(-0.5) * (s1 + s.rcm), qn, T(0.5) * (b2 + s0) * q[0])));
+  c[1] = mad(-vt, q[0], qt);
+  c[2] = mad(-s.b1, q[3], mad(s.b1 * vt, qt, mad(s1, qn, (T(1.0) - b2) * q[0])));
+  c[3] = mad(t2, q[3], mad(-t2 * vt, qt, mad(T(-0.5) * (s1 - s.rcm), qn, T(0.5) * (b2 - s0) * q[0])));
 }
 // R * c (rightEigenVectorx/y)
 template <typename T>
@@ -311,11 +325,11 @@ __device__ __forceinline__ void roe_right(const Roe2<T>& s, int dir, const T* c,
   const T vn = dir == 1 ? s.vxm : s.vym, vt = dir == 1 ? s.vym : s.vxm;
   const T t0 = vn * s.cm;
   q[0] = c[0] + c[2] + c[3];
-  const T qn = (vn - s.cm) * c[0] + vn * c[2] + (vn + s.cm) * c[3];
-  const T qt = vt * c[0] + c[1] + vt * c[2] + vt * c[3];
+  const T qn = mad(vn + s.cm, c[3], mad(vn, c[2], (vn - s.cm) * c[0]));
+  const T qt = mad(vt, c[3], mad(vt, c[2], mad(vt, c[0], c[1])));
   q[dir == 1 ? 1 : 2] = qn;
   q[dir == 1 ? 2 : 1] = qt;
-  q[3] = (s.hm - t0) * c[0] + vt * c[1] + s.qm * c[2] + (s.hm + t0) * c[3];
+  q[3] = mad(s.hm + t0, c[3], mad(s.qm, c[2], mad(vt, c[1], (s.hm - t0) * c[0])));
 }
 
 template <typename T>
@@ -324,20 +338,20 @@ __device__ __forceinline__ void primitive2(T g1, const T* q, T* w) {  // Euler2D
   w[0] = q[0];
   w[1] = q[1] * ir;
   w[2] = q[2] * ir;
-  w[3] = (q[3] - T(0.5) * (q[1] * w[1] + q[2] * w[2])) * g1;
+  w[3] = (q[3] - T(0.5) * mad(q[2], w[2], q[1] * w[1])) * g1;
 }
 
 template <typename T>
 __device__ __forceinline__ void flux2(int dir, const T* q, const T* w, T* f) {  // fluxx/fluxy
   if (dir == 1) {
     f[0] = q[1];
-    f[1] = q[1] * w[1] + w[3];
+    f[1] = mad(q[1], w[1], w[3]);
     f[2] = q[1] * w[2];
     f[3] = w[1] * (q[3] + w[3]);
   } else {
     f[0] = q[2];
     f[1] = q[2] * w[1];
-    f[2] = q[2] * w[2] + w[3];
+    f[2] = mad(q[2], w[2], w[3]);
     f[3] = w[2] * (q[3] + w[3]);
   }
 }
@@ -349,17 +363,17 @@ __device__ __forceinline__ void hllc2(T g1, int dir, const T* ql, const T* qr, T
   T wl[4], wr[4];
   const T il = T(1.0) / ql[0], ir = T(1.0) / qr[0];
   wl[0] = ql[0]; wl[1] = ql[1] * il; wl[2] = ql[2] * il;
-  wl[3] = (ql[3] - T(0.5) * (ql[1] * wl[1] + ql[2] * wl[2])) * g1;
+  wl[3] = (ql[3] - T(0.5) * mad(ql[2], wl[2], ql[1] * wl[1])) * g1;
   wr[0] = qr[0]; wr[1] = qr[1] * ir; wr[2] = qr[2] * ir;
-  wr[3] = (qr[3] - T(0.5) * (qr[1] * wr[1] + qr[2] * wr[2])) * g1;
+  wr[3] = (qr[3] - T(0.5) * mad(qr[2], wr[2], qr[1] * wr[1])) * g1;
   const T hl = (ql[3] + wl[3]) * il;
   const T hr = (qr[3] + wr[3]) * ir;
   const T rr = Cst<T>::sqrt_(fabs(wr[0] * il));
   const T rrr = T(1.0) / (T(1.0) + rr);
-  const T vm0 = (wl[1] + wr[1] * rr) * rrr;
-  const T vm1 = (wl[2] + wr[2] * rr) * rrr;
-  const T qm = T(0.5) * (vm0 * vm0 + vm1 * vm1);
-  const T hm = (hl + hr * rr) * rrr;
+  const T vm0 = mad(wr[1], rr, wl[1]) * rrr;
+  const T vm1 = mad(wr[2], rr, wl[2]) * rrr;
+  const T qm = T(0.5) * mad(vm1, vm1, vm0 * vm0);
+  const T hm = mad(hr, rr, hl) * rrr;
   const T cm = Cst<T>::sqrt_(fabs(g1 * (hm - qm)));
   const T cl = Cst<T>::sqrt_(fabs(wl[3] * il));
   const T cr = Cst<T>::sqrt_(fabs(wr[3] * ir));
@@ -367,9 +381,9 @@ __device__ __forceinline__ void hllc2(T g1, int dir, const T* ql, const T* qr, T
   const T ul = wl[dir], ur = wr[dir];
   const T sl = fmin(ul - cl, vmd - cm);
   const T sr = fmax(ur + cr, vmd + cm);
-  const T sm = (qr[dir] * (sr - ur) - ql[dir] * (sl - ul) + wl[3] - wr[3]) /
-               (wr[0] * (sr - ur) - wl[0] * (sl - ul));
-  const T ps = wl[3] + wl[0] * (ul - sl) * (ul - sm);
+  const T sm = (mad(-ql[dir], sl - ul, qr[dir] * (sr - ur)) + wl[3] - wr[3]) /
+               mad(-wl[0], sl - ul, wr[0] * (sr - ur));
+  const T ps = mad(wl[0] * (ul - sl), ul - sm, wl[3]);
   if (sl > T(0.0)) {
     flux2(dir, ql, wl, F);
   } else if (sl <= T(0.0) && sm > T(0.0)) {
@@ -378,20 +392,20 @@ __device__ __forceinline__ void hllc2(T g1, int dir, const T* ql, const T* qr, T
     const T nom = sl - ul, iden = T(1.0) / (sl - sm);
     T qs[4];
     qs[0] = wl[0] * nom * iden;
-    qs[1] = dir == 1 ? (nom * ql[1] + ps - wl[3]) * iden : nom * ql[1] * iden;
-    qs[2] = dir == 2 ? (nom * ql[2] + ps - wl[3]) * iden : nom * ql[2] * iden;
-    qs[3] = (nom * ql[3] - wl[3] * ul + ps * sm) * iden;
-    for (int k = 0; k < 4; ++k) F[k] = fl[k] + sl * (qs[k] - ql[k]);
+    qs[1] = dir == 1 ? (mad(nom, ql[1], ps) - wl[3]) * iden : nom * ql[1] * iden;
+    qs[2] = dir == 2 ? (mad(nom, ql[2], ps) - wl[3]) * iden : nom * ql[2] * iden;
+    qs[3] = mad(ps, sm, mad(-wl[3], ul, nom * ql[3])) * iden;
+    for (int k = 0; k < 4; ++k) F[k] = mad(sl, qs[k] - ql[k], fl[k]);
   } else if (sm <= T(0.0) && sr >= T(0.0)) {
     T fr[4];
     flux2(dir, qr, wr, fr);
     const T nom = sr - ur, iden = T(1.0) / (sr - sm);
     T qs[4];
     qs[0] = wr[0] * nom * iden;
-    qs[1] = dir == 1 ? (nom * qr[1] + ps - wr[3]) * iden : nom * qr[1] * iden;
-    qs[2] = dir == 2 ? (nom * qr[2] + ps - wr[3]) * iden : nom * qr[2] * iden;
-    qs[3] = (nom * qr[3] - wl[3] * ur + ps * sm) * iden;
-    for (int k = 0; k < 4; ++k) F[k] = fr[k] + sr * (qs[k] - qr[k]);
+    qs[1] = dir == 1 ? (mad(nom, qr[1], ps) - wr[3]) * iden : nom * qr[1] * iden;
+    qs[2] = dir == 2 ? (mad(nom, qr[2], ps) - wr[3]) * iden : nom * qr[2] * iden;
+    qs[3] = mad(ps, sm, mad(-wl[3], ur, nom * qr[3])) * iden;
+    for (int k = 0; k < 4; ++k) F[k] = mad(sr, qs[k] - qr[k], fr[k]);
   } else {
     flux2(dir, qr, wr, F);
   }

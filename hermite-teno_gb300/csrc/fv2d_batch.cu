@@ -126,9 +126,8 @@ cudaError_t bprepare(int* blocks_per_sm) {
                                                        NT, fused::smem_bytes<TX, TY>());
 }
 
-// MINB > 1 would set the register budget of MINB blocks per SM.  None is listed: with reduced
-// budgets the compiler contracted some float expressions of this kernel differently, and every
-// candidate must give the same bits (the tuner's choice must not change results).
+// MINB > 1: the register budget of MINB blocks per SM (as for the single-grid kernel).  Every
+// candidate gives the same bits: this unit is compiled without implicit contraction.
 #define HTENO_BVARIANT(TX, TY, NT, MINB)                                                          \
   { TX, TY, NT, fused::smem_bytes<TX, TY>(), "batch_" #TX "x" #TY "_" #NT "_b" #MINB,              \
     blaunch<TX, TY, NT, MINB>, bprepare<TX, TY, NT, MINB> }
@@ -136,6 +135,7 @@ cudaError_t bprepare(int* blocks_per_sm) {
 const BVariant kBVariants[] = {
     HTENO_BVARIANT(32, 16, 256, 1), HTENO_BVARIANT(32, 8, 256, 1),  HTENO_BVARIANT(16, 16, 256, 1),
     HTENO_BVARIANT(64, 8, 256, 1),  HTENO_BVARIANT(32, 32, 512, 1), HTENO_BVARIANT(16, 8, 128, 1),
+    HTENO_BVARIANT(32, 16, 256, 3), HTENO_BVARIANT(64, 8, 256, 3),
 };
 constexpr int kNumBVariants = sizeof(kBVariants) / sizeof(kBVariants[0]);
 

@@ -16,8 +16,8 @@ std::mutex g_mu;
 
 // MINB > 1 asks the compiler to fit MINB blocks per SM in registers (more warps to hide latency,
 // at the price of a few spills); the tuner keeps whichever shape and register budget runs
-// fastest.  Every variant must give the same bits (tested): budgets of 64 registers (MINB = 4 at
-// 256 threads) did not -- the compiler contracted some float expressions differently there.
+// fastest.  Every variant gives the same bits (tested): this unit is compiled without implicit
+// fused multiply-adds, so no instantiation can contract an expression differently.
 template <int TX, int TY, int NT, int MINB>
 __global__ void __launch_bounds__(NT, MINB) k_fused(Geo G, int stage, fused::StageArgs a) {
   if (a.st && a.st->done) return;

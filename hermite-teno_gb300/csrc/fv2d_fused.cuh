@@ -75,9 +75,9 @@ __device__ __forceinline__ int teno_pat_s(const float* v, bool improved) {
   if (!improved) tau = fabsf(lagrange_b35(v) - (SI0 + SI2 + 4.0f * SI1) * (1.0f / 6.0f));
   else tau = fmaxf(fmaxf(SI0, SI1), SI2);
   const float ez = HTENO_F32_EPSZ;
-  const float r0 = 1.0f + tau * __frcp_rn(SI0 + ez);
-  const float r1 = 1.0f + tau * __frcp_rn(SI1 + ez);
-  const float r2 = 1.0f + tau * __frcp_rn(SI2 + ez);
+  const float r0 = fmaf(tau, __frcp_rn(SI0 + ez), 1.0f);
+  const float r1 = fmaf(tau, __frcp_rn(SI1 + ez), 1.0f);
+  const float r2 = fmaf(tau, __frcp_rn(SI2 + ez), 1.0f);
   return teno_pattern(r0, r1, r2, float(HTENO_LAG_CT));
 }
 
@@ -88,7 +88,7 @@ __device__ __forceinline__ bool flat5(const float* v) {
 }
 
 __device__ __forceinline__ float weighted(float p0, float p1, float p2, const float* w) {
-  return catchnan(p0 * w[0] + p1 * w[1] + p2 * w[2]);
+  return catchnan(dot3m(p0, w[0], p1, w[1], p2, w[2]));
 }
 
 // Audit counters of the learned router: stencils seen, routed to the linear weights, routed
@@ -108,16 +108,16 @@ __device__ __forceinline__ float side_value(const DevConst& C, int kind, const f
                                             RouteCount& rc) {
   float p0, p1, p2;
   if (side == 0) {
-    p0 = C.f_crj[0][1] * u[2] + C.f_crj[1][1] * u[3] + C.f_crj[2][1] * u[4];
-    p1 = C.f_crj[0][2] * u[1] + C.f_crj[1][2] * u[2] + C.f_crj[2][2] * u[3];
-    p2 = C.f_crj[0][3] * u[0] + C.f_crj[1][3] * u[1] + C.f_crj[2][3] * u[2];
+    p0 = dot3m(C.f_crj[0][1], u[2], C.f_crj[1][1], u[3], C.f_crj[2][1], u[4]);
+    p1 = dot3m(C.f_crj[0][2], u[1], C.f_crj[1][2], u[2], C.f_crj[2][2], u[3]);
+    p2 = dot3m(C.f_crj[0][3], u[0], C.f_crj[1][3], u[1], C.f_crj[2][3], u[2]);
   } else {
-    p0 = C.f_crj[0][0] * u[3] + C.f_crj[1][0] * u[4] + C.f_crj[2][0] * u[5];
-    p1 = C.f_crj[0][1] * u[2] + C.f_crj[1][1] * u[3] + C.f_crj[2][1] * u[4];
-    p2 = C.f_crj[0][2] * u[1] + C.f_crj[1][2] * u[2] + C.f_crj[2][2] * u[3];
+    p0 = dot3m(C.f_crj[0][0], u[3], C.f_crj[1][0], u[4], C.f_crj[2][0], u[5]);
+    p1 = dot3m(C.f_crj[0][1], u[2], C.f_crj[1][1], u[3], C.f_crj[2][1], u[4]);
+    p2 = dot3m(C.f_crj[0][2], u[1], C.f_crj[1][2], u[2], C.f_crj[2][2], u[3]);
   }
   const float* v = u + side;
-  if (kind == 2) return p0 * tab[side][7][0] + p1 * tab[side][7][1] + p2 * tab[side][7][2];
+  if (kind == 2) return dot3m(p0, tab[side][7][0], p1, tab[side][7][1], p2, tab[side][7][2]);
   if (kind >= 3) return alt_side(kind, p0, p1, p2, v, tab[side], tab[side][7]);
   int pat = 7;
   if (!routed || audit) pat = teno_pat_s(v, kind == 1);
@@ -205,7 +205,7 @@ __device__ __forceinline__ double tile_stage(const DevConst& C, const Geo& G, in
     S.q[3][y][x] = e;
     const float ir = __frcp_rn(r);
     const float u = mx * ir, v = my * ir;
-    const float p = (e - 0.5f * (mx * u + my * v)) * g1;
+    const float p = (e - 0.5f * fmaf(my, v, mx * u)) * g1;
     S.p[0][y][x] = u;
     S.p[1][y][x] = v;
     S.p[2][y][x] = (e + p) * ir;
@@ -292,7 +292,7 @@ __device__ __forceinline__ double tile_stage(const DevConst& C, const Geo& G, in
       else rusanov2(float(G.gamma), g1, 1, R, ql, qr, Fm);
       const float wm = C.f_gl3w[m];
 #pragma unroll
-      for (int v = 0; v < 4; ++v) acc[v] = m == 0 ? wm * Fm[v] : acc[v] + wm * Fm[v];
+      for (int v = 0; v < 4; ++v) acc[v] = m == 0 ? wm * Fm[v] : fmaf(wm, Fm[v], acc[v]);
     }
 #pragma unroll
     for (int v = 0; v < 4; ++v) S.fx[v][r][f] = acc[v];
@@ -360,7 +360,7 @@ __device__ __forceinline__ double tile_stage(const DevConst& C, const Geo& G, in
       else rusanov2(float(G.gamma), g1, 2, R, ql, qr, Fm);
       const float wm = C.f_gl3w[m];
 #pragma unroll
-      for (int v = 0; v < 4; ++v) acc[v] = m == 0 ? wm * Fm[v] : acc[v] + wm * Fm[v];
+      for (int v = 0; v < 4; ++v) acc[v] = m == 0 ? wm * Fm[v] : fmaf(wm, Fm[v], acc[v]);
     }
 #pragma unroll
     for (int v = 0; v < 4; ++v) S.fy[v][gg][col] = acc[v];

@@ -24,8 +24,11 @@ ORACLE_DIR = REPO_DIR / "oracle"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
               "-Xcompiler", "-ffp-contract=off", "--expt-relaxed-constexpr"]
-# Translation units holding the bit-reproducible FP64 path: no fused multiply-adds.
-NO_FMAD = {"fv2d_fp64.cu", "fv1d.cu", "pointwise.cu", "hermite2d_fp64.cu", "hermite1d.cu"}
+# Units compiled without implicit fused multiply-adds: the bit-reproducible FP64 units, and the
+# fused mixed-precision units, whose tile-shape candidates must give the same bits (with implicit
+# contraction the compiler fused different float expressions in different instantiations).
+NO_FMAD = {"fv2d_fp64.cu", "fv1d.cu", "pointwise.cu", "hermite2d_fp64.cu", "hermite1d.cu",
+           "fv2d_fused.cu", "fv2d_batch.cu"}
 
 
 def _cuda_home() -> Path:

@@ -73,7 +73,7 @@ def test_batch_graph_replay_is_resumable(hteno_lib, cuda):
 def test_batch_tile_shapes_agree(hteno_lib, cuda):
     outs = []
     try:
-        for v in range(6):  # every tile shape of the tuner
+        for v in range(8):  # every tile shape and register budget of the tuner
             os.environ["HTENO_FV2D_TILE"] = str(v)
             b, _, _ = make_batch(hteno_lib, SIZES[:3], seed0=9)
             with b:
