@@ -98,6 +98,59 @@ __global__ void __launch_bounds__(kThreads) k1_flux(Geo1 G, const double* __rest
   for (int v = 0; v < 3; ++v) F[v * (n + 1) + f] = Ff[v];
 }
 
+// The FP64 face kernel with the work of a face spread over 8 lanes: lane l = r + 4 s (r < 3 the
+// characteristic field, s the side) projects its field's 6-cell stencil and reconstructs one side;
+// the group's lane 0 gathers the six values, projects back and computes the flux.  A 1D grid has
+// a few hundred faces: spreading each face's FP64 work over more lanes and warps (hence SMs)
+// shortens the step; every value is computed with the same operations as in k1_flux.
+__global__ void __launch_bounds__(kThreads) k1_flux_lanes(Geo1 G, const double* __restrict__ q,
+                                                          double* __restrict__ F,
+                                                          const StepState* st) {
+  if (st->done) return;
+  const int gid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int f = gid >> 3, l = gid & 7;
+  const bool live = f <= G.nx;
+  const int fc = live ? f : G.nx;  // lanes past the last face compute that face, store nothing
+  const int n = G.nx;
+  double qa[3], qb[3], wa[3], wb[3], ha, hb, sa, sb;
+  const int ca = bmap(fc - 1, n, G.bc), cb = bmap(fc, n, G.bc);
+  for (int v = 0; v < 3; ++v) {
+    qa[v] = q[v * n + ca];
+    qb[v] = q[v * n + cb];
+  }
+  cell_prim1(G.g1, qa, wa, ha, sa);
+  cell_prim1(G.g1, qb, wb, hb, sb);
+  double R[9], L[9];
+  par::eig1(G.g1, sa, wa[1], ha, sb, wb[1], hb, R, L);
+  const int r = l & 3, side = l >> 2;
+  double val = 0.0;
+  if (r < 3) {
+    double ch[6];
+    for (int m = 0; m < 6; ++m) {
+      const int c = bmap(fc - 3 + m, n, G.bc);
+      double sum = L[3 * r] * q[c];  // row r of par::mv3
+      sum = sum + L[3 * r + 1] * q[n + c];
+      sum = sum + L[3 * r + 2] * q[2 * n + c];
+      ch[m] = sum;
+    }
+    val = par::lagrange_side(c_dev, G.recon, ch, side);
+  }
+  const int base = int(threadIdx.x & 31u) & ~7;
+  double cl[3], cr[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    cl[k] = __shfl_sync(0xffffffffu, val, base + k);
+    cr[k] = __shfl_sync(0xffffffffu, val, base + 4 + k);
+  }
+  if (l != 0 || !live) return;
+  double ql[3], qr[3], Ff[3];
+  par::mv3(R, cl, ql);  // transformToConservative (FV_System1D.h:48-51)
+  par::mv3(R, cr, qr);
+  if (G.flux == HTENO_FLUX_HLLC) par::hllc1(G.g1, ql, qr, Ff);
+  else par::rusanov1(G.gamma, G.g1, L, R, ql, qr, Ff);
+  for (int v = 0; v < 3; ++v) F[v * (n + 1) + f] = Ff[v];
+}
+
 // rhs (FV_System1D.cpp:237-240) + RungeKutta3 (:243-272); max wave speed on the last stage
 template <typename T>
 __global__ void k1_update(Geo1 G, int stage, const T* __restrict__ F, double* __restrict__ q,
@@ -198,16 +251,48 @@ Geo1 geo1_of(const hteno_solver* s) {
 }
 
 template <typename T>
-void launch_step(hteno_solver* s, const Geo1& G) {
+void launch_step(hteno_solver* s, const Geo1& G, cudaStream_t cs) {
   const unsigned gf = unsigned((G.nx + 1 + kThreads - 1) / kThreads);
   const unsigned gc = unsigned((G.nx + kThreads - 1) / kThreads);
   T* F = static_cast<T*>(s->work);
-  k_begin_step<<<1, 1, 0, s->stream>>>(s->dstate);
+  k_begin_step<<<1, 1, 0, cs>>>(s->dstate);
+  const unsigned gl = unsigned((8 * (G.nx + 1) + kThreads - 1) / kThreads);
   for (int stage = 1; stage <= 3; ++stage) {
-    k1_flux<T><<<gf, kThreads, 0, s->stream>>>(G, s->q, F, s->dstate);
-    k1_update<T><<<gc, kThreads, 0, s->stream>>>(G, stage, F, s->q, s->q0, s->dstate);
+    if constexpr (std::is_same<T, double>::value)
+      k1_flux_lanes<<<gl, kThreads, 0, cs>>>(G, s->q, F, s->dstate);
+    else
+      k1_flux<T><<<gf, kThreads, 0, cs>>>(G, s->q, F, s->dstate);
+    k1_update<T><<<gc, kThreads, 0, cs>>>(G, stage, F, s->q, s->q0, s->dstate);
   }
-  k_end_step<<<1, 1, 0, s->stream>>>(s->dstate);
+  k_end_step<<<1, 1, 0, cs>>>(s->dstate);
+}
+
+// A 1D step is 8 small launches whose CPU launch cost exceeds their GPU time; runs of
+// kGraphSteps steps are captured once into a graph (the solver's buffers are fixed) and replayed.
+constexpr int kGraphSteps = 16;
+
+void launch_steps(hteno_solver* s, const Geo1& G, int n, cudaStream_t cs) {
+  for (int k = 0; k < n; ++k) {
+    if (s->cfg.precision == HTENO_PREC_MIXED) launch_step<float>(s, G, cs);
+    else launch_step<double>(s, G, cs);
+  }
+}
+
+cudaError_t ensure_graph(hteno_solver* s, const Geo1& G) {
+  if (s->step_graph) return cudaSuccess;
+  cudaStream_t cap;
+  cudaError_t e = cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking);
+  if (e != cudaSuccess) return e;
+  cudaGraph_t g = nullptr;
+  e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+  if (e == cudaSuccess) {
+    launch_steps(s, G, kGraphSteps, cap);
+    e = cudaStreamEndCapture(cap, &g);
+  }
+  if (e == cudaSuccess) e = cudaGraphInstantiate(&s->step_graph, g, 0);
+  if (g) cudaGraphDestroy(g);
+  cudaStreamDestroy(cap);
+  return e;
 }
 
 }  // namespace
@@ -247,10 +332,16 @@ int fv1d_kxrcf(hteno_solver* s, uint8_t* flags) {
 
 int fv1d_step_async(hteno_solver* s, int nsteps) {
   const Geo1 G = geo1_of(s);
-  for (int n = 0; n < nsteps; ++n) {
-    if (s->cfg.precision == HTENO_PREC_MIXED) launch_step<float>(s, G);
-    else launch_step<double>(s, G);
+  int left = nsteps;
+  if (!s->timing && nsteps >= kGraphSteps) {  // per-kernel timing needs the plain launches
+    const cudaError_t e = ensure_graph(s, G);
+    if (e != cudaSuccess) return cuda_error(s, e, "fv1d step graph");
+    for (; left >= kGraphSteps; left -= kGraphSteps) {
+      const cudaError_t el = cudaGraphLaunch(s->step_graph, s->stream);
+      if (el != cudaSuccess) return cuda_error(s, el, "fv1d graph launch");
+    }
   }
+  launch_steps(s, G, left, s->stream);
   return cuda_error(s, cudaGetLastError(), "fv1d step launch");
 }
 

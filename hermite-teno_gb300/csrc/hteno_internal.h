@@ -72,6 +72,7 @@ struct hteno_solver {
   uint8_t* deep = nullptr;  // plain FV 2D: cells of uniform 7 x 7 neighbourhoods (per stage)
   bool uniform_skip = true;  // FV 2D: uniform regions take their exactly zero residual directly
   double* ghost_faces = nullptr;  // plain FV 2D with HTENO_BC_TAYLOR / _DOUBLE_MACH: ghost face rows
+  cudaGraphExec_t step_graph = nullptr;  // 1D schemes: a run of steps replayed as one graph
   // learned routing (mixed FV 2D): classifier, threshold, audit period, masks, audit sums
   hteno_mlp* router = nullptr;
   float router_thr = 0.9f;

@@ -237,6 +237,23 @@ __device__ __forceinline__ void lagrange_recon(const DevConst& C, int kind, cons
                                                  : teno_side(C, p, u + 1, 1, kind == 1);
 }
 
+// One side of lagrange_recon (side 0: u^-, side 1: u^+), the same arithmetic.
+__device__ __forceinline__ double lagrange_side(const DevConst& C, int kind, const double* u, int side) {
+  double p[3];
+  if (side == 0) {
+    p[0] = dot3(C.crj[0][1], C.crj[1][1], C.crj[2][1], u + 2);
+    p[1] = dot3(C.crj[0][2], C.crj[1][2], C.crj[2][2], u + 1);
+    p[2] = dot3(C.crj[0][3], C.crj[1][3], C.crj[2][3], u + 0);
+    return kind == 2 ? dot3v(p, C.dkm) : kind >= 3 ? alt_side(C, kind, p, u, 0)
+                                                   : teno_side(C, p, u, 0, kind == 1);
+  }
+  p[0] = dot3(C.crj[0][0], C.crj[1][0], C.crj[2][0], u + 3);
+  p[1] = dot3(C.crj[0][1], C.crj[1][1], C.crj[2][1], u + 2);
+  p[2] = dot3(C.crj[0][2], C.crj[1][2], C.crj[2][2], u + 1);
+  return kind == 2 ? dot3v(p, C.dkp) : kind >= 3 ? alt_side(C, kind, p, u + 1, 1)
+                                                 : teno_side(C, p, u + 1, 1, kind == 1);
+}
+
 // weno5JS3PointsQuadrature (Schemes_Lagrange.cpp:1155-1217)
 __device__ __forceinline__ void gl3(const DevConst& C, const double* u, double* out) {
   double bg[3], cg[3], s2[3];

@@ -119,6 +119,7 @@ void release(hteno_solver* s) {
   cudaFree(s->dstate);
   if (s->hstate) cudaFreeHost(s->hstate);
   for (cudaEvent_t e : s->ev) cudaEventDestroy(e);
+  if (s->step_graph) cudaGraphExecDestroy(s->step_graph);
   if (s->own_stream && s->stream) cudaStreamDestroy(s->stream);
 }
 
