@@ -64,14 +64,33 @@ __device__ __forceinline__ double lagrange_b35(const double* v) {
   return r / 5040.0;
 }
 
+// 1/x to a relative 2^-45 for the cut-off decision only (never for a value that is kept): a
+// float reciprocal of x's significand (rcp.approx.ftz.f32, on the MUFU pipe), rescaled by x's
+// exponent on the integer pipes, and one Newton step in double (2 FMAs instead of the ~10 FP64
+// operations of a correctly rounded reciprocal).  Exponents near the ends of the range, zeros,
+// infinities and NaN take the correctly rounded reciprocal.
+__device__ __forceinline__ double decision_rcp(double x) {
+  const unsigned hx = unsigned(__double2hiint(x)), lx = unsigned(__double2loint(x));
+  const unsigned ex = (hx >> 20) & 0x7ffu;
+  if (ex - 64u > 1916u) return __drcp_rn(x);
+  const float m = __uint_as_float(0x3f800000u | ((hx & 0xfffffu) << 3) | (lx >> 29));
+  float rf;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(rf) : "f"(m));
+  const unsigned r = __float_as_uint(rf), er = (r >> 23) & 0xffu, mr = r & 0x7fffffu;
+  const unsigned hy = (hx & 0x80000000u) | ((er + 2046u - 127u - ex) << 20) | (mr >> 3);
+  const double y = __hiloint2double(int(hy), int(mr << 29));
+  return fma(y, fma(-x, y, 1.0), y);
+}
+
 // Cut-off pattern of the reference's cutOff() (:1141-1149) given SI and tau.  Fast path with a
-// guard band; inside the band the reference's arithmetic decides.
+// guard band of 1e-10 relative (the fast path's own error is ~1e-13); inside the band the
+// reference's arithmetic decides.
 __device__ __forceinline__ int cutoff_pattern(const double* SI, double tau, double epsz, double ct) {
   double r[3], a[3];
 #pragma unroll
-  for (int k = 0; k < 3; ++k) r[k] = 1.0 + tau * __drcp_rn(SI[k] + epsz);
+  for (int k = 0; k < 3; ++k) r[k] = 1.0 + tau * decision_rcp(SI[k] + epsz);
   const double rm = fmax(fmax(r[0], r[1]), r[2]);
-  const double inv = __drcp_rn(rm);
+  const double inv = decision_rcp(rm);
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
     double x = r[k] * inv;
