@@ -273,6 +273,32 @@ __device__ __forceinline__ double lagrange_side(const DevConst& C, int kind, con
                                                  : teno_side(C, p, u + 1, 1, kind == 1);
 }
 
+// Correctly rounded a / b for several numerators over one denominator: y = RN(1/b) once, then per
+// numerator q0 = RN(a y), r = a - b q0 (exact, one FMA), q = RN(q0 + r y).  By Markstein's theorem
+// (Markstein, IBM J. Res. Dev. 34(1), 1990; Muller et al., Handbook of Floating-Point Arithmetic,
+// 2018, Sec. 4.7) q is a / b correctly rounded when y is within half an ulp of 1/b and q0 within
+// one ulp of a / b, barring underflow and overflow: 3 FP64 operations per quotient instead of a
+// division's ~10.  Operands outside [2^-500, 2^501) in magnitude (zeros, subnormals, infinities,
+// NaN) take the division itself, so the theorem's conditions hold wherever the short form is used.
+struct Den {
+  double b, y;
+  bool ok;
+};
+__device__ __forceinline__ bool mid_range(double x) {
+  const unsigned e = (unsigned(__double2hiint(x)) >> 20) & 0x7ffu;
+  return e - 523u <= 1000u;  // biased exponent in [523, 1523]
+}
+__device__ __forceinline__ Den den_of(double b) { return Den{b, __drcp_rn(b), mid_range(b)}; }
+__device__ __forceinline__ double quot(double a, const Den& d) {
+  if (d.ok && mid_range(a)) {
+    const double q0 = a * d.y;
+    const double r = fma(-d.b, q0, a);
+    return fma(r, d.y, q0);
+  }
+  return a / d.b;
+}
+constexpr double kRcp24 = 1.0 / 24.0;  // RN(1/24), folded at compile time
+
 // weno5JS3PointsQuadrature (Schemes_Lagrange.cpp:1155-1217)
 __device__ __forceinline__ void gl3(const DevConst& C, const double* u, double* out) {
   double bg[3], cg[3], s2[3];
@@ -290,9 +316,10 @@ __device__ __forceinline__ void gl3(const DevConst& C, const double* u, double* 
     p[1] = dot3(C.gp[0][1], C.gp[1][1], C.gp[2][1], u + 1);
     p[2] = dot3(C.gp[0][2], C.gp[1][2], C.gp[2][2], u + 2);
     out[0] = dot3v(p, C.gl3flat[0]);
-    p[0] = (-u[0] + 2.0 * u[1] + 23.0 * u[2]) / 24.0;
-    p[1] = (-u[1] + 26.0 * u[2] - u[3]) / 24.0;
-    p[2] = (23.0 * u[2] + 2.0 * u[3] - u[4]) / 24.0;
+    const Den d24{24.0, kRcp24, true};
+    p[0] = quot(-u[0] + 2.0 * u[1] + 23.0 * u[2], d24);
+    p[1] = quot(-u[1] + 26.0 * u[2] - u[3], d24);
+    p[2] = quot(23.0 * u[2] + 2.0 * u[3] - u[4], d24);
     double c = C.sumw0p * dot3v(p, C.gl3flat[1]);
     c = c - C.sumw0m * dot3v(p, C.gl3flat[2]);
     out[1] = c;
@@ -311,21 +338,24 @@ __device__ __forceinline__ void gl3(const DevConst& C, const double* u, double* 
     s2[k] = e * e;  // pow(eps + SI, 2)
   }
   double p[3], w[3];
+  const Den ds[3] = {den_of(s2[0]), den_of(s2[1]), den_of(s2[2])};  // each serves 4 weight sets
   auto weighted = [&](const double* lw) {
 #pragma unroll
-    for (int k = 0; k < 3; ++k) w[k] = lw[k] / s2[k];
+    for (int k = 0; k < 3; ++k) w[k] = quot(lw[k], ds[k]);
     const double s = (w[0] + w[1]) + w[2];
+    const Den dn = den_of(s);
 #pragma unroll
-    for (int k = 0; k < 3; ++k) w[k] = w[k] / s;
+    for (int k = 0; k < 3; ++k) w[k] = quot(w[k], dn);
     return dot3v(p, w);
   };
   p[0] = dot3(C.gp[0][0], C.gp[1][0], C.gp[2][0], u + 0);
   p[1] = dot3(C.gp[0][1], C.gp[1][1], C.gp[2][1], u + 1);
   p[2] = dot3(C.gp[0][2], C.gp[1][2], C.gp[2][2], u + 2);
   out[0] = weighted(C.linwp);
-  p[0] = (-u[0] + 2.0 * u[1] + 23.0 * u[2]) / 24.0;
-  p[1] = (-u[1] + 26.0 * u[2] - u[3]) / 24.0;
-  p[2] = (23.0 * u[2] + 2.0 * u[3] - u[4]) / 24.0;
+  const Den d24{24.0, kRcp24, true};
+  p[0] = quot(-u[0] + 2.0 * u[1] + 23.0 * u[2], d24);
+  p[1] = quot(-u[1] + 26.0 * u[2] - u[3], d24);
+  p[2] = quot(23.0 * u[2] + 2.0 * u[3] - u[4], d24);
   double c = C.sumw0p * weighted(C.linw0p);
   c = c - C.sumw0m * weighted(C.linw0m);
   out[1] = c;
