@@ -299,8 +299,9 @@ __device__ __forceinline__ double quot(double a, const Den& d) {
 }
 constexpr double kRcp24 = 1.0 / 24.0;  // RN(1/24), folded at compile time
 
-// weno5JS3PointsQuadrature (Schemes_Lagrange.cpp:1155-1217)
-__device__ __forceinline__ void gl3(const DevConst& C, const double* u, double* out) {
+// weno5JS3PointsQuadrature (Schemes_Lagrange.cpp:1155-1217).  Not inlined: the flux kernels call
+// it 8 times per face, and eight inlined copies overflow the instruction cache.
+static __device__ __noinline__ void gl3(const DevConst& C, const double* u, double* out) {
   double bg[3], cg[3], s2[3];
   bg[0] = u[0] - 4.0 * u[1] + 3.0 * u[2];
   cg[0] = u[0] - 2.0 * u[1] + u[2];
