@@ -131,6 +131,17 @@ __device__ __forceinline__ float side_value(const DevConst& C, int kind, const f
   return weighted(p0, p1, p2, tab[side][routed ? 7 : pat]);
 }
 
+// GL3 of one face array, not inlined: phases C and E call it 8 times per face each, and inlined
+// copies crowd the instruction cache.
+struct Gl3f {
+  float a, b, c;
+};
+static __device__ __noinline__ Gl3f gl3_f(const DevConst& C, const float* u) {
+  Gl3f g;
+  gl3(C, u, g.a, g.b, g.c);
+  return g;
+}
+
 // Pointers of one stage of one grid.
 struct StageArgs {
   const double* qin;    // input state of the stage (halo reads)
@@ -274,7 +285,10 @@ __device__ __forceinline__ double tile_stage(const DevConst& C, const Geo& G, in
       float u5[5];
 #pragma unroll
       for (int m = 0; m < 5; ++m) u5[m] = S.c[k][(r + m) * Sh::XF + f];
-      gl3(C, u5, g[k][0], g[k][1], g[k][2]);
+      const Gl3f o = gl3_f(C, u5);
+      g[k][0] = o.a;
+      g[k][1] = o.b;
+      g[k][2] = o.c;
     }
     const int y = r + 3, xa = f + 2, xb = f + 3;
     const Roe2<float> R = roe2<float>(g1, S.p[3][y][xa], S.p[0][y][xa], S.p[1][y][xa],
@@ -342,7 +356,10 @@ __device__ __forceinline__ double tile_stage(const DevConst& C, const Geo& G, in
       float u5[5];
 #pragma unroll
       for (int m = 0; m < 5; ++m) u5[m] = S.c[k][gg * Sh::YC + col + m];
-      gl3(C, u5, g[k][0], g[k][1], g[k][2]);
+      const Gl3f o = gl3_f(C, u5);
+      g[k][0] = o.a;
+      g[k][1] = o.b;
+      g[k][2] = o.c;
     }
     const int x = col + 3, ya = gg + 2, yb = gg + 3;
     const Roe2<float> R = roe2<float>(g1, S.p[3][ya][x], S.p[0][ya][x], S.p[1][ya][x],
