@@ -103,32 +103,48 @@ struct RouteCount {
 // set (learned routing, TENO kinds) the side takes the linear weights without evaluating the
 // indicators; when auditing, the plain cut-off is evaluated as well and counted.  The weight
 // tables live in shared memory: a per-thread pattern would serialise constant-memory reads.
-__device__ __forceinline__ float side_value(const DevConst& C, int kind, const float (*tab)[8][3],
-                                            const float* u, int side, bool routed, bool audit,
-                                            RouteCount& rc) {
+struct SideOut {
+  float v;
+  int pat;  // the TENO cut-off pattern evaluated (7 when not evaluated)
+};
+// Not inlined (8 calls per face in phases B and D); the stencil comes by value so it stays in
+// registers.  The caller counts the audit.
+static __device__ __noinline__ SideOut side_value(const DevConst& C, int kind,
+                                                  const float (*tab)[8][3], float u0, float u1,
+                                                  float u2, float u3, float u4, float u5, int side,
+                                                  bool routed, bool audit) {
   float p0, p1, p2;
   if (side == 0) {
-    p0 = dot3m(C.f_crj[0][1], u[2], C.f_crj[1][1], u[3], C.f_crj[2][1], u[4]);
-    p1 = dot3m(C.f_crj[0][2], u[1], C.f_crj[1][2], u[2], C.f_crj[2][2], u[3]);
-    p2 = dot3m(C.f_crj[0][3], u[0], C.f_crj[1][3], u[1], C.f_crj[2][3], u[2]);
+    p0 = dot3m(C.f_crj[0][1], u2, C.f_crj[1][1], u3, C.f_crj[2][1], u4);
+    p1 = dot3m(C.f_crj[0][2], u1, C.f_crj[1][2], u2, C.f_crj[2][2], u3);
+    p2 = dot3m(C.f_crj[0][3], u0, C.f_crj[1][3], u1, C.f_crj[2][3], u2);
   } else {
-    p0 = dot3m(C.f_crj[0][0], u[3], C.f_crj[1][0], u[4], C.f_crj[2][0], u[5]);
-    p1 = dot3m(C.f_crj[0][1], u[2], C.f_crj[1][1], u[3], C.f_crj[2][1], u[4]);
-    p2 = dot3m(C.f_crj[0][2], u[1], C.f_crj[1][2], u[2], C.f_crj[2][2], u[3]);
+    p0 = dot3m(C.f_crj[0][0], u3, C.f_crj[1][0], u4, C.f_crj[2][0], u5);
+    p1 = dot3m(C.f_crj[0][1], u2, C.f_crj[1][1], u3, C.f_crj[2][1], u4);
+    p2 = dot3m(C.f_crj[0][2], u1, C.f_crj[1][2], u2, C.f_crj[2][2], u3);
   }
-  const float* v = u + side;
-  if (kind == 2) return dot3m(p0, tab[side][7][0], p1, tab[side][7][1], p2, tab[side][7][2]);
-  if (kind >= 3) return alt_side(kind, p0, p1, p2, v, tab[side], tab[side][7]);
+  const float v[5] = {side ? u1 : u0, side ? u2 : u1, side ? u3 : u2, side ? u4 : u3, side ? u5 : u4};
+  if (kind == 2) return {dot3m(p0, tab[side][7][0], p1, tab[side][7][1], p2, tab[side][7][2]), 7};
+  if (kind >= 3) return {alt_side(kind, p0, p1, p2, v, tab[side], tab[side][7]), 7};
   int pat = 7;
   if (!routed || audit) pat = teno_pat_s(v, kind == 1);
-  if (audit) {
+  return {weighted(p0, p1, p2, tab[side][routed ? 7 : pat]), pat};
+}
+
+// One side of teno5 / teno5i / linear / an alternative for the stencil u[0..5], with the audit
+// of the learned router counted here (TENO kinds).
+__device__ __forceinline__ float side_counted(const DevConst& C, int kind, const float (*tab)[8][3],
+                                              const float* u, int side, bool routed, bool audit,
+                                              RouteCount& rc) {
+  const SideOut o = side_value(C, kind, tab, u[0], u[1], u[2], u[3], u[4], u[5], side, routed, audit);
+  if (audit && kind <= 1) {
     rc.seen += 1;
-    rc.smooth += pat == 7;
-    rc.flat += flat5(v);
+    rc.smooth += o.pat == 7;
+    rc.flat += flat5(u + side);
     rc.routed += routed;
-    rc.misrouted += routed && pat != 7;
+    rc.misrouted += routed && o.pat != 7;
   }
-  return weighted(p0, p1, p2, tab[side][routed ? 7 : pat]);
+  return o.v;
 }
 
 // GL3 of one face array, not inlined: phases C and E call it 8 times per face each, and inlined
@@ -270,8 +286,8 @@ __device__ __forceinline__ double tile_stage(const DevConst& C, const Geo& G, in
     }
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
-      S.c[r][it] = side_value(C, G.recon, S.wtab, ch[r], 0, (route >> (2 * r)) & 1, own, rc);
-      S.c[4 + r][it] = side_value(C, G.recon, S.wtab, ch[r], 1, (route >> (2 * r + 1)) & 1, own, rc);
+      S.c[r][it] = side_counted(C, G.recon, S.wtab, ch[r], 0, (route >> (2 * r)) & 1, own, rc);
+      S.c[4 + r][it] = side_counted(C, G.recon, S.wtab, ch[r], 1, (route >> (2 * r + 1)) & 1, own, rc);
     }
   }
   __syncthreads();
@@ -341,8 +357,8 @@ __device__ __forceinline__ double tile_stage(const DevConst& C, const Geo& G, in
     }
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
-      S.c[r][it] = side_value(C, G.recon, S.wtab, ch[r], 0, (route >> (2 * r)) & 1, own, rc);
-      S.c[4 + r][it] = side_value(C, G.recon, S.wtab, ch[r], 1, (route >> (2 * r + 1)) & 1, own, rc);
+      S.c[r][it] = side_counted(C, G.recon, S.wtab, ch[r], 0, (route >> (2 * r)) & 1, own, rc);
+      S.c[4 + r][it] = side_counted(C, G.recon, S.wtab, ch[r], 1, (route >> (2 * r + 1)) & 1, own, rc);
     }
   }
   __syncthreads();
