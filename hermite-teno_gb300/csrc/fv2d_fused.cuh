@@ -158,6 +158,25 @@ static __device__ __noinline__ Gl3f gl3_f(const DevConst& C, const float* u) {
   return g;
 }
 
+// The flux at one Gauss point of a face: R back-projection of both sides' characteristic values,
+// then HLLC or Rusanov.  Not inlined (3 calls per face in each of phases C and E).
+struct F4 {
+  float v[4];
+};
+template <int DIR>
+static __device__ __noinline__ F4 gauss_flux(Roe2<float> R, int flux, float g1, float gamma, float l0,
+                                             float l1, float l2, float l3, float r0, float r1,
+                                             float r2, float r3) {
+  const float cl[4] = {l0, l1, l2, l3}, cr[4] = {r0, r1, r2, r3};
+  float ql[4], qr[4];
+  F4 F;
+  roe_right(R, DIR, cl, ql);
+  roe_right(R, DIR, cr, qr);
+  if (flux == HTENO_FLUX_HLLC) hllc2(g1, DIR, ql, qr, F.v);
+  else rusanov2(gamma, g1, DIR, R, ql, qr, F.v);
+  return F;
+}
+
 // Pointers of one stage of one grid.
 struct StageArgs {
   const double* qin;    // input state of the stage (halo reads)
@@ -313,16 +332,11 @@ __device__ __forceinline__ double tile_stage(const DevConst& C, const Geo& G, in
     float acc[4];
 #pragma unroll
     for (int m = 0; m < 3; ++m) {
-      const float cl[4] = {g[0][m], g[1][m], g[2][m], g[3][m]};
-      const float cr[4] = {g[4][m], g[5][m], g[6][m], g[7][m]};
-      float ql[4], qr[4], Fm[4];
-      roe_right(R, 1, cl, ql);
-      roe_right(R, 1, cr, qr);
-      if (G.flux == HTENO_FLUX_HLLC) hllc2(g1, 1, ql, qr, Fm);
-      else rusanov2(float(G.gamma), g1, 1, R, ql, qr, Fm);
+      const F4 Fm = gauss_flux<1>(R, G.flux, g1, float(G.gamma), g[0][m], g[1][m], g[2][m], g[3][m],
+                                   g[4][m], g[5][m], g[6][m], g[7][m]);
       const float wm = C.f_gl3w[m];
 #pragma unroll
-      for (int v = 0; v < 4; ++v) acc[v] = m == 0 ? wm * Fm[v] : fmaf(wm, Fm[v], acc[v]);
+      for (int v = 0; v < 4; ++v) acc[v] = m == 0 ? wm * Fm.v[v] : fmaf(wm, Fm.v[v], acc[v]);
     }
 #pragma unroll
     for (int v = 0; v < 4; ++v) S.fx[v][r][f] = acc[v];
@@ -384,16 +398,11 @@ __device__ __forceinline__ double tile_stage(const DevConst& C, const Geo& G, in
     float acc[4];
 #pragma unroll
     for (int m = 0; m < 3; ++m) {
-      const float cl[4] = {g[0][m], g[1][m], g[2][m], g[3][m]};
-      const float cr[4] = {g[4][m], g[5][m], g[6][m], g[7][m]};
-      float ql[4], qr[4], Fm[4];
-      roe_right(R, 2, cl, ql);
-      roe_right(R, 2, cr, qr);
-      if (G.flux == HTENO_FLUX_HLLC) hllc2(g1, 2, ql, qr, Fm);
-      else rusanov2(float(G.gamma), g1, 2, R, ql, qr, Fm);
+      const F4 Fm = gauss_flux<2>(R, G.flux, g1, float(G.gamma), g[0][m], g[1][m], g[2][m], g[3][m],
+                                   g[4][m], g[5][m], g[6][m], g[7][m]);
       const float wm = C.f_gl3w[m];
 #pragma unroll
-      for (int v = 0; v < 4; ++v) acc[v] = m == 0 ? wm * Fm[v] : fmaf(wm, Fm[v], acc[v]);
+      for (int v = 0; v < 4; ++v) acc[v] = m == 0 ? wm * Fm.v[v] : fmaf(wm, Fm.v[v], acc[v]);
     }
 #pragma unroll
     for (int v = 0; v < 4; ++v) S.fy[v][gg][col] = acc[v];
