@@ -38,6 +38,34 @@ __device__ __forceinline__ double dot3v(const double* p, const double* w) {
   return s;
 }
 
+// Correctly rounded a / b for several numerators over one denominator: y = RN(1/b) once, then per
+// numerator q0 = RN(a y), r = a - b q0 (exact, one FMA), q = RN(q0 + r y).  By Markstein's theorem
+// (Markstein, IBM J. Res. Dev. 34(1), 1990; Muller et al., Handbook of Floating-Point Arithmetic,
+// 2018, Sec. 4.7) q is a / b correctly rounded when y is within half an ulp of 1/b and q0 within
+// one ulp of a / b, barring underflow and overflow: 3 FP64 operations per quotient instead of a
+// division's ~10.  Operands outside [2^-500, 2^501) in magnitude (zeros, subnormals, infinities,
+// NaN) take the division itself, so the theorem's conditions hold wherever the short form is used.
+struct Den {
+  double b, y;
+  bool ok;
+};
+__device__ __forceinline__ bool mid_range(double x) {
+  const unsigned e = (unsigned(__double2hiint(x)) >> 20) & 0x7ffu;
+  return e - 523u <= 1000u;  // biased exponent in [523, 1523]
+}
+__device__ __forceinline__ Den den_of(double b) { return Den{b, __drcp_rn(b), mid_range(b)}; }
+__device__ __forceinline__ double quot(double a, const Den& d) {
+  if (d.ok && mid_range(a)) {
+    const double q0 = a * d.y;
+    const double r = fma(-d.b, q0, a);
+    return fma(r, d.y, q0);
+  }
+  return a / d.b;
+}
+constexpr double kRcp24 = 1.0 / 24.0;  // RN(1/24), RN(1/6), RN(1/5040), folded at compile time
+constexpr double kRcp6 = 1.0 / 6.0;
+constexpr double kRcp5040 = 1.0 / 5040.0;
+
 // ---- Schemes::Lagrange ----------------------------------------------------------------------
 
 // smoothnessMeasure (Schemes_Lagrange.cpp:1013-1026)
@@ -61,7 +89,7 @@ __device__ __forceinline__ double lagrange_b35(const double* v) {
              v[3] * (104963.0 * v[3] - 299076.0 * v[2] + 179098.0 * v[1] - 38947.0 * v[0]) +
              v[2] * (231153.0 * v[2] - 299076.0 * v[1] + 67923.0 * v[0]) +
              v[1] * (104963.0 * v[1] - 51001.0 * v[0]) + 6908.0 * v[0] * v[0];
-  return r / 5040.0;
+  return quot(r, Den{5040.0, kRcp5040, true});  // r / 5040
 }
 
 // 1/x to a relative 2^-45 for the cut-off decision only (never for a value that is kept): a
@@ -132,7 +160,7 @@ __device__ __forceinline__ double teno_side(const DevConst& C, const double* p, 
   double tau;
   if (!improved) {
     const double b35 = lagrange_b35(v);
-    tau = fabs(b35 - (SI[0] + SI[2] + 4.0 * SI[1]) / 6.0);
+    tau = fabs(b35 - quot(SI[0] + SI[2] + 4.0 * SI[1], Den{6.0, kRcp6, true}));  // ... / 6.0
   } else {
     tau = SI[0];
     tau = (tau < SI[1]) ? SI[1] : tau;
@@ -273,31 +301,6 @@ __device__ __forceinline__ double lagrange_side(const DevConst& C, int kind, con
                                                  : teno_side(C, p, u + 1, 1, kind == 1);
 }
 
-// Correctly rounded a / b for several numerators over one denominator: y = RN(1/b) once, then per
-// numerator q0 = RN(a y), r = a - b q0 (exact, one FMA), q = RN(q0 + r y).  By Markstein's theorem
-// (Markstein, IBM J. Res. Dev. 34(1), 1990; Muller et al., Handbook of Floating-Point Arithmetic,
-// 2018, Sec. 4.7) q is a / b correctly rounded when y is within half an ulp of 1/b and q0 within
-// one ulp of a / b, barring underflow and overflow: 3 FP64 operations per quotient instead of a
-// division's ~10.  Operands outside [2^-500, 2^501) in magnitude (zeros, subnormals, infinities,
-// NaN) take the division itself, so the theorem's conditions hold wherever the short form is used.
-struct Den {
-  double b, y;
-  bool ok;
-};
-__device__ __forceinline__ bool mid_range(double x) {
-  const unsigned e = (unsigned(__double2hiint(x)) >> 20) & 0x7ffu;
-  return e - 523u <= 1000u;  // biased exponent in [523, 1523]
-}
-__device__ __forceinline__ Den den_of(double b) { return Den{b, __drcp_rn(b), mid_range(b)}; }
-__device__ __forceinline__ double quot(double a, const Den& d) {
-  if (d.ok && mid_range(a)) {
-    const double q0 = a * d.y;
-    const double r = fma(-d.b, q0, a);
-    return fma(r, d.y, q0);
-  }
-  return a / d.b;
-}
-constexpr double kRcp24 = 1.0 / 24.0;  // RN(1/24), folded at compile time
 
 // weno5JS3PointsQuadrature (Schemes_Lagrange.cpp:1155-1217).  Not inlined: the flux kernels call
 // it 8 times per face, and eight inlined copies overflow the instruction cache.
