@@ -98,6 +98,10 @@ typedef struct hteno_solver hteno_solver;
  * 2D, FV, TENO5, Rusanov, zero-gradient, FP64, gamma 1.4, CFL 0.4, [0,1]^2. */
 void hteno_config_default(hteno_config* cfg);
 
+/* Creates a solver (device buffers on the current device, its own stream).  Environment read at
+ * creation: HTENO_UNIFORM_SKIP=0 computes uniform regions in full instead of taking their exactly
+ * zero residual (the results are the same bits either way); HTENO_FV2D_TILE=<k> fixes the tile
+ * candidate of the mixed FV 2D kernel instead of timing them (same bits for every candidate). */
 int hteno_create(const hteno_config* cfg, hteno_solver** out);
 int hteno_destroy(hteno_solver* s);
 
