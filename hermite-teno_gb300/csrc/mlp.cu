@@ -55,7 +55,28 @@ struct Smem {
   float stage[16][24];  // classifier: the 6 cells x 4 conserved values of 16 faces
   alignas(8) uint64_t mbar;
   uint32_t tmem;
+  static constexpr bool kTrain = true;
+  static constexpr uint32_t kTmemCols = 256;
 };
+
+// Shared memory of the inference kernels (forward pass only).  The allocation is padded so that
+// at most 4 blocks share an SM, whose 4 x 128 tensor-memory columns are the SM's 512: twice the
+// blocks of the training layout, to overlap more of the layers' issue-wait-load round trips.
+struct SmemI {
+  alignas(128) unsigned char x[128 * 16 * 2];
+  alignas(128) unsigned char h1[128 * 32 * 2];
+  alignas(128) unsigned char h2[128 * 32 * 2];
+  alignas(128) unsigned char w1[32 * 16 * 2];
+  alignas(128) unsigned char w2[32 * 32 * 2];
+  alignas(128) unsigned char w3[16 * 32 * 2];
+  float b1[32], b2[32], b3[16];
+  alignas(8) uint64_t mbar;
+  uint32_t tmem;
+  static constexpr bool kTrain = false;
+  static constexpr uint32_t kTmemCols = 128;
+};
+constexpr size_t kSmemIBytes = 48 * 1024;
+static_assert(sizeof(SmemI) <= kSmemIBytes, "inference shared memory");
 
 // tensor-memory columns
 constexpr uint32_t C_D1 = 0, C_D2 = 32, C_D3 = 64, C_DH2 = 80, C_DH1 = 112;
@@ -66,20 +87,23 @@ __device__ __forceinline__ uint64_t desc_k(const unsigned char* base, int K, int
 }
 
 // Copies the BF16 weight images into the operand layouts and the FP32 biases.
-__device__ void load_weights(Smem& S, const Weights& W) {
+template <typename SM>
+__device__ void load_weights(SM& S, const Weights& W) {
   const __nv_bfloat16* w1 = reinterpret_cast<const __nv_bfloat16*>(W.w1);
   for (int e = threadIdx.x; e < 32 * 16; e += blockDim.x) {
     const int r = e / 16, k = e % 16;
     *reinterpret_cast<__nv_bfloat16*>(S.w1 + tc::kmaj(r, k, 16)) = w1[e];
-    *reinterpret_cast<__nv_bfloat16*>(S.w3t + tc::kmaj(r, k, 16)) =
-        reinterpret_cast<const __nv_bfloat16*>(W.w3t)[e];
+    if constexpr (SM::kTrain)
+      *reinterpret_cast<__nv_bfloat16*>(S.w3t + tc::kmaj(r, k, 16)) =
+          reinterpret_cast<const __nv_bfloat16*>(W.w3t)[e];
   }
   for (int e = threadIdx.x; e < 32 * 32; e += blockDim.x) {
     const int r = e / 32, k = e % 32;
     *reinterpret_cast<__nv_bfloat16*>(S.w2 + tc::kmaj(r, k, 32)) =
         reinterpret_cast<const __nv_bfloat16*>(W.w2)[e];
-    *reinterpret_cast<__nv_bfloat16*>(S.w2t + tc::kmaj(r, k, 32)) =
-        reinterpret_cast<const __nv_bfloat16*>(W.w2t)[e];
+    if constexpr (SM::kTrain)
+      *reinterpret_cast<__nv_bfloat16*>(S.w2t + tc::kmaj(r, k, 32)) =
+          reinterpret_cast<const __nv_bfloat16*>(W.w2t)[e];
   }
   for (int e = threadIdx.x; e < 16 * 32; e += blockDim.x) {
     const int r = e / 32, k = e % 32;
@@ -95,7 +119,8 @@ __device__ void load_weights(Smem& S, const Weights& W) {
 
 // Issue (thread 0) after a barrier; every thread then waits for completion.  Returns false on
 // timeout (uniform over the block).
-__device__ __forceinline__ bool wait_mma(Smem& S, uint32_t& phase) {
+template <typename SM>
+__device__ __forceinline__ bool wait_mma(SM& S, uint32_t& phase) {
   const bool ok = !__syncthreads_or(!tc::mbar_wait(&S.mbar, phase, kWaitLimit));
   if (ok) phase ^= 1u;  // on timeout `phase` stays the pending one
   tc::fence_after();
@@ -118,7 +143,8 @@ __device__ __forceinline__ float warp_sum(float v) {
 
 // Forward pass of the tile whose inputs are in S.x / S.xt; leaves z1..z3 per thread.
 // keep_t: also store H1^T / H2^T (needed by the weight gradients).
-__device__ __forceinline__ bool forward(Smem& S, uint32_t tbase, uint32_t& phase, float* h1,
+template <typename SM>
+__device__ __forceinline__ bool forward(SM& S, uint32_t tbase, uint32_t& phase, float* h1,
                                         float* h2, float* z3, bool keep_t) {
   const int row = threadIdx.x;
   const uint32_t lane_addr = tbase + (uint32_t(threadIdx.x & ~31) << 16);
@@ -135,7 +161,8 @@ __device__ __forceinline__ bool forward(Smem& S, uint32_t tbase, uint32_t& phase
   for (int c = 0; c < 32; ++c) {
     h1[c] = fmaxf(h1[c] + S.b1[c], 0.0f);
     tc::st_bf16(S.h1, tc::kmaj(row, c, 32), h1[c]);
-    if (keep_t) tc::st_bf16(S.h1t, tc::kmaj(c, row, 128), h1[c]);
+    if constexpr (SM::kTrain)
+      if (keep_t) tc::st_bf16(S.h1t, tc::kmaj(c, row, 128), h1[c]);
   }
   before_issue();
   if (threadIdx.x == 0) {
@@ -151,7 +178,8 @@ __device__ __forceinline__ bool forward(Smem& S, uint32_t tbase, uint32_t& phase
   for (int c = 0; c < 32; ++c) {
     h2[c] = fmaxf(h2[c] + S.b2[c], 0.0f);
     tc::st_bf16(S.h2, tc::kmaj(row, c, 32), h2[c]);
-    if (keep_t) tc::st_bf16(S.h2t, tc::kmaj(c, row, 128), h2[c]);
+    if constexpr (SM::kTrain)
+      if (keep_t) tc::st_bf16(S.h2t, tc::kmaj(c, row, 128), h2[c]);
   }
   before_issue();
   if (threadIdx.x == 0) {
@@ -169,40 +197,47 @@ __device__ __forceinline__ bool forward(Smem& S, uint32_t tbase, uint32_t& phase
 }
 
 // Writes one input row (6 features, bf16 bits) into S.x and S.xt.
-__device__ __forceinline__ void put_input(Smem& S, int row, const uint16_t* f) {
+template <typename SM>
+__device__ __forceinline__ void put_input(SM& S, int row, const uint16_t* f) {
 #pragma unroll
   for (int k = 0; k < 16; ++k) {
     const uint16_t bits = k < 6 ? f[k] : uint16_t(0);
     *reinterpret_cast<uint16_t*>(S.x + tc::kmaj(row, k, 16)) = bits;
-    *reinterpret_cast<uint16_t*>(S.xt + tc::kmaj(k, row, 128)) = bits;
+    if constexpr (SM::kTrain) *reinterpret_cast<uint16_t*>(S.xt + tc::kmaj(k, row, 128)) = bits;
   }
 }
 
-__device__ void setup(Smem& S, const Weights& W) {
-  for (int e = threadIdx.x; e < int(sizeof(S.at) / 16); e += blockDim.x)
-    reinterpret_cast<uint4*>(S.at)[e] = make_uint4(0, 0, 0, 0);
+template <typename SM>
+__device__ void setup(SM& S, const Weights& W) {
+  if constexpr (SM::kTrain) {
+    for (int e = threadIdx.x; e < int(sizeof(S.at) / 16); e += blockDim.x)
+      reinterpret_cast<uint4*>(S.at)[e] = make_uint4(0, 0, 0, 0);
+  }
   load_weights(S, W);
-  if (threadIdx.x < 32) {
-    S.gb1[threadIdx.x] = 0.f;
-    S.gb2[threadIdx.x] = 0.f;
-    if (threadIdx.x < 16) S.gb3[threadIdx.x] = 0.f;
+  if constexpr (SM::kTrain) {
+    if (threadIdx.x < 32) {
+      S.gb1[threadIdx.x] = 0.f;
+      S.gb2[threadIdx.x] = 0.f;
+      if (threadIdx.x < 16) S.gb3[threadIdx.x] = 0.f;
+    }
+    if (threadIdx.x == 0) S.loss = 0.f;
   }
   if (threadIdx.x == 0) {
-    S.loss = 0.f;
     tc::mbar_init(&S.mbar, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  if (threadIdx.x < 32) tc::tmem_alloc(&S.tmem, kCols);
+  if (threadIdx.x < 32) tc::tmem_alloc(&S.tmem, SM::kTmemCols);
   tc::fence_before();
   __syncthreads();
   tc::fence_after();
 }
 
-__device__ void teardown(Smem& S, uint32_t tbase) {
+template <typename SM>
+__device__ void teardown(SM& S, uint32_t tbase) {
   tc::fence_before();
   __syncthreads();
   tc::fence_after();
-  if (threadIdx.x < 32) tc::tmem_dealloc(tbase, kCols);
+  if (threadIdx.x < 32) tc::tmem_dealloc(tbase, SM::kTmemCols);
 }
 
 // Gradient of the mean BCE loss over `n_total` rows, accumulated into G (padded layout).
@@ -345,7 +380,7 @@ __global__ void __launch_bounds__(128) k_train(Weights W, const uint16_t* __rest
 __global__ void __launch_bounds__(128) k_predict(Weights W, const uint16_t* __restrict__ X, long n,
                                                  float* __restrict__ P, int* __restrict__ err) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
-  Smem& S = *reinterpret_cast<Smem*>(smem_raw);
+  SmemI& S = *reinterpret_cast<SmemI*>(smem_raw);
   setup(S, W);
   const uint32_t tbase = S.tmem;
   uint32_t phase = 0;
@@ -494,7 +529,7 @@ __global__ void __launch_bounds__(128) k_route_rows(Weights W, const uint4* __re
                                                     uint8_t* __restrict__ my, float zthr,
                                                     int* __restrict__ err) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
-  Smem& S = *reinterpret_cast<Smem*>(smem_raw);
+  SmemI& S = *reinterpret_cast<SmemI*>(smem_raw);
   const long n = long(min(*nrows, (unsigned long long)cap));
   const long ntiles = (n + 127) / 128;
   if (long(blockIdx.x) >= ntiles) return;  // uniform over the block; no tensor memory taken
@@ -618,9 +653,10 @@ int set_attr() {
   static int done = 0;
   if (done) return HTENO_OK;
   const int sm = int(mlp::smem_bytes());
+  const int smi = int(mlp::kSmemIBytes);
   if (cudaFuncSetAttribute(k_train, cudaFuncAttributeMaxDynamicSharedMemorySize, sm) != cudaSuccess ||
-      cudaFuncSetAttribute(k_predict, cudaFuncAttributeMaxDynamicSharedMemorySize, sm) != cudaSuccess ||
-      cudaFuncSetAttribute(k_route_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, sm) != cudaSuccess)
+      cudaFuncSetAttribute(k_predict, cudaFuncAttributeMaxDynamicSharedMemorySize, smi) != cudaSuccess ||
+      cudaFuncSetAttribute(k_route_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, smi) != cudaSuccess)
     return HTENO_ERR_CUDA;
   done = 1;
   return HTENO_OK;
@@ -678,7 +714,7 @@ int mlp_classify(hteno_mlp* m, const Geo& G, const double* q, uint8_t* mx, uint8
   cudaMemsetAsync(nrows, 0, sizeof(unsigned long long), st);
   k_route_prep<<<unsigned((nf + 255) / 256), 256, 0, st>>>(G, q, mx, my, rows, info, nrows, cap);
   const float zthr = std::log(thr / (1.0f - thr));  // sigmoid(z) > thr  <=>  z > logit(thr)
-  k_route_rows<<<2 * m->sms, 128, mlp::smem_bytes(), st>>>(m->W, rows, info, nrows, cap, nxf, mx, my,
+  k_route_rows<<<4 * m->sms, 128, mlp::kSmemIBytes, st>>>(m->W, rows, info, nrows, cap, nxf, mx, my,
                                                           zthr, m->err);
   return cudaGetLastError() == cudaSuccess ? HTENO_OK : HTENO_ERR_CUDA;
 }
@@ -836,8 +872,8 @@ int hteno_mlp_train(hteno_mlp* m, const uint16_t* x, const uint8_t* y, long n, i
 int hteno_mlp_predict(hteno_mlp* m, const uint16_t* x, long n, float* p) {
   if (!m || !x || n <= 0 || !p) return HTENO_ERR_INVALID_ARG;
   const long tiles = (n + 127) / 128;
-  const int grid = int(std::min<long>(tiles, 2L * m->sms));
-  k_predict<<<grid, 128, mlp::smem_bytes(), m->stream>>>(m->W, x, n, p, m->err);
+  const int grid = int(std::min<long>(tiles, 4L * m->sms));
+  k_predict<<<grid, 128, mlp::kSmemIBytes, m->stream>>>(m->W, x, n, p, m->err);
   const int rc = merr(m, cudaGetLastError(), "k_predict");
   return rc ? rc : check_err(m);
 }
