@@ -78,6 +78,30 @@ def test_gl3(hteno_lib, cuda, oracle, pw):
     close_scaled(oracle.gl3(pw["gl3_u"]), pw["gl3_out"], 1.0, 0.0)
 
 
+def test_gl3_bitwise_extreme_scales(hteno_lib, cuda, oracle):
+    """The FP64 GL3 divides by shared denominators through one correctly rounded reciprocal and a
+    remainder correction, with operands outside [2^-500, 2^501) sent to the division itself.
+    Stencils scaled from 1e-300 to 1e300, with zeros, negative zeros, subnormals and lone spikes,
+    reproduce the CPU oracle (plain IEEE division) bit for bit."""
+    rng = np.random.default_rng(17)
+    n = 40000
+    u = rng.normal(size=(n, 5)) * 10.0 ** rng.uniform(-300, 300, (n, 1))
+    u[:2000] = 0.0
+    u[2000:4000] = -0.0
+    u[4000:6000, 2] = rng.normal(size=2000) * 1e-310  # subnormal spikes on zero
+    u[6000:8000] = rng.normal(size=(2000, 5)) * 5e-324 * rng.integers(1, 50, (2000, 1))
+    spikes = rng.integers(0, 5, 4000)
+    u[8000:12000] = 0.0
+    u[8000 + np.arange(4000), spikes] = 10.0 ** rng.uniform(-200, 200, 4000)
+    u[12000:14000] = np.array([1.0, 1.0, 1.0, 1.0, 1.0]) * 10.0 ** rng.uniform(-250, 250, (2000, 1))
+    du = dev(cuda, u)
+    out = cuda.empty((n, 3), dtype=cuda.float64, device="cuda")
+    assert hteno_lib.lib().hteno_gl3_batch(0, du.data_ptr(), out.data_ptr(), n, None) == 0
+    cuda.cuda.synchronize()
+    got, want = out.cpu().numpy(), oracle.gl3(u)
+    np.testing.assert_array_equal(got.view(np.uint64), want.view(np.uint64))
+
+
 def test_hermite_recon_and_limiter(hteno_lib, cuda, oracle, pw):
     dx = float(pw["her_dx"])
     u, d = pw["her_u"], pw["her_d"]
