@@ -147,10 +147,8 @@ __device__ __forceinline__ int cutoff_pattern(const double* SI, double tau, doub
 }
 
 // One side of teno5 (:481-511) / teno5i (:1235-1263) given the candidates p and stencil v.
-__device__ __forceinline__ double teno_side(const DevConst& C, const double* p, const double* v,
-                                            int side, bool improved) {
-  double SI[3];
-  lagrange_si(v, SI);
+__device__ __forceinline__ double teno_side_si(const DevConst& C, const double* p, const double* v,
+                                               const double* SI, int side, bool improved) {
   // All three indicators exactly zero (constant data): the three ratios 1 + tau/(0 + epsz) are
   // equal whatever tau is, and the cut-off keeps all candidates (pattern 7) -- decided without
   // tau, same bits.  (Equal values alone do not suffice: 3u - 4u + u can leave a rounding
@@ -169,6 +167,12 @@ __device__ __forceinline__ double teno_side(const DevConst& C, const double* p, 
   const int pat = cutoff_pattern(SI, tau, HTENO_LAG_EPSZ, HTENO_LAG_CT);
   const double* w = side ? C.wtab_p[pat] : C.wtab_m[pat];
   return catchnan(dot3v(p, w));
+}
+__device__ __forceinline__ double teno_side(const DevConst& C, const double* p, const double* v,
+                                            int side, bool improved) {
+  double SI[3];
+  lagrange_si(v, SI);
+  return teno_side_si(C, p, v, SI, side, improved);
 }
 
 // ---- the selectable alternatives (Schemes_Lagrange.cpp:358-594, 1265-1294), one side each ----
@@ -275,13 +279,44 @@ __device__ __forceinline__ void lagrange_recon(const DevConst& C, int kind, cons
   p[0] = dot3(C.crj[0][1], C.crj[1][1], C.crj[2][1], u + 2);
   p[1] = dot3(C.crj[0][2], C.crj[1][2], C.crj[2][2], u + 1);
   p[2] = dot3(C.crj[0][3], C.crj[1][3], C.crj[2][3], u + 0);
-  outm = kind == 2 ? dot3v(p, C.dkm) : kind >= 3 ? alt_side(C, kind, p, u, 0)
-                                                 : teno_side(C, p, u, 0, kind == 1);
+  if (kind <= 1) {
+    // teno5 / teno5i: the two sides' windows overlap in 5 cells, so the + side reuses two of the
+    // - side's candidates (p1+ = p0-, p2+ = p1-) and two of its indicator terms: the same
+    // expressions on the same operands, the same bits
+    double c[4], SIm[3], SIp[3];
+    c[0] = u[2] - 2.0 * u[3] + u[4];
+    c[1] = u[1] - 2.0 * u[2] + u[3];
+    c[2] = u[0] - 2.0 * u[1] + u[2];
+    c[3] = u[3] - 2.0 * u[4] + u[5];  // c0 of the + side
+    double t[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) t[k] = (13.0 / 12.0) * c[k] * c[k];
+    double bm[3], bp[3];
+    bm[0] = (3.0 * u[2] - 4.0 * u[3] + u[4]) / 2.0;
+    bm[1] = (u[1] - u[3]) / 2.0;
+    bm[2] = (u[0] - 4.0 * u[1] + 3.0 * u[2]) / 2.0;
+    bp[0] = (3.0 * u[3] - 4.0 * u[4] + u[5]) / 2.0;
+    bp[1] = (u[2] - u[4]) / 2.0;
+    bp[2] = (u[1] - 4.0 * u[2] + 3.0 * u[3]) / 2.0;
+    SIm[0] = bm[0] * bm[0] + t[0];
+    SIm[1] = bm[1] * bm[1] + t[1];
+    SIm[2] = bm[2] * bm[2] + t[2];
+    SIp[0] = bp[0] * bp[0] + t[3];
+    SIp[1] = bp[1] * bp[1] + t[0];
+    SIp[2] = bp[2] * bp[2] + t[1];
+    outm = teno_side_si(C, p, u, SIm, 0, kind == 1);
+    double pp[3];
+    pp[0] = dot3(C.crj[0][0], C.crj[1][0], C.crj[2][0], u + 3);
+    pp[1] = p[0];
+    pp[2] = p[1];
+    outp = teno_side_si(C, pp, u + 1, SIp, 1, kind == 1);
+    return;
+  }
+  outm = kind == 2 ? dot3v(p, C.dkm) : alt_side(C, kind, p, u, 0);
   p[0] = dot3(C.crj[0][0], C.crj[1][0], C.crj[2][0], u + 3);
   p[1] = dot3(C.crj[0][1], C.crj[1][1], C.crj[2][1], u + 2);
   p[2] = dot3(C.crj[0][2], C.crj[1][2], C.crj[2][2], u + 1);
-  outp = kind == 2 ? dot3v(p, C.dkp) : kind >= 3 ? alt_side(C, kind, p, u + 1, 1)
-                                                 : teno_side(C, p, u + 1, 1, kind == 1);
+  outp = kind == 2 ? dot3v(p, C.dkp) : alt_side(C, kind, p, u + 1, 1);
 }
 
 // One side of lagrange_recon (side 0: u^-, side 1: u^+), the same arithmetic.
