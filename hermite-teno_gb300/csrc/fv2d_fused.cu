@@ -162,8 +162,8 @@ void fv2d_fused_step(hteno_solver* s, const Geo& G, double* qc) {
   if (s->router) {
     const int kc = trace_kind(s, "classify", 0.0, 0.0);
     trace_begin(s, kc);
-    mlp_classify(s->router, G, s->q, s->route_x, s->route_y, s->router_thr, s->route_rows,
-                 s->route_info, s->audit + 5, s->route_cap, s->stream);
+    mlp_classify(s->router, G, s->q, s->route_x, s->route_y, s->router_thr, s->route_rows, s->audit + 5,
+                 s->route_cap, s->stream);
     trace_end(s);
     const bool aud = s->audit_every > 0 && s->router_steps % s->audit_every == 0;
     for (fused::StageArgs* a : {&a1, &a2, &a3}) {
@@ -207,15 +207,16 @@ int hteno_set_router(hteno_solver* s, hteno_mlp* m, float threshold, int audit_e
     s->launches_per_step = 2 + 3;
     return HTENO_OK;
   }
+  const size_t bx = size_t(s->cfg.nx + 1) * s->cfg.ny, by = size_t(s->cfg.ny + 1) * s->cfg.nx;
+  if (bx + by >= (size_t(1) << 29))  // a network row carries (face << 3 | bit) in 32 bits
+    return set_error(s, HTENO_ERR_UNSUPPORTED, "learned routing takes grids of fewer than 2^29 faces");
   if (!s->route_x) {
-    const size_t bx = size_t(s->cfg.nx + 1) * s->cfg.ny, by = size_t(s->cfg.ny + 1) * s->cfg.nx;
-    // rows for the network: up to every stencil of every face, at most 64 M rows (1.5 GB)
-    s->route_cap = long(std::min<size_t>(8 * (bx + by), size_t(64) << 20));
+    // rows for the network: every stencil of every face, at most 256 M rows (4 GB)
+    s->route_cap = long(std::min<size_t>(8 * (bx + by), size_t(256) << 20));
     cudaError_t e = cudaMalloc(&s->route_x, (bx + 3) & ~size_t(3));
     if (e == cudaSuccess) e = cudaMalloc(&s->route_y, (by + 3) & ~size_t(3));
     if (e == cudaSuccess) e = cudaMalloc(&s->audit, 6 * sizeof(unsigned long long));
     if (e == cudaSuccess) e = cudaMalloc(&s->route_rows, size_t(s->route_cap) * sizeof(uint4));
-    if (e == cudaSuccess) e = cudaMalloc(&s->route_info, size_t(s->route_cap) * sizeof(unsigned long long));
     if (e != cudaSuccess) return cuda_error(s, e, "route masks");
   }
   cudaMemset(s->audit, 0, 6 * sizeof(unsigned long long));

@@ -81,10 +81,9 @@ struct hteno_solver {
   uint8_t* route_x = nullptr;
   uint8_t* route_y = nullptr;
   unsigned long long* audit = nullptr;  // [6]: seen, routed, misrouted, smooth, flat; rows asked
-  long audits = 0;
-  uint4* route_rows = nullptr;             // non-flat stencils handed to the network
-  unsigned long long* route_info = nullptr;
+  uint4* route_rows = nullptr;          // non-flat stencils handed to the network
   long route_cap = 0;
+  long audits = 0;
   bool strict = false;
   std::string err;
 

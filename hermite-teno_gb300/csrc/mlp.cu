@@ -52,20 +52,21 @@ struct Smem {
   float b1[32], b2[32], b3[16];
   float gb1[32], gb2[32], gb3[16];
   float loss;
-  float stage[16][24];  // classifier: the 6 cells x 4 conserved values of 16 faces
   alignas(8) uint64_t mbar;
   uint32_t tmem;
   static constexpr bool kTrain = true;
   static constexpr uint32_t kTmemCols = 256;
 };
 
-// Shared memory of the inference kernels (forward pass only).  The allocation is padded so that
-// at most 4 blocks share an SM, whose 4 x 128 tensor-memory columns are the SM's 512: twice the
-// blocks of the training layout, to overlap more of the layers' issue-wait-load round trips.
-struct SmemI {
-  alignas(128) unsigned char x[128 * 16 * 2];
-  alignas(128) unsigned char h1[128 * 32 * 2];
-  alignas(128) unsigned char h2[128 * 32 * 2];
+// Shared memory of the inference kernels (the forward pass only).  A CTA runs kCT tiles of 128
+// rows at once, so that each issue-wait-load round trip of a layer serves 512 rows; a tile's X,
+// H1 and H2 share one buffer (each is dead once the product that reads it has completed), and its
+// three accumulators share 32 tensor-memory columns.  The allocation is padded to 48 KB so that at
+// most 4 CTAs share an SM, whose 4 x 128 tensor-memory columns are the SM's 512.
+constexpr int kCT = 4;              // tiles per network round
+constexpr int kCRound = kCT * 128;  // rows per network round
+struct SmemC {
+  alignas(128) unsigned char buf[kCT][128 * 32 * 2];
   alignas(128) unsigned char w1[32 * 16 * 2];
   alignas(128) unsigned char w2[32 * 32 * 2];
   alignas(128) unsigned char w3[16 * 32 * 2];
@@ -75,12 +76,12 @@ struct SmemI {
   static constexpr bool kTrain = false;
   static constexpr uint32_t kTmemCols = 128;
 };
-constexpr size_t kSmemIBytes = 48 * 1024;
-static_assert(sizeof(SmemI) <= kSmemIBytes, "inference shared memory");
+constexpr size_t kSmemCBytes = 48 * 1024;
+static_assert(sizeof(SmemC) <= kSmemCBytes, "inference shared memory");
 
 // tensor-memory columns
 constexpr uint32_t C_D1 = 0, C_D2 = 32, C_D3 = 64, C_DH2 = 80, C_DH1 = 112;
-constexpr uint32_t C_GW3 = 144, C_GW2 = 176, C_GW1 = 208, kCols = 256;
+constexpr uint32_t C_GW3 = 144, C_GW2 = 176, C_GW1 = 208;
 
 __device__ __forceinline__ uint64_t desc_k(const unsigned char* base, int K, int kstep) {
   return tc::sdesc(tc::smem_u32(base) + uint32_t(kstep) * 256u, 128u, uint32_t(K / 8) * 128u);
@@ -193,6 +194,89 @@ __device__ __forceinline__ bool forward(SM& S, uint32_t tbase, uint32_t& phase, 
   tc::tmem_ld16(lane_addr + C_D3, d3);
 #pragma unroll
   for (int k = 0; k < 3; ++k) z3[k] = d3[k] + S.b3[k];
+  return true;
+}
+
+// Two floats -> two BF16 (round to nearest even) with negative results clamped to +0: ReLU then
+// rounding, in one instruction.  lo goes to the lower address.
+__device__ __forceinline__ uint32_t pack_relu(float lo, float hi) {
+  uint32_t d;
+  asm("cvt.rn.relu.bf16x2.f32 %0, %1, %2;" : "=r"(d) : "f"(hi), "f"(lo));
+  return d;
+}
+
+// Bias, ReLU and BF16 rounding of this thread's 32-column accumulator row, stored as its row of
+// the next layer's A operand (four 16-byte rows of K-major core matrices).
+__device__ __forceinline__ void hidden_row(uint32_t taddr, const float* b, unsigned char* dst, int row) {
+  float h[32];
+  tc::tmem_ld16(taddr, h);
+  tc::tmem_ld16(taddr + 16, h + 16);
+#pragma unroll
+  for (int g = 0; g < 4; ++g) {
+    uint32_t w[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int c = 8 * g + 2 * j;
+      w[j] = pack_relu(h[c] + b[c], h[c + 1] + b[c + 1]);
+    }
+    *reinterpret_cast<uint4*>(dst + tc::kmaj(row, 8 * g, 32)) = make_uint4(w[0], w[1], w[2], w[3]);
+  }
+}
+
+// Forward pass of up to kCT tiles at once (inference): thread r holds row r of tile t in in[t]
+// (6 BF16 features in .x .y .z); n valid rows in all, tiles beyond them are not computed.  Leaves
+// the three output logits of each of its rows in z.  Returns false on a timed-out wait (uniform).
+__device__ __forceinline__ bool forward_rows(SmemC& S, uint32_t tbase, uint32_t& phase, const uint4* in,
+                                             int n, float (*z)[3]) {
+  const int row = threadIdx.x;
+  const int ntile = (n + 127) >> 7;
+  const uint32_t lane_addr = tbase + (uint32_t(threadIdx.x & ~31) << 16);
+#pragma unroll
+  for (int t = 0; t < kCT; ++t)
+    if (t < ntile) {
+      *reinterpret_cast<uint4*>(S.buf[t] + tc::kmaj(row, 0, 16)) = make_uint4(in[t].x, in[t].y, in[t].z, 0u);
+      *reinterpret_cast<uint4*>(S.buf[t] + tc::kmaj(row, 8, 16)) = make_uint4(0u, 0u, 0u, 0u);
+    }
+  before_issue();
+  if (threadIdx.x == 0) {
+    tc::fence_after();
+    for (int t = 0; t < ntile; ++t)
+      tc::mma_bf16(tbase + 32 * t, desc_k(S.buf[t], 16, 0), desc_k(S.w1, 16, 0), tc::idesc_bf16(128, 32), 0);
+    tc::commit(&S.mbar);
+  }
+  if (!wait_mma(S, phase)) return false;
+#pragma unroll
+  for (int t = 0; t < kCT; ++t)
+    if (t < ntile) hidden_row(lane_addr + 32 * t, S.b1, S.buf[t], row);
+  before_issue();
+  if (threadIdx.x == 0) {
+    tc::fence_after();
+    for (int t = 0; t < ntile; ++t)
+      for (int k = 0; k < 2; ++k)
+        tc::mma_bf16(tbase + 32 * t, desc_k(S.buf[t], 32, k), desc_k(S.w2, 32, k), tc::idesc_bf16(128, 32), k);
+    tc::commit(&S.mbar);
+  }
+  if (!wait_mma(S, phase)) return false;
+#pragma unroll
+  for (int t = 0; t < kCT; ++t)
+    if (t < ntile) hidden_row(lane_addr + 32 * t, S.b2, S.buf[t], row);
+  before_issue();
+  if (threadIdx.x == 0) {
+    tc::fence_after();
+    for (int t = 0; t < ntile; ++t)
+      for (int k = 0; k < 2; ++k)
+        tc::mma_bf16(tbase + 32 * t, desc_k(S.buf[t], 32, k), desc_k(S.w3, 32, k), tc::idesc_bf16(128, 16), k);
+    tc::commit(&S.mbar);
+  }
+  if (!wait_mma(S, phase)) return false;
+#pragma unroll
+  for (int t = 0; t < kCT; ++t)
+    if (t < ntile) {
+      float d3[16];
+      tc::tmem_ld16(lane_addr + 32 * t, d3);
+#pragma unroll
+      for (int k = 0; k < 3; ++k) z[t][k] = d3[k] + S.b3[k];
+    }
   return true;
 }
 
@@ -376,29 +460,34 @@ __global__ void __launch_bounds__(128) k_train(Weights W, const uint16_t* __rest
   teardown(S, tbase);
 }
 
-// Probabilities of the three cut-off bits for n rows.
-__global__ void __launch_bounds__(128) k_predict(Weights W, const uint16_t* __restrict__ X, long n,
-                                                 float* __restrict__ P, int* __restrict__ err) {
+// Probabilities of the three cut-off bits for n rows (rounds of kCRound rows per CTA).
+__global__ void __launch_bounds__(128, 4) k_predict(Weights W, const uint16_t* __restrict__ X, long n,
+                                                    float* __restrict__ P, int* __restrict__ err) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
-  SmemI& S = *reinterpret_cast<SmemI*>(smem_raw);
+  SmemC& S = *reinterpret_cast<SmemC*>(smem_raw);
   setup(S, W);
   const uint32_t tbase = S.tmem;
   uint32_t phase = 0;
   bool ok = true;
-  const long ntiles = (n + 127) / 128;
-  for (long t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
-    const long r = t * 128 + threadIdx.x;
-    uint16_t f[6] = {0, 0, 0, 0, 0, 0};
-    if (r < n) {
-      const uint4 raw = *reinterpret_cast<const uint4*>(X + r * 8);
-      const uint16_t* p = reinterpret_cast<const uint16_t*>(&raw);
-      for (int k = 0; k < 6; ++k) f[k] = p[k];
+  const long nround = (n + kCRound - 1) / kCRound;
+  for (long rd = blockIdx.x; rd < nround && ok; rd += gridDim.x) {
+    const long base = rd * kCRound;
+    const int m = int(n - base < kCRound ? n - base : kCRound);
+    uint4 in[kCT];
+    float z[kCT][3];
+#pragma unroll
+    for (int t = 0; t < kCT; ++t) {
+      const int k = t * 128 + int(threadIdx.x);
+      in[t] = k < m ? *reinterpret_cast<const uint4*>(X + (base + k) * 8) : make_uint4(0u, 0u, 0u, 0u);
     }
-    put_input(S, threadIdx.x, f);
-    float h1[32], h2[32], z3[3];
-    ok = forward(S, tbase, phase, h1, h2, z3, false);
-    if (ok && r < n)
-      for (int k = 0; k < 3; ++k) P[r * 3 + k] = 1.0f / (1.0f + __expf(-z3[k]));
+    ok = forward_rows(S, tbase, phase, in, m, z);
+    if (ok)
+#pragma unroll
+      for (int t = 0; t < kCT; ++t) {
+        const int k = t * 128 + int(threadIdx.x);
+        if (k < m)
+          for (int j = 0; j < 3; ++j) P[(base + k) * 3 + j] = 1.0f / (1.0f + __expf(-z[t][j]));
+      }
   }
   if (!ok) {
     if (threadIdx.x == 0) atomicExch(err, 1);
@@ -407,92 +496,137 @@ __global__ void __launch_bounds__(128) k_predict(Weights W, const uint16_t* __re
   teardown(S, tbase);
 }
 
-// Learned routing of a mixed FV 2D grid, pass 1: one thread per face (x faces, then y faces)
-// computes the 8 stencils the fused kernel will reconstruct (4 characteristic fields x 2 sides,
-// float, from the double state as the fused kernel sees it) and clears the face's mask byte.
-// Flat stencils (six equal float values) are left alone: the stage kernel takes the linear
-// weights for flat windows by itself.  The others are appended, normalised and in BF16, to the
-// row list for the network, with (face << 3 | bit) beside each.  Appends are aggregated per
-// block: one atomic per block.
-__global__ void __launch_bounds__(256) k_route_prep(Geo G, const double* __restrict__ q,
-                                                    uint8_t* __restrict__ mx, uint8_t* __restrict__ my,
+// The non-flat stencils of one face of a mixed FV 2D grid, as network rows: the 8 stencils the
+// fused stage kernel reconstructs (4 characteristic fields x 2 sides, float, from the double
+// state as that kernel sees it), each normalised to [-1, 1] in BF16, with (face << 3 | bit) in
+// .w (bit = 2 * field + side).  cq: the 6 cells' conserved values; cp: u, v, H and sqrt|rho| of
+// the face's two cells.  Stencils whose six float values are equal are flat and left out: the
+// stage kernel takes the linear weights for flat windows by itself.  Returns the bit mask of the
+// rows written.
+__device__ __forceinline__ uint32_t stencil_rows(float g1, int dir, const float (&cq)[6][4],
+                                                 const float (&cp)[2][4], uint32_t face, uint4 (&row)[8]) {
+  const Roe2<float> R = roe2<float>(g1, cp[0][3], cp[0][0], cp[0][1], cp[0][2], cp[1][3], cp[1][0],
+                                    cp[1][1], cp[1][2]);
+  float ch[4][6];
+#pragma unroll
+  for (int m = 0; m < 6; ++m) {
+    float cc[4];
+    roe_left(R, dir, cq[m], cc);
+#pragma unroll
+    for (int r = 0; r < 4; ++r) ch[r][m] = cc[r];
+  }
+  uint32_t keep = 0;
+#pragma unroll
+  for (int b = 0; b < 8; ++b) {
+    const int r = b >> 1, side = b & 1;
+    float w[6];
+#pragma unroll
+    for (int m = 0; m < 6; ++m) w[side ? 5 - m : m] = ch[r][m];
+    float mean = 0.f, hi = w[0], lo = w[0];
+#pragma unroll
+    for (int m = 0; m < 6; ++m) {
+      mean += w[m];
+      hi = fmaxf(hi, w[m]);
+      lo = fminf(lo, w[m]);
+    }
+    row[b] = make_uint4(0u, 0u, 0u, 0u);
+    if (hi == lo) continue;
+    mean *= (1.0f / 6.0f);
+    const float inv = 1.0f / (hi - lo);
+    uint32_t f[6];
+#pragma unroll
+    for (int m = 0; m < 6; ++m) {
+      const __nv_bfloat16 bv = __float2bfloat16_rn(fminf(1.f, fmaxf(-1.f, (w[m] - mean) * inv)));
+      f[m] = *reinterpret_cast<const uint16_t*>(&bv);
+    }
+    row[b] = make_uint4(f[0] | (f[1] << 16), f[2] | (f[3] << 16), f[4] | (f[5] << 16), face << 3 | uint32_t(b));
+    keep |= 1u << b;
+  }
+  return keep;
+}
+
+// Faces per block of the routing pass: A along the sweep direction x B lines across it.
+template <int DIR>
+struct RouteTile {
+  static constexpr int A = DIR == 1 ? 64 : 8, B = DIR == 1 ? 4 : 32;
+};
+
+// Learned routing of a mixed FV 2D grid, pass 1 (masks zeroed beforehand), one launch per
+// direction: a block stages the float conserved values and the primitives (u, v, H, sqrt|rho|)
+// of its (A + 5) x B cells in shared memory (each cell converted once), then one thread per face
+// appends the face's non-flat stencils to the row list; appends are aggregated per block, one
+// atomic per block.  A face whose six cells are equal has only flat stencils and is skipped
+// before its eigenvectors.  Rows beyond `cap` are dropped (their stencils keep full TENO).
+template <int DIR>
+__global__ void __launch_bounds__(256) k_route_prep(Geo G, const double* __restrict__ q, int tiles_a,
                                                     uint4* __restrict__ rows,
-                                                    unsigned long long* __restrict__ info,
                                                     unsigned long long* __restrict__ nrows, long cap) {
+  constexpr int A = RouteTile<DIR>::A, B = RouteTile<DIR>::B, L = A + 5, NC = L * B;
+  static_assert(A * B == 256, "one face per thread");
+  __shared__ float sq[4][NC];  // conserved values, float
+  __shared__ float sp[4][NC];  // u, v, H, sqrt|rho|
   __shared__ int warp_tot[8];
   __shared__ unsigned long long block_base;
   const size_t nc = size_t(G.nx) * G.ny;
-  const long nxf = long(G.nx + 1) * G.ny, nyf = long(G.ny + 1) * G.nx, nf = nxf + nyf;
-  const long face = blockIdx.x * long(blockDim.x) + threadIdx.x;
   const float g1 = float(G.g1);
-  uint4 row[8];
-  int nmine = 0;
-  uint8_t byte = 0;
-  if (face < nf) {
-    int dir = 1, fi, tt;
-    if (face < nxf) {
-      fi = int(face % (G.nx + 1));
-      tt = int(face / (G.nx + 1));
-    } else {
-      const long k = face - nxf;
-      dir = 2;
-      fi = int(k / G.nx);
-      tt = int(k % G.nx);
+  const int n_along = DIR == 1 ? G.nx : G.ny, n_across = DIR == 1 ? G.ny : G.nx;
+  const int f0 = int(blockIdx.x % unsigned(tiles_a)) * A, l0 = int(blockIdx.x / unsigned(tiles_a)) * B;
+  // staged cell e: along index f0 - 3 + a, line l0 + b; e = b * L + a (x) or a * B + b (y), so
+  // that consecutive e are consecutive in memory
+  for (int e = threadIdx.x; e < NC; e += 256) {
+    const int a = DIR == 1 ? e % L : e / B, b = DIR == 1 ? e / L : e % B;
+    const int line = min(l0 + b, n_across - 1);  // lines past the grid: their faces are not listed
+    const int ia = fused::cmap(f0 - 3 + a, n_along, G.bc);
+    const size_t k = DIR == 1 ? size_t(line) * G.nx + ia : size_t(ia) * G.nx + line;
+    float c[4];
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      c[v] = fused::d2f(__ldg(q + v * nc + k));
+      sq[v][e] = c[v];
     }
-    float cq[6][4];
-    for (int m = 0; m < 6; ++m) {
-      const int sidx = fused::cmap(fi - 3 + m, dir == 1 ? G.nx : G.ny, G.bc);
-      const size_t k = dir == 1 ? size_t(tt) * G.nx + sidx : size_t(sidx) * G.nx + tt;
-      for (int v = 0; v < 4; ++v) cq[m][v] = fused::d2f(__ldg(q + v * nc + k));
-    }
-    float cp[2][4];
-    for (int h = 0; h < 2; ++h) {  // primitives of the two cells of the face
-      const float* c = cq[2 + h];
-      const float ir = __frcp_rn(c[0]);
-      const float u = c[1] * ir, v = c[2] * ir;
-      const float p = (c[3] - 0.5f * (c[1] * u + c[2] * v)) * g1;
-      cp[h][0] = u;
-      cp[h][1] = v;
-      cp[h][2] = (c[3] + p) * ir;
-      cp[h][3] = sqrtf(fabsf(c[0]));
-    }
-    const Roe2<float> R = roe2<float>(g1, cp[0][3], cp[0][0], cp[0][1], cp[0][2], cp[1][3], cp[1][0],
-                                      cp[1][1], cp[1][2]);
-    float ch[4][6];
-    for (int m = 0; m < 6; ++m) {
-      float cc[4];
-      roe_left(R, dir, cq[m], cc);
-      for (int r = 0; r < 4; ++r) ch[r][m] = cc[r];
-    }
-    for (int b = 0; b < 8; ++b) {
-      const int r = b >> 1, side = b & 1;
-      float w[6];
-      for (int m = 0; m < 6; ++m) w[side ? 5 - m : m] = ch[r][m];
-      float mean = 0.f, hi = w[0], lo = w[0];
-      for (int m = 0; m < 6; ++m) {
-        mean += w[m];
-        hi = fmaxf(hi, w[m]);
-        lo = fminf(lo, w[m]);
-      }
-      if (hi == lo) continue;  // flat in float: the stage kernel takes the linear weights itself
-      mean *= (1.0f / 6.0f);
-      const float inv = 1.0f / (hi - lo);
-      uint16_t f[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-      for (int m = 0; m < 6; ++m) {
-        const __nv_bfloat16 bv = __float2bfloat16_rn(fminf(1.f, fmaxf(-1.f, (w[m] - mean) * inv)));
-        f[m] = *reinterpret_cast<const uint16_t*>(&bv);
-      }
-      row[nmine] = make_uint4(f[0] | (uint32_t(f[1]) << 16), f[2] | (uint32_t(f[3]) << 16),
-                              f[4] | (uint32_t(f[5]) << 16), 0u);
-      row[nmine].w = uint32_t(b);  // temporarily: the bit (the pad column is rewritten below)
-      ++nmine;
-    }
-    if (face < nxf) mx[face] = byte;
-    else my[face - nxf] = byte;
+    const float ir = __frcp_rn(c[0]);
+    const float u = c[1] * ir, v = c[2] * ir;
+    const float p = (c[3] - 0.5f * (c[1] * u + c[2] * v)) * g1;
+    sp[0][e] = u;
+    sp[1][e] = v;
+    sp[2][e] = (c[3] + p) * ir;
+    sp[3][e] = sqrtf(fabsf(c[0]));
   }
-  // block-aggregated append
+  __syncthreads();
+  const int fa = DIR == 1 ? int(threadIdx.x) % A : int(threadIdx.x) / B;
+  const int fb = DIR == 1 ? int(threadIdx.x) / A : int(threadIdx.x) % B;
+  const int fi = f0 + fa, line = l0 + fb;
+  uint4 row[8];
+  uint32_t keep = 0;
+  if (fi <= n_along && line < n_across) {
+    float cq[6][4];
+    bool same = true;
+#pragma unroll
+    for (int m = 0; m < 6; ++m) {
+      const int e = DIR == 1 ? fb * L + fa + m : (fa + m) * B + fb;
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        cq[m][v] = sq[v][e];
+        same = same && cq[m][v] == cq[0][v];
+      }
+    }
+    if (!same) {
+      float cp[2][4];
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int e = DIR == 1 ? fb * L + fa + 2 + h : (fa + 2 + h) * B + fb;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) cp[h][k] = sp[k][e];
+      }
+      const long nxf = long(G.nx + 1) * G.ny;
+      const long face = DIR == 1 ? long(line) * (G.nx + 1) + fi : nxf + long(fi) * G.nx + line;
+      keep = stencil_rows(g1, DIR, cq, cp, uint32_t(face), row);
+    }
+  }
+  const int nmine = __popc(keep);
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   int incl = nmine;
+#pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
     const int v = __shfl_up_sync(0xffffffffu, incl, o);
     if (lane >= o) incl += v;
@@ -501,7 +635,7 @@ __global__ void __launch_bounds__(256) k_route_prep(Geo G, const double* __restr
   __syncthreads();
   if (threadIdx.x == 0) {
     int tot = 0;
-    for (int w = 0; w < int(blockDim.x >> 5); ++w) {
+    for (int w = 0; w < 8; ++w) {
       const int t = warp_tot[w];
       warp_tot[w] = tot;
       tot += t;
@@ -510,51 +644,52 @@ __global__ void __launch_bounds__(256) k_route_prep(Geo G, const double* __restr
   }
   __syncthreads();
   const unsigned long long base = block_base + warp_tot[wid] + (incl - nmine);
-  for (int k = 0; k < nmine; ++k) {
-    const unsigned long long slot = base + k;
-    if (slot >= (unsigned long long)cap) break;  // beyond capacity: left unrouted (full TENO)
-    const uint32_t bit = row[k].w;
-    row[k].w = 0u;
-    rows[slot] = row[k];
-    info[slot] = (unsigned long long)(face) << 3 | bit;
-  }
+#pragma unroll
+  for (int b = 0; b < 8; ++b)
+    if (keep >> b & 1u) {
+      const unsigned long long slot = base + __popc(keep & ((1u << b) - 1u));
+      if (slot < (unsigned long long)cap) rows[slot] = row[b];
+    }
 }
 
-// Pass 2: the network over the appended rows; a row whose three probabilities all exceed the
-// threshold sets its bit in the face's mask byte.
-__global__ void __launch_bounds__(128) k_route_rows(Weights W, const uint4* __restrict__ rows,
-                                                    const unsigned long long* __restrict__ info,
-                                                    const unsigned long long* __restrict__ nrows, long cap,
-                                                    long nxf, uint8_t* __restrict__ mx,
-                                                    uint8_t* __restrict__ my, float zthr,
-                                                    int* __restrict__ err) {
+// Pass 2: the network over the appended rows, in rounds of kCRound rows per CTA; a row whose three
+// logits all exceed zthr sets its bit in its face's mask byte.
+__global__ void __launch_bounds__(128, 4) k_route_rows(Weights W, const uint4* __restrict__ rows,
+                                                       const unsigned long long* __restrict__ nrows,
+                                                       long cap, long nxf, uint8_t* __restrict__ mx,
+                                                       uint8_t* __restrict__ my, float zthr,
+                                                       int* __restrict__ err) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
-  SmemI& S = *reinterpret_cast<SmemI*>(smem_raw);
+  SmemC& S = *reinterpret_cast<SmemC*>(smem_raw);
   const long n = long(min(*nrows, (unsigned long long)cap));
-  const long ntiles = (n + 127) / 128;
-  if (long(blockIdx.x) >= ntiles) return;  // uniform over the block; no tensor memory taken
+  const long nround = (n + kCRound - 1) / kCRound;
+  if (long(blockIdx.x) >= nround) return;  // uniform over the block; no tensor memory taken
   setup(S, W);
   const uint32_t tbase = S.tmem;
   uint32_t phase = 0;
   bool ok = true;
-  for (long t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
-    const long r = t * 128 + threadIdx.x;
-    uint16_t f[6] = {0, 0, 0, 0, 0, 0};
-    if (r < n) {
-      const uint4 raw = rows[r];
-      const uint16_t* p = reinterpret_cast<const uint16_t*>(&raw);
-      for (int k = 0; k < 6; ++k) f[k] = p[k];
+  for (long rd = blockIdx.x; rd < nround && ok; rd += gridDim.x) {
+    const long base = rd * kCRound;
+    const int m = int(n - base < kCRound ? n - base : kCRound);
+    uint4 in[kCT];
+    float z[kCT][3];
+#pragma unroll
+    for (int t = 0; t < kCT; ++t) {
+      const int k = t * 128 + int(threadIdx.x);
+      in[t] = k < m ? rows[base + k] : make_uint4(0u, 0u, 0u, 0u);
     }
-    put_input(S, threadIdx.x, f);
-    float h1[32], h2[32], z3[3];
-    ok = forward(S, tbase, phase, h1, h2, z3, false);
-    if (ok && r < n && z3[0] > zthr && z3[1] > zthr && z3[2] > zthr) {
-      const unsigned long long in = info[r];
-      const long face = long(in >> 3);
-      uint8_t* m = face < nxf ? mx + face : my + (face - nxf);
-      const size_t a = reinterpret_cast<size_t>(m);
-      atomicOr(reinterpret_cast<unsigned int*>(a & ~size_t(3)), (1u << (in & 7)) << (8 * (a & 3)));
-    }
+    ok = forward_rows(S, tbase, phase, in, m, z);
+    if (ok)
+#pragma unroll
+      for (int t = 0; t < kCT; ++t) {
+        const int k = t * 128 + int(threadIdx.x);
+        if (k < m && z[t][0] > zthr && z[t][1] > zthr && z[t][2] > zthr) {
+          const long face = long(in[t].w >> 3);
+          uint8_t* mk = face < nxf ? mx + face : my + (face - nxf);
+          const size_t a = reinterpret_cast<size_t>(mk);
+          atomicOr(reinterpret_cast<unsigned int*>(a & ~size_t(3)), (1u << (in[t].w & 7u)) << (8 * (a & 3)));
+        }
+      }
   }
   if (!ok) {
     if (threadIdx.x == 0) atomicExch(err, 1);
@@ -653,10 +788,10 @@ int set_attr() {
   static int done = 0;
   if (done) return HTENO_OK;
   const int sm = int(mlp::smem_bytes());
-  const int smi = int(mlp::kSmemIBytes);
+  const int smc = int(mlp::kSmemCBytes);
   if (cudaFuncSetAttribute(k_train, cudaFuncAttributeMaxDynamicSharedMemorySize, sm) != cudaSuccess ||
-      cudaFuncSetAttribute(k_predict, cudaFuncAttributeMaxDynamicSharedMemorySize, smi) != cudaSuccess ||
-      cudaFuncSetAttribute(k_route_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, smi) != cudaSuccess)
+      cudaFuncSetAttribute(k_predict, cudaFuncAttributeMaxDynamicSharedMemorySize, smc) != cudaSuccess ||
+      cudaFuncSetAttribute(k_route_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, smc) != cudaSuccess)
     return HTENO_ERR_CUDA;
   done = 1;
   return HTENO_OK;
@@ -705,17 +840,26 @@ int refresh_images(hteno_mlp* m) {
 
 namespace hteno {
 
-// Route masks of a mixed FV 2D grid from its current state (k_route_prep, then k_route_rows on
-// the non-flat stencils).  rows/info/nrows: scratch of `cap` rows owned by the caller.
+// Route masks of a mixed FV 2D grid from its current state: the masks are zeroed, k_route_prep
+// (x faces, then y faces) lists the non-flat stencils (at most `cap` rows, scratch owned by the caller), k_route_rows runs
+// the network on them.  *nrows receives the number of non-flat stencils.
 int mlp_classify(hteno_mlp* m, const Geo& G, const double* q, uint8_t* mx, uint8_t* my, float thr,
-                 uint4* rows, unsigned long long* info, unsigned long long* nrows, long cap,
-                 cudaStream_t st) {
-  const long nxf = long(G.nx + 1) * G.ny, nf = nxf + long(G.ny + 1) * G.nx;
+                 uint4* rows, unsigned long long* nrows, long cap, cudaStream_t st) {
+  const long nxf = long(G.nx + 1) * G.ny, nyf = long(G.ny + 1) * G.nx;
+  cudaMemsetAsync(mx, 0, size_t(nxf), st);
+  cudaMemsetAsync(my, 0, size_t(nyf), st);
   cudaMemsetAsync(nrows, 0, sizeof(unsigned long long), st);
-  k_route_prep<<<unsigned((nf + 255) / 256), 256, 0, st>>>(G, q, mx, my, rows, info, nrows, cap);
+  {
+    using T1 = RouteTile<1>;
+    using T2 = RouteTile<2>;
+    const int ta1 = (G.nx + 1 + T1::A - 1) / T1::A, tb1 = (G.ny + T1::B - 1) / T1::B;
+    const int ta2 = (G.ny + 1 + T2::A - 1) / T2::A, tb2 = (G.nx + T2::B - 1) / T2::B;
+    k_route_prep<1><<<unsigned(ta1) * unsigned(tb1), 256, 0, st>>>(G, q, ta1, rows, nrows, cap);
+    k_route_prep<2><<<unsigned(ta2) * unsigned(tb2), 256, 0, st>>>(G, q, ta2, rows, nrows, cap);
+  }
   const float zthr = std::log(thr / (1.0f - thr));  // sigmoid(z) > thr  <=>  z > logit(thr)
-  k_route_rows<<<4 * m->sms, 128, mlp::kSmemIBytes, st>>>(m->W, rows, info, nrows, cap, nxf, mx, my,
-                                                          zthr, m->err);
+  k_route_rows<<<4 * m->sms, 128, mlp::kSmemCBytes, st>>>(m->W, rows, nrows, cap, nxf, mx, my, zthr,
+                                                          m->err);
   return cudaGetLastError() == cudaSuccess ? HTENO_OK : HTENO_ERR_CUDA;
 }
 
@@ -871,9 +1015,9 @@ int hteno_mlp_train(hteno_mlp* m, const uint16_t* x, const uint8_t* y, long n, i
 // Probabilities of the three cut-off bits: x device bf16 [n][8] -> p device float [n][3].
 int hteno_mlp_predict(hteno_mlp* m, const uint16_t* x, long n, float* p) {
   if (!m || !x || n <= 0 || !p) return HTENO_ERR_INVALID_ARG;
-  const long tiles = (n + 127) / 128;
-  const int grid = int(std::min<long>(tiles, 4L * m->sms));
-  k_predict<<<grid, 128, mlp::kSmemIBytes, m->stream>>>(m->W, x, n, p, m->err);
+  const long rounds = (n + mlp::kCRound - 1) / mlp::kCRound;
+  const int grid = int(std::min<long>(rounds, 4L * m->sms));
+  k_predict<<<grid, 128, mlp::kSmemCBytes, m->stream>>>(m->W, x, n, p, m->err);
   const int rc = merr(m, cudaGetLastError(), "k_predict");
   return rc ? rc : check_err(m);
 }

@@ -108,7 +108,6 @@ void release(hteno_solver* s) {
   cudaFree(s->route_rows);
   cudaFree(s->deep);
   cudaFree(s->ghost_faces);
-  cudaFree(s->route_info);
   cudaFree(s->q);
   cudaFree(s->q0);
   cudaFree(s->v);
