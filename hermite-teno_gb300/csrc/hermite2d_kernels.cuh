@@ -19,7 +19,8 @@ constexpr int kHFluxThreads = 64;
 struct GeoH {
   int nx, ny;
   double dx, dy, area, gamma, g1, g3;  // g3 = gamma - 3 as the reference computes it
-  double rdx, rdy;                     // 1/dx, 1/dy (mixed-precision update)
+  double rdx, rdy;                     // 1/dx, 1/dy
+  float rdxf, rdyf;                    // the same in float (mixed-precision update)
 };
 
 // Loads of the double state into the compute type and back: for float on the integer pipes
@@ -529,8 +530,16 @@ template <typename T, int DIR>
 __global__ void __launch_bounds__(kHFluxThreads) kh_flux(GeoH G, const T* __restrict__ fc,
                                                         const T* __restrict__ froe,
                                                         T* __restrict__ F, const StepState* st) {
-  // GL3 values of the 24 face arrays at the 3 Gauss points, per thread, in shared memory
-  __shared__ T sg[kHFluxThreads][24][3];
+  // GL3 values of the 24 face arrays at the 3 Gauss points, per thread, in shared memory: for
+  // float [array][point][thread] (a warp's accesses fall in 32 distinct banks); for double
+  // [thread][array][point] with a one-value pad per thread (par::gl3 writes 3 contiguous values;
+  // the odd stride of 73 values spreads a warp's 8-byte accesses over all banks)
+  constexpr int kSgT = std::is_same<T, double>::value ? 73 : 72;
+  __shared__ T sg[kHFluxThreads * kSgT];
+  auto gat = [&](int a, int m) -> T& {
+    if constexpr (std::is_same<T, double>::value) return sg[threadIdx.x * kSgT + a * 3 + m];
+    else return sg[(a * 3 + m) * kHFluxThreads + threadIdx.x];
+  };
   if (st && st->done) return;
   const int nf = DIR == 1 ? G.nx + 1 : G.ny + 1;
   const int nt = DIR == 1 ? G.ny : G.nx;
@@ -550,13 +559,12 @@ __global__ void __launch_bounds__(kHFluxThreads) kh_flux(GeoH G, const T* __rest
   size_t nb[5];
 #pragma unroll
   for (int m = 0; m < 5; ++m) nb[m] = fidx(t - 2 + m);
-  T (*g)[3] = sg[threadIdx.x];
   for (int a = 0; a < 24; ++a) {
     T u5[5];
 #pragma unroll
     for (int m = 0; m < 5; ++m) u5[m] = fc[size_t(a) * nface + nb[m]];
-    if constexpr (std::is_same<T, double>::value) par::gl3(c_dev, u5, g[a]);
-    else gl3(c_dev, u5, g[a][0], g[a][1], g[a][2]);
+    if constexpr (std::is_same<T, double>::value) par::gl3(c_dev, u5, &gat(a, 0));
+    else gl3(c_dev, u5, gat(a, 0), gat(a, 1), gat(a, 2));
   }
   const size_t o = nb[2];
   T acc[12];
@@ -579,7 +587,7 @@ __global__ void __launch_bounds__(kHFluxThreads) kh_flux(GeoH G, const T* __rest
     for (int m = 0; m < 3; ++m) {
       double X[6][4];
       for (int a = 0; a < 6; ++a) {
-        const double c[4] = {g[4 * a + 0][m], g[4 * a + 1][m], g[4 * a + 2][m], g[4 * a + 3][m]};
+        const double c[4] = {gat(4 * a + 0, m), gat(4 * a + 1, m), gat(4 * a + 2, m), gat(4 * a + 3, m)};
         par::right(E, DIR, c, X[a]);
       }
       double fu[4], fn[4], ft[4];
@@ -608,7 +616,7 @@ __global__ void __launch_bounds__(kHFluxThreads) kh_flux(GeoH G, const T* __rest
       T X[6][4];
 #pragma unroll
       for (int a = 0; a < 6; ++a) {
-        T c[4] = {g[4 * a + 0][m], g[4 * a + 1][m], g[4 * a + 2][m], g[4 * a + 3][m]};
+        T c[4] = {gat(4 * a + 0, m), gat(4 * a + 1, m), gat(4 * a + 2, m), gat(4 * a + 3, m)};
         roe_right(R, DIR, c, X[a]);
       }
       T fu[4], fn[4], ft[4];
@@ -649,12 +657,15 @@ __global__ void kh_update(GeoH G, int stage, const T* __restrict__ fx, const T* 
     const double dt = st->dt;
     double qn[4];
     if constexpr (std::is_same<T, float>::value) {
-      // mixed precision: float flux differences are exact in double; RK stage with FMAs; the
-      // conversions on the integer pipes; primitives with a refined float reciprocal of rho
+      // mixed precision: the residual from the float fluxes in float (a difference of two
+      // nearby fluxes is exact in float; otherwise its rounding is far below the fluxes' own),
+      // the RK stage in double with FMAs; the conversions on the integer pipes; primitives with
+      // a refined float reciprocal of rho.  The FP64 pipe (1/64 of the float rate) does only
+      // the accumulation and the primitives.
       auto rhs = [&](int kx, int ky, int e) {
-        const double dfx = mix::f2d(fx[(kx + e) * nxf + ox]) - mix::f2d(fx[(kx + e) * nxf + ox + 1]);
-        const double dfy = mix::f2d(fy[(ky + e) * nyf + oy]) - mix::f2d(fy[(ky + e) * nyf + oy + G.nx]);
-        return fma(dfx, G.rdx, dfy * G.rdy);
+        const float dfx = fx[(kx + e) * nxf + ox] - fx[(kx + e) * nxf + ox + 1];
+        const float dfy = fy[(ky + e) * nyf + oy] - fy[(ky + e) * nyf + oy + G.nx];
+        return mix::f2d(fmaf(dfx, G.rdxf, dfy * G.rdyf));
       };
 #pragma unroll
       for (int e = 0; e < 4; ++e) {
@@ -751,6 +762,8 @@ GeoH geo_of(const hteno_solver* s) {
   G.g3 = s->cfg.gamma - 3.0;
   G.rdx = 1.0 / s->dx;
   G.rdy = 1.0 / s->dy;
+  G.rdxf = float(G.rdx);
+  G.rdyf = float(G.rdy);
   return G;
 }
 
