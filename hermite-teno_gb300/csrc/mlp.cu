@@ -552,19 +552,17 @@ struct RouteTile {
 };
 
 // Learned routing of a mixed FV 2D grid, pass 1 (masks zeroed beforehand), one launch per
-// direction: a block stages the float conserved values and the primitives (u, v, H, sqrt|rho|)
-// of its (A + 5) x B cells in shared memory (each cell converted once), then one thread per face
-// appends the face's non-flat stencils to the row list; appends are aggregated per block, one
-// atomic per block.  A face whose six cells are equal has only flat stencils and is skipped
-// before its eigenvectors.  Rows beyond `cap` are dropped (their stencils keep full TENO).
+// direction: a block stages the float conserved values of its (A + 5) x B cells in shared memory
+// (each cell converted once), then one thread per face appends the face's non-flat stencils to
+// the row list; appends are aggregated per block, one atomic per block.  A face whose six cells
+// are equal has only flat stencils and is skipped before its primitives and eigenvectors.  Rows beyond `cap` are dropped (their stencils keep full TENO).
 template <int DIR>
-__global__ void __launch_bounds__(256) k_route_prep(Geo G, const double* __restrict__ q, int tiles_a,
+__global__ void __launch_bounds__(256, 6) k_route_prep(Geo G, const double* __restrict__ q, int tiles_a,
                                                     uint4* __restrict__ rows,
                                                     unsigned long long* __restrict__ nrows, long cap) {
   constexpr int A = RouteTile<DIR>::A, B = RouteTile<DIR>::B, L = A + 5, NC = L * B;
   static_assert(A * B == 256, "one face per thread");
   __shared__ float sq[4][NC];  // conserved values, float
-  __shared__ float sp[4][NC];  // u, v, H, sqrt|rho|
   __shared__ int warp_tot[8];
   __shared__ unsigned long long block_base;
   const size_t nc = size_t(G.nx) * G.ny;
@@ -572,25 +570,28 @@ __global__ void __launch_bounds__(256) k_route_prep(Geo G, const double* __restr
   const int n_along = DIR == 1 ? G.nx : G.ny, n_across = DIR == 1 ? G.ny : G.nx;
   const int f0 = int(blockIdx.x % unsigned(tiles_a)) * A, l0 = int(blockIdx.x / unsigned(tiles_a)) * B;
   // staged cell e: along index f0 - 3 + a, line l0 + b; e = b * L + a (x) or a * B + b (y), so
-  // that consecutive e are consecutive in memory
-  for (int e = threadIdx.x; e < NC; e += 256) {
-    const int a = DIR == 1 ? e % L : e / B, b = DIR == 1 ? e / L : e % B;
-    const int line = min(l0 + b, n_across - 1);  // lines past the grid: their faces are not listed
-    const int ia = fused::cmap(f0 - 3 + a, n_along, G.bc);
-    const size_t k = DIR == 1 ? size_t(line) * G.nx + ia : size_t(ia) * G.nx + line;
-    float c[4];
+  // that consecutive e are consecutive in memory.  All of a thread's loads are issued before
+  // the first conversion.
+  constexpr int NS = (NC + 255) / 256;
+  double raw[NS][4];
 #pragma unroll
-    for (int v = 0; v < 4; ++v) {
-      c[v] = fused::d2f(__ldg(q + v * nc + k));
-      sq[v][e] = c[v];
+  for (int j = 0; j < NS; ++j) {
+    const int e = int(threadIdx.x) + 256 * j;
+    if (e < NC) {
+      const int a = DIR == 1 ? e % L : e / B, b = DIR == 1 ? e / L : e % B;
+      const int line = min(l0 + b, n_across - 1);  // lines past the grid: their faces are not listed
+      const int ia = fused::cmap(f0 - 3 + a, n_along, G.bc);
+      const size_t k = DIR == 1 ? size_t(line) * G.nx + ia : size_t(ia) * G.nx + line;
+#pragma unroll
+      for (int v = 0; v < 4; ++v) raw[j][v] = __ldg(q + v * nc + k);
     }
-    const float ir = __frcp_rn(c[0]);
-    const float u = c[1] * ir, v = c[2] * ir;
-    const float p = (c[3] - 0.5f * (c[1] * u + c[2] * v)) * g1;
-    sp[0][e] = u;
-    sp[1][e] = v;
-    sp[2][e] = (c[3] + p) * ir;
-    sp[3][e] = sqrtf(fabsf(c[0]));
+  }
+#pragma unroll
+  for (int j = 0; j < NS; ++j) {
+    const int e = int(threadIdx.x) + 256 * j;
+    if (e < NC)
+#pragma unroll
+      for (int v = 0; v < 4; ++v) sq[v][e] = fused::d2f(raw[j][v]);
   }
   __syncthreads();
   const int fa = DIR == 1 ? int(threadIdx.x) % A : int(threadIdx.x) / B;
@@ -611,12 +612,17 @@ __global__ void __launch_bounds__(256) k_route_prep(Geo G, const double* __restr
       }
     }
     if (!same) {
-      float cp[2][4];
+      float cp[2][4];  // primitives of the face's two cells
 #pragma unroll
       for (int h = 0; h < 2; ++h) {
-        const int e = DIR == 1 ? fb * L + fa + 2 + h : (fa + 2 + h) * B + fb;
-#pragma unroll
-        for (int k = 0; k < 4; ++k) cp[h][k] = sp[k][e];
+        const float* c = cq[2 + h];
+        const float ir = __frcp_rn(c[0]);
+        const float u = c[1] * ir, v = c[2] * ir;
+        const float p = (c[3] - 0.5f * (c[1] * u + c[2] * v)) * g1;
+        cp[h][0] = u;
+        cp[h][1] = v;
+        cp[h][2] = (c[3] + p) * ir;
+        cp[h][3] = sqrtf(fabsf(c[0]));
       }
       const long nxf = long(G.nx + 1) * G.ny;
       const long face = DIR == 1 ? long(line) * (G.nx + 1) + fi : nxf + long(fi) * G.nx + line;
