@@ -674,16 +674,22 @@ __global__ void __launch_bounds__(128, 4) k_route_rows(Weights W, const uint4* _
   const uint32_t tbase = S.tmem;
   uint32_t phase = 0;
   bool ok = true;
+  // this thread's rows of round rd (zero beyond the list)
+  auto fetch = [&](long rd, uint4* in) {
+    const long base = rd * kCRound;
+#pragma unroll
+    for (int t = 0; t < kCT; ++t) {
+      const long k = base + t * 128 + int(threadIdx.x);
+      in[t] = rd < nround && k < n ? rows[k] : make_uint4(0u, 0u, 0u, 0u);
+    }
+  };
+  uint4 in[kCT], next[kCT];
+  fetch(blockIdx.x, in);
   for (long rd = blockIdx.x; rd < nround && ok; rd += gridDim.x) {
     const long base = rd * kCRound;
     const int m = int(n - base < kCRound ? n - base : kCRound);
-    uint4 in[kCT];
+    fetch(rd + gridDim.x, next);  // in flight during this round's products
     float z[kCT][3];
-#pragma unroll
-    for (int t = 0; t < kCT; ++t) {
-      const int k = t * 128 + int(threadIdx.x);
-      in[t] = k < m ? rows[base + k] : make_uint4(0u, 0u, 0u, 0u);
-    }
     ok = forward_rows(S, tbase, phase, in, m, z);
     if (ok)
 #pragma unroll
@@ -696,6 +702,8 @@ __global__ void __launch_bounds__(128, 4) k_route_rows(Weights W, const uint4* _
           atomicOr(reinterpret_cast<unsigned int*>(a & ~size_t(3)), (1u << (in[t].w & 7u)) << (8 * (a & 3)));
         }
       }
+#pragma unroll
+    for (int t = 0; t < kCT; ++t) in[t] = next[t];
   }
   if (!ok) {
     if (threadIdx.x == 0) atomicExch(err, 1);
