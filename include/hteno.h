@@ -264,7 +264,8 @@ const char* hteno_mlp_last_error(hteno_mlp* m);
  * result when all three candidates are kept) and skip the nonlinear weights; every other stencil
  * takes full TENO.  Every `audit_every` steps (0: never) the stages also evaluate the plain TENO
  * cut-off of every stencil and count the routing errors.  m = NULL switches routing off; the
- * classifier must outlive its use by the solver. */
+ * classifier must outlive its use by the solver.  HTENO_ERR_UNSUPPORTED unless the solver is
+ * mixed-precision FV 2D with teno5 or teno5i and has fewer than 2^29 faces. */
 int hteno_set_router(hteno_solver* s, hteno_mlp* m, float threshold, int audit_every);
 /* stats[7]: audited stencils, routed, misrouted (routed though plain TENO cut a candidate),
  * all-smooth by plain TENO, flat (a window of equal float values: the stage kernel takes the
