@@ -68,7 +68,16 @@ template <> struct Cst<float> {
          : which == 2 ? c.f_hwtab_md[pat] : c.f_hwtab_pd[pat];
   }
   __device__ static float epsz() { return HTENO_F32_EPSZ; }
-  __device__ static float rcp(float x) { return __frcp_rn(x); }
+  // The MUFU reciprocal (rcp.approx.ftz.f32, relative error below 2^-23): one instruction
+  // instead of a correctly rounded reciprocal's refinement and range checks.  Every float
+  // reciprocal of the mixed path goes through here: weights, cut-off ratios, 1/rho, the HLLC
+  // star-state denominators -- none takes a subnormal argument (their floors: eps^2 = 1e-12,
+  // epsz = 1e-30, densities of the state).
+  __device__ static float rcp(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+  }
   __device__ static float sqrt_(float x) { return sqrtf(x); }
 };
 
@@ -295,14 +304,14 @@ template <typename T>
 __device__ __forceinline__ Roe2<T> roe2(T g1, T ra, T ua, T va, T ha, T rb, T ub, T vb, T hb) {
   // ra, rb: sqrt(|rho|) of the two cells; u, v velocities; h total enthalpy
   Roe2<T> s;
-  T t0 = ra / (ra + rb);
+  T t0 = ra * Cst<T>::rcp(ra + rb);
   T t1 = T(1.0) - t0;
   s.vxm = mad(t1, ub, t0 * ua);
   s.vym = mad(t1, vb, t0 * va);
   s.hm = mad(t1, hb, t0 * ha);
   s.qm = T(0.5) * mad(s.vym, s.vym, s.vxm * s.vxm);
   s.cm = Cst<T>::sqrt_(fabs(g1 * (s.hm - s.qm)));
-  s.rcm = T(1.0) / s.cm;
+  s.rcm = Cst<T>::rcp(s.cm);
   s.b1 = g1 * s.rcm * s.rcm;
   return s;
 }
@@ -361,7 +370,7 @@ __device__ __forceinline__ void flux2(int dir, const T* q, const T* w, T* f) {  
 template <typename T>
 __device__ __forceinline__ void hllc2(T g1, int dir, const T* ql, const T* qr, T* F) {
   T wl[4], wr[4];
-  const T il = T(1.0) / ql[0], ir = T(1.0) / qr[0];
+  const T il = Cst<T>::rcp(ql[0]), ir = Cst<T>::rcp(qr[0]);
   wl[0] = ql[0]; wl[1] = ql[1] * il; wl[2] = ql[2] * il;
   wl[3] = (ql[3] - T(0.5) * mad(ql[2], wl[2], ql[1] * wl[1])) * g1;
   wr[0] = qr[0]; wr[1] = qr[1] * ir; wr[2] = qr[2] * ir;
@@ -369,7 +378,7 @@ __device__ __forceinline__ void hllc2(T g1, int dir, const T* ql, const T* qr, T
   const T hl = (ql[3] + wl[3]) * il;
   const T hr = (qr[3] + wr[3]) * ir;
   const T rr = Cst<T>::sqrt_(fabs(wr[0] * il));
-  const T rrr = T(1.0) / (T(1.0) + rr);
+  const T rrr = Cst<T>::rcp(T(1.0) + rr);
   const T vm0 = mad(wr[1], rr, wl[1]) * rrr;
   const T vm1 = mad(wr[2], rr, wl[2]) * rrr;
   const T qm = T(0.5) * mad(vm1, vm1, vm0 * vm0);
@@ -381,15 +390,15 @@ __device__ __forceinline__ void hllc2(T g1, int dir, const T* ql, const T* qr, T
   const T ul = wl[dir], ur = wr[dir];
   const T sl = fmin(ul - cl, vmd - cm);
   const T sr = fmax(ur + cr, vmd + cm);
-  const T sm = (mad(-ql[dir], sl - ul, qr[dir] * (sr - ur)) + wl[3] - wr[3]) /
-               mad(-wl[0], sl - ul, wr[0] * (sr - ur));
+  const T sm = (mad(-ql[dir], sl - ul, qr[dir] * (sr - ur)) + wl[3] - wr[3]) *
+               Cst<T>::rcp(mad(-wl[0], sl - ul, wr[0] * (sr - ur)));
   const T ps = mad(wl[0] * (ul - sl), ul - sm, wl[3]);
   if (sl > T(0.0)) {
     flux2(dir, ql, wl, F);
   } else if (sl <= T(0.0) && sm > T(0.0)) {
     T fl[4];
     flux2(dir, ql, wl, fl);
-    const T nom = sl - ul, iden = T(1.0) / (sl - sm);
+    const T nom = sl - ul, iden = Cst<T>::rcp(sl - sm);
     T qs[4];
     qs[0] = wl[0] * nom * iden;
     qs[1] = dir == 1 ? (mad(nom, ql[1], ps) - wl[3]) * iden : nom * ql[1] * iden;
@@ -399,7 +408,7 @@ __device__ __forceinline__ void hllc2(T g1, int dir, const T* ql, const T* qr, T
   } else if (sm <= T(0.0) && sr >= T(0.0)) {
     T fr[4];
     flux2(dir, qr, wr, fr);
-    const T nom = sr - ur, iden = T(1.0) / (sr - sm);
+    const T nom = sr - ur, iden = Cst<T>::rcp(sr - sm);
     T qs[4];
     qs[0] = wr[0] * nom * iden;
     qs[1] = dir == 1 ? (mad(nom, qr[1], ps) - wr[3]) * iden : nom * qr[1] * iden;

@@ -75,9 +75,9 @@ __device__ __forceinline__ int teno_pat_s(const float* v, bool improved) {
   if (!improved) tau = fabsf(lagrange_b35(v) - (SI0 + SI2 + 4.0f * SI1) * (1.0f / 6.0f));
   else tau = fmaxf(fmaxf(SI0, SI1), SI2);
   const float ez = HTENO_F32_EPSZ;
-  const float r0 = fmaf(tau, __frcp_rn(SI0 + ez), 1.0f);
-  const float r1 = fmaf(tau, __frcp_rn(SI1 + ez), 1.0f);
-  const float r2 = fmaf(tau, __frcp_rn(SI2 + ez), 1.0f);
+  const float r0 = fmaf(tau, Cst<float>::rcp(SI0 + ez), 1.0f);
+  const float r1 = fmaf(tau, Cst<float>::rcp(SI1 + ez), 1.0f);
+  const float r2 = fmaf(tau, Cst<float>::rcp(SI2 + ez), 1.0f);
   return teno_pattern(r0, r1, r2, float(HTENO_LAG_CT));
 }
 
@@ -249,7 +249,7 @@ __device__ __forceinline__ double tile_stage(const DevConst& C, const Geo& G, in
     S.q[1][y][x] = mx;
     S.q[2][y][x] = my;
     S.q[3][y][x] = e;
-    const float ir = __frcp_rn(r);
+    const float ir = Cst<float>::rcp(r);
     const float u = mx * ir, v = my * ir;
     const float p = (e - 0.5f * fmaf(my, v, mx * u)) * g1;
     S.p[0][y][x] = u;
