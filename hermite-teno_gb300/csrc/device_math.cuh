@@ -78,8 +78,21 @@ template <> struct Cst<float> {
     asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
     return r;
   }
-  __device__ static float sqrt_(float x) { return sqrtf(x); }
+  // Likewise the MUFU-based square root (sqrt.approx.ftz.f32) for sound speeds and sqrt|rho|.
+  __device__ static float sqrt_(float x) {
+    float r;
+    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+  }
 };
+
+// a / b: in float through the MUFU reciprocal, in double the correctly rounded division (the
+// double instantiations serve the bit-reproducible paths).
+template <typename T>
+__device__ __forceinline__ T fdiv(T a, T b) {
+  if constexpr (sizeof(T) == 4) return a * Cst<T>::rcp(b);
+  else return a / b;
+}
 
 // a * b + c: an explicit fused multiply-add in float (so every instantiation rounds alike even
 // where the compiler is not allowed to contract); for double the unfused expression, which
@@ -428,8 +441,8 @@ __device__ __forceinline__ void rusanov2(T g, T g1, int dir, const Roe2<T>& s, c
   T wl[4], wr[4], fl[4], fr[4], d[4], m[4], a[4];
   primitive2(g1, ql, wl);
   primitive2(g1, qr, wr);
-  const T cl = Cst<T>::sqrt_(fabs(g * wl[3] / wl[0]));
-  const T cr = Cst<T>::sqrt_(fabs(g * wr[3] / wr[0]));
+  const T cl = Cst<T>::sqrt_(fabs(fdiv(g * wl[3], wl[0])));
+  const T cr = Cst<T>::sqrt_(fabs(fdiv(g * wr[3], wr[0])));
   const T vl = wl[dir], vr = wr[dir];
   a[0] = fmax(fabs(vl - cl), fabs(vr - cr));
   a[1] = fmax(fabs(vl), fabs(vr));
@@ -448,7 +461,7 @@ __device__ __forceinline__ void rusanov2(T g, T g1, int dir, const Roe2<T>& s, c
 // maxSpeed (Equations_Euler2D.cpp:207-219)
 template <typename T>
 __device__ __forceinline__ T max_speed2(T g, const T* w, int dir) {
-  T c = Cst<T>::sqrt_(fabs(g * w[3] / w[0]));
+  T c = Cst<T>::sqrt_(fabs(fdiv(g * w[3], w[0])));
   return fmax(w[dir] - c, fabs(w[dir] + c));
 }
 

@@ -255,7 +255,7 @@ __device__ __forceinline__ double tile_stage(const DevConst& C, const Geo& G, in
     S.p[0][y][x] = u;
     S.p[1][y][x] = v;
     S.p[2][y][x] = (e + p) * ir;
-    S.p[3][y][x] = sqrtf(fabsf(r));
+    S.p[3][y][x] = Cst<float>::sqrt_(fabsf(r));
   }
   __syncthreads();
 
@@ -446,7 +446,7 @@ __device__ __forceinline__ double tile_stage(const DevConst& C, const Geo& G, in
       if (isnan(p)) bad |= 1;
       else if (qn[0] <= 0.0 || p <= 0.0) bad |= 2;
       const float fr = d2f(qn[0]), fu = d2f(qn[1] * ir), fv = d2f(qn[2] * ir);
-      const float c = sqrtf(fabsf(float(G.gamma) * d2f(p) / fr));
+      const float c = Cst<float>::sqrt_(fabsf(float(G.gamma) * d2f(p) * Cst<float>::rcp(fr)));
       const float m = fmaxf(fmaxf(fu - c, fabsf(fu + c)), fmaxf(fv - c, fabsf(fv + c)));
       msf = fmaxf(msf, m);
     }

@@ -698,7 +698,7 @@ __global__ void kh_update(GeoH G, int stage, const T* __restrict__ fx, const T* 
       primt[k] = mix::d2f(u);
       primt[nc + k] = mix::d2f(vv);
       primt[2 * nc + k] = mix::d2f((qn[3] + p) * ir);
-      primt[3 * nc + k] = sqrtf(fabsf(fr));
+      primt[3 * nc + k] = Cst<float>::sqrt_(fabsf(fr));
       if (stage == 3) {
         const float fu = mix::d2f(u), fv = mix::d2f(vv);
         const float cs = sqrtf(fabsf(float(G.gamma) * mix::d2f(p) / fr));

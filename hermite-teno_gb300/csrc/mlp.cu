@@ -616,13 +616,15 @@ __global__ void __launch_bounds__(256, 6) k_route_prep(Geo G, const double* __re
 #pragma unroll
       for (int h = 0; h < 2; ++h) {
         const float* c = cq[2 + h];
-        const float ir = __frcp_rn(c[0]);
+        // the fused stage kernel's phase-A arithmetic (this unit is also compiled without
+        // implicit contraction), so the stencils are the bits that kernel reconstructs
+        const float ir = Cst<float>::rcp(c[0]);
         const float u = c[1] * ir, v = c[2] * ir;
-        const float p = (c[3] - 0.5f * (c[1] * u + c[2] * v)) * g1;
+        const float p = (c[3] - 0.5f * fmaf(c[2], v, c[1] * u)) * g1;
         cp[h][0] = u;
         cp[h][1] = v;
         cp[h][2] = (c[3] + p) * ir;
-        cp[h][3] = sqrtf(fabsf(c[0]));
+        cp[h][3] = Cst<float>::sqrt_(fabsf(c[0]));
       }
       const long nxf = long(G.nx + 1) * G.ny;
       const long face = DIR == 1 ? long(line) * (G.nx + 1) + fi : nxf + long(fi) * G.nx + line;

@@ -28,7 +28,7 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
 # fused mixed-precision units, whose tile-shape candidates must give the same bits (with implicit
 # contraction the compiler fused different float expressions in different instantiations).
 NO_FMAD = {"fv2d_fp64.cu", "fv1d.cu", "pointwise.cu", "hermite2d_fp64.cu", "hermite1d.cu",
-           "fv2d_fused.cu", "fv2d_batch.cu"}
+           "fv2d_fused.cu", "fv2d_batch.cu", "mlp.cu"}
 
 
 def _cuda_home() -> Path:
