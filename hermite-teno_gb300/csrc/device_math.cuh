@@ -356,7 +356,7 @@ __device__ __forceinline__ void roe_right(const Roe2<T>& s, int dir, const T* c,
 
 template <typename T>
 __device__ __forceinline__ void primitive2(T g1, const T* q, T* w) {  // Euler2D::primitive :20-26
-  T ir = T(1.0) / q[0];
+  T ir = fdiv(T(1.0), q[0]);
   w[0] = q[0];
   w[1] = q[1] * ir;
   w[2] = q[2] * ir;

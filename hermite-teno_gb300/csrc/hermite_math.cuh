@@ -225,7 +225,7 @@ __device__ __forceinline__ void dflux2_apply(T g, T g1, int dir, const T* q, con
   const T xn = dir == 1 ? x[1] : x[2], xt = dir == 1 ? x[2] : x[1];
   const T sv = un * un;
   const T dv = T(0.5) * g1 * (sv + ut * ut);
-  const T h = (q[3] + w[3]) / w[0];
+  const T h = fdiv(q[3] + w[3], w[0]);
   y[0] = xn;
   // normal momentum row: (dv - sv, -g3 un, -g1 ut, g1)
   const T yn = (dv - sv) * x[0] + (-g3 * un) * xn + (-g1 * ut) * xt + g1 * x[3];
@@ -244,8 +244,8 @@ __device__ __forceinline__ void drusanov2(T g, T g1, int dir, const Roe2<T>& s, 
   T wl[4], wr[4], a[4], d[4], m[4], al[4], ar[4], rm[4];
   primitive2(g1, ql, wl);
   primitive2(g1, qr, wr);
-  const T cl = Cst<T>::sqrt_(fabs(g * wl[3] / wl[0]));
-  const T cr = Cst<T>::sqrt_(fabs(g * wr[3] / wr[0]));
+  const T cl = Cst<T>::sqrt_(fabs(fdiv(g * wl[3], wl[0])));
+  const T cr = Cst<T>::sqrt_(fabs(fdiv(g * wr[3], wr[0])));
   const T vl = wl[dir], vr = wr[dir];
   a[0] = fmax(fabs(vl - cl), fabs(vr - cr));
   a[1] = fmax(fabs(vl), fabs(vr));
