@@ -153,6 +153,32 @@ def test_fluxes(hteno_lib, cuda, oracle, pw):
     close_scaled(o3.cpu().numpy(), pw["hllc1d_out"], scale[:, :1], RTOL64)
 
 
+def test_fluxes_float(hteno_lib, cuda, pw):
+    """The float fluxes of the mixed path (reciprocals and square roots on the MUFU) against the
+    reference's FP64 values: within float accuracy of the states' magnitude."""
+    L = hteno_lib.lib()
+    ql, qr, qa, qb = pw["flux_ql"], pw["flux_qr"], pw["flux_qa"], pw["flux_qb"]
+    dql, dqr = pw["flux_dql"], pw["flux_dqr"]
+    n = ql.shape[0]
+    t = {k: dev(cuda, v) for k, v in dict(ql=ql, qr=qr, qa=qa, qb=qb, dql=dql, dqr=dqr).items()}
+    out = cuda.empty((n, 4), dtype=cuda.float64, device="cuda")
+    scale = np.maximum(np.abs(ql).max(axis=1), np.abs(qr).max(axis=1))[:, None] * 4
+    rtol = 2e-5  # float (2^-24) through ~20 dependent operations, approximate reciprocals included
+    for d in (1, 2):
+        assert L.hteno_hllc2d_batch(1, 1.4, d, t["ql"].data_ptr(), t["qr"].data_ptr(), out.data_ptr(), n, None) == 0
+        cuda.cuda.synchronize()
+        close_scaled(out.cpu().numpy(), pw[f"hllc2d_{d}"], scale, rtol)
+        assert L.hteno_rusanov2d_batch(1, 1.4, d, t["qa"].data_ptr(), t["qb"].data_ptr(), t["ql"].data_ptr(),
+                                       t["qr"].data_ptr(), out.data_ptr(), n, None) == 0
+        cuda.cuda.synchronize()
+        close_scaled(out.cpu().numpy(), pw[f"rusanov2d_{d}"], scale, rtol)
+        assert L.hteno_drusanov2d_batch(1, 1.4, d, t["qa"].data_ptr(), t["qb"].data_ptr(), t["ql"].data_ptr(),
+                                        t["qr"].data_ptr(), t["dql"].data_ptr(), t["dqr"].data_ptr(),
+                                        out.data_ptr(), n, None) == 0
+        cuda.cuda.synchronize()
+        close_scaled(out.cpu().numpy(), pw[f"drusanov2d_{d}"], scale * 4, rtol)
+
+
 def test_ssprk3_bitwise(hteno_lib, cuda, pw):
     """The stage combination is plain IEEE arithmetic in the reference's order: bit-exact."""
     q0, qn, rhs = (dev(cuda, pw[k]) for k in ("rk_q0", "rk_qn", "rk_rhs"))
