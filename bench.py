@@ -66,6 +66,9 @@ def parse():
     ap.add_argument("--c5-fp64-steps", type=int, default=3)
     ap.add_argument("--c5-epochs", type=int, default=10)
     ap.add_argument("--c5-audit-every", type=int, default=10)
+    ap.add_argument("--c5-threshold", type=float, default=0.99,
+                    help="routing threshold: a stencil takes the linear weights when all three "
+                         "predicted cut-off probabilities exceed it")
     ap.add_argument("--batch-steps", type=int, default=100)
     return ap.parse_args()
 
@@ -334,7 +337,7 @@ def learned_path(hteno, torch, stream, args, world, n=4096):
     loss = m.train(x, y, epochs=args.c5_epochs, batch=16384, lr=3e-3)
     torch.cuda.synchronize()
     t3 = time.perf_counter()
-    acc, routed, mis = learned.accuracy(m, torch, x, y, 0.9)
+    acc, routed, mis = learned.accuracy(m, torch, x, y, args.c5_threshold)
     out["training"] = {"rows": int(x.shape[0]), "smooth_fraction": float((y == 7).float().mean().item()),
                        "harvest_s": t1 - t0, "train_s": t3 - t2, "epochs": args.c5_epochs,
                        "rows_per_s": x.shape[0] * args.c5_epochs / (t3 - t2), "final_loss": loss,
@@ -364,7 +367,7 @@ def learned_path(hteno, torch, stream, args, world, n=4096):
         with hteno.Solver(cfg32) as s:
             s.set_stream(stream.cuda_stream)
             if router is not None:
-                s.set_router(router, 0.9, args.c5_audit_every)
+                s.set_router(router, args.c5_threshold, args.c5_audit_every)
             s.set_state(q)
             s.step_async(2)  # warm-up
             s.sync()
@@ -398,7 +401,7 @@ def learned_path(hteno, torch, stream, args, world, n=4096):
                            "network_rows_last_step": st["network_rows"],
                            "misrouted_of_routed": st["misrouted"] / max(1, st["routed"]),
                            "plain_teno_smooth_fraction": st["smooth"] / max(1, st["seen"]),
-                           "audited_steps": st["audits"], "threshold": 0.9,
+                           "audited_steps": st["audits"], "threshold": args.c5_threshold,
                            "audit_every": args.c5_audit_every}
         out[name] = d
     m.close()
