@@ -153,7 +153,7 @@ def test_trained_router_gains(hteno_lib, cuda):
             ref = s.get_state()
         cfg = h.config(dims=2, nx=256, ny=256, flux=1, precision=1)
         with h.Solver(cfg) as s:
-            s.set_router(m, 0.9, 5)
+            s.set_router(m, 0.99, 5)
             s.set_state(q)
             s.step(1000, t_ref)
             st = s.router_stats()
