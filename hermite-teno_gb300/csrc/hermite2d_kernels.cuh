@@ -638,7 +638,7 @@ __global__ void __launch_bounds__(kHFluxThreads) kh_flux(GeoH G, const T* __rest
 
 // rhs (:710-730) and RungeKutta3 (:733-782) for u, v, w
 template <typename T>
-__global__ void kh_update(GeoH G, int stage, const T* __restrict__ fx, const T* __restrict__ fy,
+__global__ void __launch_bounds__(256, 4) kh_update(GeoH G, int stage, const T* __restrict__ fx, const T* __restrict__ fy,
                           double* __restrict__ q, double* __restrict__ q0,
                           double* __restrict__ v, double* __restrict__ v0,
                           double* __restrict__ vs, double* __restrict__ w,
