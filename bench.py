@@ -552,7 +552,10 @@ def run_gpu(args):
                             "peak_tflops": fp64_peak, "peak_source": "measured FP64 FMA microbenchmark (hteno_measure_fma_peak)",
                             "frac": dom["flops_per_launch"] / avg_s / 1e12 / fp64_peak,
                             "flops_note": "algorithmic flops of the reference (+,-,*,/,sqrt = 1, pow = 1), op-counted on the oracle"},
-                "kernels": kernels}
+                "kernels": kernels,
+                "note": "the bit-reproducible FP64 kernels are bound by the FP64 pipe (2 FP64 "
+                        "operations per SM per cycle on GB300), not by HBM: compute.frac is the "
+                        "fraction that applies; frac is the HBM one the contract asks for"}
     step_flops = sum(k["flops_per_launch"] * k["launches"] for k in kernels) / args.steps
     roofline["step"] = {"achieved_tflops": step_flops * args.steps / (ms / 1e3) / 1e12,
                         "frac_of_fp64_peak": step_flops * args.steps / (ms / 1e3) / 1e12 / fp64_peak}
