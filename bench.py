@@ -59,13 +59,15 @@ def parse():
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-hermite", action="store_true")
     ap.add_argument("--no-sod", action="store_true")
-    ap.add_argument("--hermite-steps", type=int, default=10)
+    ap.add_argument("--hermite-steps", type=int, default=10,
+                    help="steps of both Hermite arms (the same window from the initial state)")
     ap.add_argument("--hermite-n", type=int, default=2048, help="grid side of the Hermite 2D path")
     ap.add_argument("--no-learned", action="store_true")
-    ap.add_argument("--c5-steps", type=int, default=20)
-    ap.add_argument("--c5-fp64-steps", type=int, default=3)
+    ap.add_argument("--c5-steps", type=int, default=500,
+                    help="steps of the 4096^2 learned-routing case: the FP64 arm runs them, the FP32 "
+                         "arms run from the same initial state to the FP64 arm's end time")
     ap.add_argument("--c5-epochs", type=int, default=10)
-    ap.add_argument("--c5-audit-every", type=int, default=10)
+    ap.add_argument("--c5-audit-every", type=int, default=50)
     ap.add_argument("--c5-threshold", type=float, default=0.99,
                     help="routing threshold: a stencil takes the linear weights when all three "
                          "predicted cut-off probabilities exceed it")
@@ -100,9 +102,9 @@ def allreduce_max(torch, world, x):
     return replicas.reduce(torch, x, "max", "cuda") if world > 1 else x
 
 
-def config_block(args, world):
+def config_block(args, world, timed_from_step):
     return {"workload": WORKLOAD, "nx": NX, "ny": NY, "recon": "teno5", "flux": "hllc",
-            "timed_from_step": max(args.warmup, args.start_step),
+            "timed_from_step": timed_from_step,
             "bc": "zero-gradient", "cfl": 0.4, "gamma": 1.4, "seed": SEED,
             "parallelism": f"replicas{world}" if world > 1 else "single-gpu",
             "l2": "working set ~0.45 GB per GPU > 129 MB L2 (no flush needed)"}
@@ -168,6 +170,17 @@ def traffic_from_profiles(kernel: str):
     return None
 
 
+def fp64_pipe_from_profiles(kernel: str):
+    """FP64-pipe figures of `kernel` from the committed ncu summary, if present: pipe utilisation
+    and FP64 thread-instructions executed per algorithmic flop."""
+    p = REPO / "profiles" / "fp64_pipe.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        if kernel in d:
+            return d[kernel]
+    return None
+
+
 def cpu_baseline_sample(threads: int):
     """The oracle (CPU restatement of the reference, OpenMP over rows) on a bounded sample of the
     same workload: a 512 x 512 four-quadrant grid, 10 steps."""
@@ -206,7 +219,7 @@ def run_reference(args):
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": el * 1e3 / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": config_block(args, 1), "impl": "reference",
+            "config": config_block(args, 1, max(0, args.warmup)), "impl": "reference",
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                              "sample": f"full {NX}x{NY} grid, one step per timed step; the reference's "
                                        "own sources need Eigen3 and cannot be built on the GPU host, so "
@@ -267,11 +280,11 @@ def kernel_shares(hteno, solver, steps):
     return {name: round(ms / tot, 4) for name, ms in rows}
 
 
-def hermite_path(hteno, torch, stream, steps, ref_steps, world, n=2048):
+def hermite_path(hteno, torch, stream, steps, world, n=2048):
     """Hermite-WENO 2D (FVHermite::System2D) on n x n: 32 seeded Gaussian density blobs on
-    rho = 1, p = 1, a Mach-2 shock entering from x = 0, moments by face differences; mixed
-    precision timed over `steps` steps; density error against the plain FP64 run advanced
-    `ref_steps` steps, the mixed run stopping at the same time."""
+    rho = 1, p = 1, a Mach-2 shock entering from x = 0, moments by face differences.  Both arms
+    (plain FP64, mixed) are timed over the same window, `steps` steps from the initial state;
+    the mixed arm's density error is taken against the FP64 state at the FP64 arm's end time."""
     from hteno import ic
 
     f = ic.blobs_shock_fn(5)
@@ -288,42 +301,42 @@ def hermite_path(hteno, torch, stream, steps, ref_steps, world, n=2048):
             s.set_stream(stream.cuda_stream)
             s.set_state(q)
             s.set_moments(v, w)
-            k = ref_steps if prec == hteno.PREC_FP64 else steps
             ev0 = torch.cuda.Event(enable_timing=True)
             ev1 = torch.cuda.Event(enable_timing=True)
             torch.cuda.synchronize()
             ev0.record(stream)
-            s.step_async(k)
+            if prec == hteno.PREC_FP64:
+                s.step_async(steps)
+            else:
+                s.step(1 << 20, ref[0])  # to the FP64 arm's end time
             ev1.record(stream)
             ev1.synchronize()
             s.sync()
             ms = ev0.elapsed_time(ev1)
+            k = s.time()[1]
             name = "fp64" if prec == hteno.PREC_FP64 else "fp32_mixed"
             out[name] = {"value": n * n * k * world / (ms / 1e3) / 1e6, "unit": UNIT,
-                         "ms_per_step": ms / k, "steps": k}
-            if prec == hteno.PREC_MIXED:  # where a mixed step spends its time (separate run)
-                out[name]["kernel_shares"] = kernel_shares(hteno, s, 2)
+                         "ms_per_step": ms / k, "steps": k, "t": s.time()[0]}
             if prec == hteno.PREC_FP64:
                 ref = (s.time()[0], s.get_state())
             else:
-                s.set_state(q)
-                s.set_moments(v, w)
-                s.step(1 << 20, ref[0])
                 l1, linf = density_errors(s.get_state(), ref[1])
-                out[name].update({"l1_rho_vs_fp64": l1, "linf_rho_vs_fp64": linf, "t": ref[0]})
+                out[name].update({"l1_rho_vs_fp64": l1, "linf_rho_vs_fp64": linf})
+                out[name]["kernel_shares"] = kernel_shares(hteno, s, 2)  # separate, after the timing
     out["speedup_mixed_vs_fp64"] = out["fp64"]["ms_per_step"] / out["fp32_mixed"]["ms_per_step"]
     out["workload"] = f"hermite2d_blobs_mach2_{n}x{n}_rusanov_ssprk3"
+    out["window"] = f"both arms from the initial state to the FP64 arm's time after {steps} steps"
     return out
 
 
 def learned_path(hteno, torch, stream, args, world, n=4096):
     """The learned-routing workload: 4096 x 4096 seeded four-quadrant data, TENO5 + HLLC.
     The classifier trains on rows the plain FP64 solver records from runs with fresh seeds of the
-    1024^2 four-quadrant problem and the 400-cell Sod tube.  Three arms run from the same
-    state: plain FP64, FP32 (mixed) and FP32 + learned routing with a plain-TENO audit every
-    `c5_audit_every` steps (50 in the configuration's 500-step run, 10 for the short default).
-    The mixed arms are timed over `c5_steps`; the FP64 arm over `c5_fp64_steps`.  Densities are
-    compared at the FP64 arm's final time."""
+    1024^2 four-quadrant problem and the 400-cell Sod tube.  Three arms run over the same window:
+    plain FP64 runs `c5_steps` steps from the initial state; FP32 (mixed) and FP32 + learned
+    routing (a plain-TENO audit every `c5_audit_every` steps) run from the same initial state to
+    the FP64 arm's end time.  Each arm is timed over its whole run; densities are compared at
+    that end time."""
     from hteno import ic, learned
 
     out = {"workload": f"fv2d_fourquadrant_{n}x{n}_teno5_hllc_learned_routing"}
@@ -341,27 +354,35 @@ def learned_path(hteno, torch, stream, args, world, n=4096):
     out["training"] = {"rows": int(x.shape[0]), "smooth_fraction": float((y == 7).float().mean().item()),
                        "harvest_s": t1 - t0, "train_s": t3 - t2, "epochs": args.c5_epochs,
                        "rows_per_s": x.shape[0] * args.c5_epochs / (t3 - t2), "final_loss": loss,
-                       "bit_accuracy": acc, "routed_fraction": routed, "misrouted_of_routed": mis}
+                       "bit_accuracy": acc, "routed_fraction": routed, "misrouted_of_routed": mis,
+                       "deterministic": "per-CTA partial gradients summed in CTA order"}
     del x, y
     q = ic.four_quadrant(n, n, 7)
+
+    def timed_run(s, nsteps=None, t_end=None):
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        if nsteps is not None:
+            s.step_async(nsteps)
+        else:
+            s.step(1 << 20, t_end)
+        ev1.record(stream)
+        ev1.synchronize()
+        s.sync()
+        return ev0.elapsed_time(ev1), s.time()
 
     cfg64 = hteno.config(dims=2, nx=n, ny=n, flux=hteno.FLUX_HLLC, precision=hteno.PREC_FP64)
     with hteno.Solver(cfg64) as s:
         s.set_stream(stream.cuda_stream)
         s.set_state(q)
-        ev0 = torch.cuda.Event(enable_timing=True)
-        ev1 = torch.cuda.Event(enable_timing=True)
-        torch.cuda.synchronize()
-        ev0.record(stream)
-        s.step_async(args.c5_fp64_steps)
-        ev1.record(stream)
-        ev1.synchronize()
-        s.sync()
-        ms64 = ev0.elapsed_time(ev1)
-        t_ref = s.time()[0]
+        ms64, (t_ref, n64, _) = timed_run(s, nsteps=args.c5_steps)
         ref = s.get_state()
-    out["fp64"] = {"value": n * n * args.c5_fp64_steps * world / (ms64 / 1e3) / 1e6, "unit": UNIT,
-                   "ms_per_step": ms64 / args.c5_fp64_steps, "steps": args.c5_fp64_steps}
+        u64 = s.uniform_cells()
+    out["fp64"] = {"value": n * n * n64 * world / (ms64 / 1e3) / 1e6, "unit": UNIT,
+                   "ms_per_step": ms64 / n64, "steps": n64, "t_end": t_ref,
+                   "uniform_cell_fraction": u64 / (3.0 * n * n * n64)}
     cfg32 = hteno.config(dims=2, nx=n, ny=n, flux=hteno.FLUX_HLLC, precision=hteno.PREC_MIXED)
     for name, router in (("fp32_plain", None), ("fp32_learned", m)):
         with hteno.Solver(cfg32) as s:
@@ -369,30 +390,21 @@ def learned_path(hteno, torch, stream, args, world, n=4096):
             if router is not None:
                 s.set_router(router, args.c5_threshold, args.c5_audit_every)
             s.set_state(q)
-            s.step_async(2)  # warm-up
+            s.step_async(2)  # warm-up (the tile tuner ran when the state was first set)
             s.sync()
-            ev0 = torch.cuda.Event(enable_timing=True)
-            ev1 = torch.cuda.Event(enable_timing=True)
-            torch.cuda.synchronize()
-            ev0.record(stream)
-            s.step_async(args.c5_steps)
-            ev1.record(stream)
-            ev1.synchronize()
-            s.sync()
-            ms = ev0.elapsed_time(ev1)
-            st = s.router_stats() if router is not None else None
-            shares = kernel_shares(hteno, s, 2)
-            # accuracy: the same arm from the initial state to the FP64 arm's time
             s.set_state(q)
-            s.step(1 << 20, t_ref)
+            ms, (t_end, nsteps, _) = timed_run(s, t_end=t_ref)
+            st = s.router_stats() if router is not None else None
             got = s.get_state()
+            uc = s.uniform_cells()
             l1, linf = density_errors(got, ref)
             shift = shock_shift(got, ref)
-        d = {"value": n * n * args.c5_steps * world / (ms / 1e3) / 1e6, "unit": UNIT,
-             "ms_per_step": ms / args.c5_steps, "steps": args.c5_steps,
-             "speedup_vs_fp64": (ms64 / args.c5_fp64_steps) / (ms / args.c5_steps),
+            shares = kernel_shares(hteno, s, 2)  # a separate pass after the timed run
+        d = {"value": n * n * nsteps * world / (ms / 1e3) / 1e6, "unit": UNIT,
+             "ms_per_step": ms / nsteps, "steps": nsteps, "t_end": t_end,
+             "speedup_vs_fp64": (ms64 / n64) / (ms / nsteps),
              "l1_rho_vs_fp64": l1, "linf_rho_vs_fp64": linf, "shock_shift_cells": shift,
-             "t_compared": t_ref, "kernel_shares": shares}
+             "uniform_cell_fraction": uc / (3.0 * n * n * nsteps), "kernel_shares": shares}
         if st is not None:
             nonflat_smooth = max(1, st["smooth"] - st["flat"])
             d["router"] = {"audited_stencils": st["seen"], "routed_fraction": st["routed"] / max(1, st["seen"]),
@@ -406,6 +418,8 @@ def learned_path(hteno, torch, stream, args, world, n=4096):
         out[name] = d
     m.close()
     out["learned_vs_fp32_plain"] = out["fp32_plain"]["ms_per_step"] / out["fp32_learned"]["ms_per_step"]
+    out["window"] = (f"every arm from the initial state: FP64 {args.c5_steps} steps, the FP32 arms to the "
+                     "FP64 arm's end time; errors at that time")
     return out
 
 
@@ -502,12 +516,13 @@ def run_gpu(args):
     solver.sync()
     start_state = solver.get_state()
 
-    # timed region: K steps, device-resident, CUDA events on the solver's stream
-    lib.hteno_enable_kernel_timing(solver.h, 1)
+    # timed region: K steps, device-resident, CUDA events on the solver's stream, nothing else
+    # inside it (per-kernel times come from a separate pass below)
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
     clocks = Clocks(int(os.environ.get("CUDA_VISIBLE_DEVICES", str(local)).split(",")[0])
                     if os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",")[0].isdigit() else local)
+    uni0 = solver.uniform_cells()
     barrier(torch, world)
     torch.cuda.synchronize()
     with clocks:
@@ -522,14 +537,22 @@ def run_gpu(args):
     ms = ev0.elapsed_time(ev1)
     t_plain, _, _ = solver.time()
     ref_state = solver.get_state()
+    uniform_fraction = (solver.uniform_cells() - uni0) / (3.0 * ncell * args.steps)
     ms_max = allreduce_max(torch, world, ms)
     value = ncell * args.steps * world / (ms_max / 1e3) / 1e6
 
-    # per-kernel times inside the timed region (events bracketing every launch)
-    KT = hteno.KernelTime * 16
-    kt = KT()
-    cnt = __import__("ctypes").c_int()
-    lib.hteno_kernel_timing(solver.h, kt, 16, __import__("ctypes").byref(cnt))
+    # per-kernel times of the same K steps, replayed from the timed region's start state with CUDA
+    # events bracketing every launch (set_state restarts the clock at 0; dt follows from the state
+    # alone, so the replayed steps are the timed ones)
+    import ctypes
+
+    solver.set_state(start_state)
+    lib.hteno_enable_kernel_timing(solver.h, 1)
+    solver.step_async(args.steps)
+    solver.sync()
+    kt = (hteno.KernelTime * 16)()
+    cnt = ctypes.c_int()
+    lib.hteno_kernel_timing(solver.h, kt, 16, ctypes.byref(cnt))
     lib.hteno_enable_kernel_timing(solver.h, 0)
     kernels = []
     for k in range(cnt.value):
@@ -543,22 +566,30 @@ def run_gpu(args):
     dom = max(kernels, key=lambda k: k["ms"])
     avg_s = dom["ms"] / dom["launches"] / 1e3
     hbm, hbm_src = peaks()
-    achieved = dom["bytes_per_launch"] / avg_s / 1e9
     fp64_peak = hteno.measure_fma_peak(0)
-    roofline = {"bound": "hbm", "kernel": dom["name"], "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                "frac": achieved / hbm, "peak_source": f"{hbm_src} (MEASURED_PEAKS.json hbm_gbs)" if hbm_src == "measured" else "fallback 6.8 TB/s",
-                "traffic": traffic_from_profiles(dom["name"]),
-                "compute": {"pipe": "fp64", "achieved_tflops": dom["flops_per_launch"] / avg_s / 1e12,
-                            "peak_tflops": fp64_peak, "peak_source": "measured FP64 FMA microbenchmark (hteno_measure_fma_peak)",
-                            "frac": dom["flops_per_launch"] / avg_s / 1e12 / fp64_peak,
-                            "flops_note": "algorithmic flops of the reference (+,-,*,/,sqrt = 1, pow = 1), op-counted on the oracle"},
-                "kernels": kernels,
-                "note": "the bit-reproducible FP64 kernels are bound by the FP64 pipe (2 FP64 "
-                        "operations per SM per cycle on GB300), not by HBM: compute.frac is the "
-                        "fraction that applies; frac is the HBM one the contract asks for"}
+    achieved = dom["flops_per_launch"] / avg_s / 1e12
     step_flops = sum(k["flops_per_launch"] * k["launches"] for k in kernels) / args.steps
-    roofline["step"] = {"achieved_tflops": step_flops * args.steps / (ms / 1e3) / 1e12,
-                        "frac_of_fp64_peak": step_flops * args.steps / (ms / 1e3) / 1e12 / fp64_peak}
+    roofline = {"bound": "fp64", "kernel": dom["name"], "achieved": achieved, "peak": fp64_peak,
+                "unit": "TFLOP/s", "frac": achieved / fp64_peak,
+                "peak_source": "measured FP64 FMA throughput of this GPU (hteno_measure_fma_peak; "
+                               "MEASURED_PEAKS.json has no FP64 figure)",
+                "traffic": traffic_from_profiles(dom["name"]),
+                "flops_note": "algorithmic flops of the reference per launch (+,-,*,/,sqrt = 1, pow = 1), "
+                              "op-counted on the oracle, for every face of the launch including the "
+                              "uniform-region faces the path skips exactly",
+                "hbm": {"achieved": dom["bytes_per_launch"] / avg_s / 1e9, "peak": hbm, "unit": "GB/s",
+                        "frac": dom["bytes_per_launch"] / avg_s / 1e9 / hbm,
+                        "peak_source": f"{hbm_src} (MEASURED_PEAKS.json hbm_gbs)" if hbm_src == "measured"
+                                       else "fallback 6.8 TB/s"},
+                "fp64_pipe": fp64_pipe_from_profiles(dom["name"]),
+                "step": {"achieved_tflops": step_flops * args.steps / (ms / 1e3) / 1e12,
+                         "frac_of_fp64_peak": step_flops * args.steps / (ms / 1e3) / 1e12 / fp64_peak},
+                "uniform_cell_fraction": uniform_fraction,
+                "kernels": kernels,
+                "note": "the bit-reproducible FP64 kernels are bound by the FP64 pipe (2 FP64 operations "
+                        "per SM per cycle on GB300), not by HBM; uniform_cell_fraction is the share of "
+                        "cell-stages of the timed steps whose exactly zero residual was taken without "
+                        "computing their faces"}
 
     # end to end through the C-ABI with pinned host buffers: every step copies the state in,
     # advances one step and reads the state back
@@ -589,7 +620,7 @@ def run_gpu(args):
     if not args.no_sod and rank == 0:
         paths["sod_1d_400"] = sod_path(hteno, torch)
     if not args.no_hermite:
-        paths[f"hermite_{args.hermite_n}"] = hermite_path(hteno, torch, stream, args.hermite_steps, 3, world,
+        paths[f"hermite_{args.hermite_n}"] = hermite_path(hteno, torch, stream, args.hermite_steps, world,
                                                            n=args.hermite_n)
     if not args.no_learned:
         paths["learned_4096"] = learned_path(hteno, torch, stream, args, world)
@@ -599,7 +630,8 @@ def run_gpu(args):
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": config_block(args, world), "gpu_launches": launches * args.steps,
+            "config": config_block(args, world, max(args.warmup, args.start_step)),
+            "gpu_launches": launches * args.steps,
             "clocks": clocks.summary(), "roofline": roofline, "e2e": e2e, "paths": paths}
     if rank == 0 and world == 1 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline_sample(os.cpu_count() or 1)

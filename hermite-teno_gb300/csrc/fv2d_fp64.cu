@@ -63,7 +63,7 @@ __device__ __forceinline__ int cmap_any(int i, int n, int bc) {  // any offset (
 }
 
 __global__ void __launch_bounds__(256) kp_deep(Geo G, const double* __restrict__ q,
-                                               uint8_t* __restrict__ deep, const StepState* st) {
+                                               uint8_t* __restrict__ deep, StepState* st) {
   if (st && st->done) return;
   constexpr int TX = 32, TY = 8, W = TX + 6, H = TY + 6;
   __shared__ unsigned long long key[4][H][W];
@@ -87,25 +87,30 @@ __global__ void __launch_bounds__(256) kp_deep(Geo G, const double* __restrict__
   __syncthreads();
   const int tx = threadIdx.x % TX, ty = threadIdx.x / TX;
   const int gi = i0 + tx, gj = j0 + ty;
-  if (gi >= G.nx || gj >= G.ny) return;
-  const unsigned long long c0 = key[0][ty + 3][tx + 3], c1 = key[1][ty + 3][tx + 3];
-  const unsigned long long c2 = key[2][ty + 3][tx + 3], c3 = key[3][ty + 3][tx + 3];
-  const double qc[4] = {__longlong_as_double(static_cast<long long>(c0)),
-                        __longlong_as_double(static_cast<long long>(c1)),
-                        __longlong_as_double(static_cast<long long>(c2)),
-                        __longlong_as_double(static_cast<long long>(c3))};
-  double w[4];
-  par::primitive(G.g1, qc, w);
-  constexpr double lo = 0x1p-64, hi = 0x1p64;
-  bool u = w[0] >= lo && w[0] <= hi && w[3] >= lo && w[3] <= hi &&
-           w[1] * w[1] + w[2] * w[2] <= 64.0 * (G.gamma * w[3] / w[0]);
+  bool u = false;
+  if (gi < G.nx && gj < G.ny) {
+    const unsigned long long c0 = key[0][ty + 3][tx + 3], c1 = key[1][ty + 3][tx + 3];
+    const unsigned long long c2 = key[2][ty + 3][tx + 3], c3 = key[3][ty + 3][tx + 3];
+    const double qc[4] = {__longlong_as_double(static_cast<long long>(c0)),
+                          __longlong_as_double(static_cast<long long>(c1)),
+                          __longlong_as_double(static_cast<long long>(c2)),
+                          __longlong_as_double(static_cast<long long>(c3))};
+    double w[4];
+    par::primitive(G.g1, qc, w);
+    constexpr double lo = 0x1p-64, hi = 0x1p64;
+    u = w[0] >= lo && w[0] <= hi && w[3] >= lo && w[3] <= hi &&
+        w[1] * w[1] + w[2] * w[2] <= 64.0 * (G.gamma * w[3] / w[0]);
 #pragma unroll
-  for (int dy = 0; dy < 7; ++dy)
+    for (int dy = 0; dy < 7; ++dy)
 #pragma unroll
-    for (int dx = 0; dx < 7; ++dx)
-      u &= key[0][ty + dy][tx + dx] == c0 && key[1][ty + dy][tx + dx] == c1 &&
-           key[2][ty + dy][tx + dx] == c2 && key[3][ty + dy][tx + dx] == c3;
-  deep[size_t(gj) * G.nx + gi] = u ? 1 : 0;
+      for (int dx = 0; dx < 7; ++dx)
+        u &= key[0][ty + dy][tx + dx] == c0 && key[1][ty + dy][tx + dx] == c1 &&
+             key[2][ty + dy][tx + dx] == c2 && key[3][ty + dy][tx + dx] == c3;
+    deep[size_t(gj) * G.nx + gi] = u ? 1 : 0;
+  }
+  // cells given their zero residual this stage (every thread reaches the count)
+  const int n = __syncthreads_count(u);
+  if (threadIdx.x == 0 && n && st) atomicAdd(&st->uniform, (unsigned long long)n);
 }
 
 template <int DIR>
@@ -555,8 +560,11 @@ extern "C" int hteno_residual_noalloc(const hteno_config* cfg, const double* q, 
   if (c.dims != 2 || c.scheme != HTENO_SCHEME_FV || c.precision != HTENO_PREC_FP64)
     return HTENO_ERR_UNSUPPORTED;
   if (c.nx < 6 || c.ny < 6 || !(c.xr > c.xl) || !(c.yt > c.yb) || !(c.gamma > 1.0) ||
-      c.recon < 0 || c.recon > 2 || c.flux < 0 || c.flux > 1 || c.bc < 0 || c.bc > 1)
+      c.recon < HTENO_RECON_TENO5 || c.recon > HTENO_RECON_TENO5A || c.flux < 0 || c.flux > 1 ||
+      c.bc < HTENO_BC_ZEROGRAD || c.bc > HTENO_BC_DOUBLE_MACH)
     return HTENO_ERR_INVALID_ARG;
+  // the Taylor and double-Mach boundaries need ghost face rows beyond the scratch layout
+  if (c.bc >= HTENO_BC_TAYLOR) return HTENO_ERR_UNSUPPORTED;
   // size limit of the fixed scratch array
   if ((long long)c.nx * c.ny > kNoAllocMaxCells || c.nx + c.ny > kNoAllocMaxEdge)
     return HTENO_ERR_INVALID_ARG;
@@ -578,7 +586,7 @@ extern "C" int hteno_residual_noalloc(const hteno_config* cfg, const double* q, 
   }
   if (upload_const(c_dev, &g_noalloc_const, &g_mu) != cudaSuccess) return HTENO_ERR_CUDA;
 
-  Geo G;
+  Geo G{};  // every field set, as geo_of() sets them for a solver
   G.nx = c.nx;
   G.ny = c.ny;
   G.bc = c.bc;
@@ -589,6 +597,10 @@ extern "C" int hteno_residual_noalloc(const hteno_config* cfg, const double* q, 
   G.area = G.dx * G.dy;
   G.gamma = c.gamma;
   G.g1 = c.gamma - 1.0;
+  G.x0 = c.xl;
+  G.y0 = c.yb;
+  G.t0 = c.t_init;
+  fill_bc_consts(c.gamma, G.bq, &G.ctan, &G.c16, &G.s3);
   const Work<double> W = carve<double>(scratch, c.nx, c.ny);
   cudaStream_t cs = static_cast<cudaStream_t>(stream);
   const long nxf = long(c.nx + 1) * c.ny, nyf = long(c.ny + 1) * c.nx;

@@ -275,6 +275,8 @@ __device__ __forceinline__ double tile_stage(const DevConst& C, const Geo& G, in
     }
     flat = __syncthreads_and(same) &&
            tame_state(S.q[0][0][0], S.q[1][0][0], S.q[2][0][0], S.q[3][0][0], g1, float(G.gamma));
+    if (flat && stage > 0 && tid == 0)  // cells of the tile given their zero residual
+      atomicAdd(&a.st->uniform, (unsigned long long)(min(TX, G.nx - i0) * min(TY, G.ny - j0)));
   }
 
   if (!flat) {

@@ -25,8 +25,9 @@ int hermite2d_setup(hteno_solver* s) {
                                                        : work_bytes_h<double>(nx, ny);
   cudaError_t e = cudaMalloc(&s->work, s->work_bytes);
   if (e != cudaSuccess) return cuda_error(s, e, "work buffer");
-  cudaMemset(s->v, 0, s->ncell * 4 * sizeof(double));
-  cudaMemset(s->w, 0, s->ncell * 4 * sizeof(double));
+  e = cudaMemset(s->v, 0, s->ncell * 4 * sizeof(double));
+  if (e == cudaSuccess) e = cudaMemset(s->w, 0, s->ncell * 4 * sizeof(double));
+  if (e != cudaSuccess) return cuda_error(s, e, "moment buffers");
   s->launches_per_step = 2 + 3 * 7;
   return HTENO_OK;
 }

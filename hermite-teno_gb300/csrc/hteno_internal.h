@@ -24,6 +24,7 @@ struct StepState {
   long long steps;   // completed steps
   int done;          // 1 once t >= t_final: the remaining launches of the call are no-ops
   int status;        // bit 0: NaN seen; bit 1: non-positive density/pressure seen
+  unsigned long long uniform;  // cell-stages given their exactly zero residual (uniform regions)
 };
 
 // Per-device upload of the constant block of one translation unit.

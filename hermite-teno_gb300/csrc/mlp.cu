@@ -50,8 +50,9 @@ struct Smem {
   alignas(128) unsigned char w3t[32 * 16 * 2];
   alignas(128) unsigned char w2t[32 * 32 * 2];
   float b1[32], b2[32], b3[16];
-  float gb1[32], gb2[32], gb3[16];
-  float loss;
+  // bias gradients and loss, one slot per warp (summed in warp order at the end: deterministic)
+  float gb1[4][32], gb2[4][32], gb3[4][16];
+  float loss[4];
   alignas(8) uint64_t mbar;
   uint32_t tmem;
   static constexpr bool kTrain = true;
@@ -121,8 +122,8 @@ __device__ void load_weights(SM& S, const Weights& W) {
 // Issue (thread 0) after a barrier; every thread then waits for completion.  Returns false on
 // timeout (uniform over the block).
 template <typename SM>
-__device__ __forceinline__ bool wait_mma(SM& S, uint32_t& phase) {
-  const bool ok = !__syncthreads_or(!tc::mbar_wait(&S.mbar, phase, kWaitLimit));
+__device__ __forceinline__ bool wait_mma(SM& S, uint32_t& phase, uint32_t limit) {
+  const bool ok = !__syncthreads_or(!tc::mbar_wait(&S.mbar, phase, limit));
   if (ok) phase ^= 1u;  // on timeout `phase` stays the pending one
   tc::fence_after();
   return ok;
@@ -146,7 +147,7 @@ __device__ __forceinline__ float warp_sum(float v) {
 // keep_t: also store H1^T / H2^T (needed by the weight gradients).
 template <typename SM>
 __device__ __forceinline__ bool forward(SM& S, uint32_t tbase, uint32_t& phase, float* h1,
-                                        float* h2, float* z3, bool keep_t) {
+                                        float* h2, float* z3, bool keep_t, uint32_t limit) {
   const int row = threadIdx.x;
   const uint32_t lane_addr = tbase + (uint32_t(threadIdx.x & ~31) << 16);
   before_issue();
@@ -155,7 +156,7 @@ __device__ __forceinline__ bool forward(SM& S, uint32_t tbase, uint32_t& phase, 
     tc::mma_bf16(tbase + C_D1, desc_k(S.x, 16, 0), desc_k(S.w1, 16, 0), tc::idesc_bf16(128, 32), 0);
     tc::commit(&S.mbar);
   }
-  if (!wait_mma(S, phase)) return false;
+  if (!wait_mma(S, phase, limit)) return false;
   tc::tmem_ld16(lane_addr + C_D1, h1);
   tc::tmem_ld16(lane_addr + C_D1 + 16, h1 + 16);
 #pragma unroll
@@ -172,7 +173,7 @@ __device__ __forceinline__ bool forward(SM& S, uint32_t tbase, uint32_t& phase, 
       tc::mma_bf16(tbase + C_D2, desc_k(S.h1, 32, s), desc_k(S.w2, 32, s), tc::idesc_bf16(128, 32), s);
     tc::commit(&S.mbar);
   }
-  if (!wait_mma(S, phase)) return false;
+  if (!wait_mma(S, phase, limit)) return false;
   tc::tmem_ld16(lane_addr + C_D2, h2);
   tc::tmem_ld16(lane_addr + C_D2 + 16, h2 + 16);
 #pragma unroll
@@ -189,7 +190,7 @@ __device__ __forceinline__ bool forward(SM& S, uint32_t tbase, uint32_t& phase, 
       tc::mma_bf16(tbase + C_D3, desc_k(S.h2, 32, s), desc_k(S.w3, 32, s), tc::idesc_bf16(128, 16), s);
     tc::commit(&S.mbar);
   }
-  if (!wait_mma(S, phase)) return false;
+  if (!wait_mma(S, phase, limit)) return false;
   float d3[16];
   tc::tmem_ld16(lane_addr + C_D3, d3);
 #pragma unroll
@@ -227,7 +228,7 @@ __device__ __forceinline__ void hidden_row(uint32_t taddr, const float* b, unsig
 // (6 BF16 features in .x .y .z); n valid rows in all, tiles beyond them are not computed.  Leaves
 // the three output logits of each of its rows in z.  Returns false on a timed-out wait (uniform).
 __device__ __forceinline__ bool forward_rows(SmemC& S, uint32_t tbase, uint32_t& phase, const uint4* in,
-                                             int n, float (*z)[3]) {
+                                             int n, float (*z)[3], uint32_t limit) {
   const int row = threadIdx.x;
   const int ntile = (n + 127) >> 7;
   const uint32_t lane_addr = tbase + (uint32_t(threadIdx.x & ~31) << 16);
@@ -244,7 +245,7 @@ __device__ __forceinline__ bool forward_rows(SmemC& S, uint32_t tbase, uint32_t&
       tc::mma_bf16(tbase + 32 * t, desc_k(S.buf[t], 16, 0), desc_k(S.w1, 16, 0), tc::idesc_bf16(128, 32), 0);
     tc::commit(&S.mbar);
   }
-  if (!wait_mma(S, phase)) return false;
+  if (!wait_mma(S, phase, limit)) return false;
 #pragma unroll
   for (int t = 0; t < kCT; ++t)
     if (t < ntile) hidden_row(lane_addr + 32 * t, S.b1, S.buf[t], row);
@@ -256,7 +257,7 @@ __device__ __forceinline__ bool forward_rows(SmemC& S, uint32_t tbase, uint32_t&
         tc::mma_bf16(tbase + 32 * t, desc_k(S.buf[t], 32, k), desc_k(S.w2, 32, k), tc::idesc_bf16(128, 32), k);
     tc::commit(&S.mbar);
   }
-  if (!wait_mma(S, phase)) return false;
+  if (!wait_mma(S, phase, limit)) return false;
 #pragma unroll
   for (int t = 0; t < kCT; ++t)
     if (t < ntile) hidden_row(lane_addr + 32 * t, S.b2, S.buf[t], row);
@@ -268,7 +269,7 @@ __device__ __forceinline__ bool forward_rows(SmemC& S, uint32_t tbase, uint32_t&
         tc::mma_bf16(tbase + 32 * t, desc_k(S.buf[t], 32, k), desc_k(S.w3, 32, k), tc::idesc_bf16(128, 16), k);
     tc::commit(&S.mbar);
   }
-  if (!wait_mma(S, phase)) return false;
+  if (!wait_mma(S, phase, limit)) return false;
 #pragma unroll
   for (int t = 0; t < kCT; ++t)
     if (t < ntile) {
@@ -299,12 +300,12 @@ __device__ void setup(SM& S, const Weights& W) {
   }
   load_weights(S, W);
   if constexpr (SM::kTrain) {
-    if (threadIdx.x < 32) {
-      S.gb1[threadIdx.x] = 0.f;
-      S.gb2[threadIdx.x] = 0.f;
-      if (threadIdx.x < 16) S.gb3[threadIdx.x] = 0.f;
+    for (int e = threadIdx.x; e < 4 * 32; e += blockDim.x) {
+      S.gb1[e / 32][e % 32] = 0.f;
+      S.gb2[e / 32][e % 32] = 0.f;
+      if (e % 32 < 16) S.gb3[e / 32][e % 32] = 0.f;
     }
-    if (threadIdx.x == 0) S.loss = 0.f;
+    if (threadIdx.x < 4) S.loss[threadIdx.x] = 0.f;
   }
   if (threadIdx.x == 0) {
     tc::mbar_init(&S.mbar, 1);
@@ -324,17 +325,20 @@ __device__ void teardown(SM& S, uint32_t tbase) {
   if (threadIdx.x < 32) tc::tmem_dealloc(tbase, SM::kTmemCols);
 }
 
-// Gradient of the mean BCE loss over `n_total` rows, accumulated into G (padded layout).
+// Gradient of the mean BCE loss over `n_total` rows: each CTA writes its partial gradient (padded
+// layout) to Gp[blockIdx.x] and its partial loss sum to Lp[blockIdx.x]; k_reduce_grad adds the
+// partials in CTA order, so the gradient does not depend on the order in which CTAs finish.
+// `limit`: polls of each tensor-core completion wait before the kernel gives up.
 __global__ void __launch_bounds__(128) k_train(Weights W, const uint16_t* __restrict__ X,
                                                const uint8_t* __restrict__ Y, long n, long n_total,
-                                               float* __restrict__ G, float* __restrict__ loss,
-                                               int* __restrict__ err) {
+                                               float* __restrict__ Gp, float* __restrict__ Lp,
+                                               int* __restrict__ err, uint32_t limit) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   Smem& S = *reinterpret_cast<Smem*>(smem_raw);
   setup(S, W);
   const uint32_t tbase = S.tmem;
   const uint32_t lane_addr = tbase + (uint32_t(threadIdx.x & ~31) << 16);
-  const int row = threadIdx.x, lane = threadIdx.x & 31;
+  const int row = threadIdx.x, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const float inv_n = 1.0f / float(n_total);
   uint32_t phase = 0;
   bool ok = true;
@@ -354,7 +358,7 @@ __global__ void __launch_bounds__(128) k_train(Weights W, const uint16_t* __rest
     }
     put_input(S, row, f);
     float h1[32], h2[32], z3[3];
-    ok = forward(S, tbase, phase, h1, h2, z3, true);
+    ok = forward(S, tbase, phase, h1, h2, z3, true, limit);
     if (!ok) break;
     // loss and dZ3
     float dz3[3], l = 0.f;
@@ -368,7 +372,7 @@ __global__ void __launch_bounds__(128) k_train(Weights W, const uint16_t* __rest
     }
     if (!valid) l = 0.f;
     l = warp_sum(l);
-    if (lane == 0) atomicAdd(&S.loss, l);
+    if (lane == 0) S.loss[warp] += l;
 #pragma unroll
     for (int k = 0; k < 16; ++k) {
       const float v = k < 3 ? dz3[k] : 0.f;
@@ -379,7 +383,7 @@ __global__ void __launch_bounds__(128) k_train(Weights W, const uint16_t* __rest
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
       const float s = warp_sum(rbf(dz3[k]));
-      if (lane == 0) atomicAdd(&S.gb3[k], s);
+      if (lane == 0) S.gb3[warp][k] += s;
     }
     before_issue();
     if (threadIdx.x == 0) {
@@ -390,7 +394,7 @@ __global__ void __launch_bounds__(128) k_train(Weights W, const uint16_t* __rest
                      (tiles_done > 0 || s > 0) ? 1 : 0);
       tc::commit(&S.mbar);
     }
-    if (!(ok = wait_mma(S, phase))) break;
+    if (!(ok = wait_mma(S, phase, limit))) break;
     // dZ2
     float d[32];
     tc::tmem_ld16(lane_addr + C_DH2, d);
@@ -401,7 +405,7 @@ __global__ void __launch_bounds__(128) k_train(Weights W, const uint16_t* __rest
       tc::st_bf16(S.dz2, tc::kmaj(row, c, 32), v);
       tc::st_bf16(S.at, tc::kmaj(c, row, 128), v);
       const float s = warp_sum(rbf(v));
-      if (lane == 0) atomicAdd(&S.gb2[c], s);
+      if (lane == 0) S.gb2[warp][c] += s;
     }
     before_issue();
     if (threadIdx.x == 0) {
@@ -413,7 +417,7 @@ __global__ void __launch_bounds__(128) k_train(Weights W, const uint16_t* __rest
                      (tiles_done > 0 || s > 0) ? 1 : 0);
       tc::commit(&S.mbar);
     }
-    if (!(ok = wait_mma(S, phase))) break;
+    if (!(ok = wait_mma(S, phase, limit))) break;
     // dZ1
     tc::tmem_ld16(lane_addr + C_DH1, d);
     tc::tmem_ld16(lane_addr + C_DH1 + 16, d + 16);
@@ -422,7 +426,7 @@ __global__ void __launch_bounds__(128) k_train(Weights W, const uint16_t* __rest
       const float v = h1[c] > 0.f ? d[c] : 0.f;
       tc::st_bf16(S.at, tc::kmaj(c, row, 128), v);
       const float s = warp_sum(rbf(v));
-      if (lane == 0) atomicAdd(&S.gb1[c], s);
+      if (lane == 0) S.gb1[warp][c] += s;
     }
     before_issue();
     if (threadIdx.x == 0) {
@@ -432,37 +436,42 @@ __global__ void __launch_bounds__(128) k_train(Weights W, const uint16_t* __rest
                      (tiles_done > 0 || s > 0) ? 1 : 0);
       tc::commit(&S.mbar);
     }
-    if (!(ok = wait_mma(S, phase))) break;
+    if (!(ok = wait_mma(S, phase, limit))) break;
   }
   if (!ok) {
     if (threadIdx.x == 0) atomicExch(err, 1);
     // give in-flight MMAs a bounded chance to finish before the columns are released
     tc::mbar_wait(&S.mbar, phase, kWaitLimit);
-  } else if (tiles_done > 0) {
-    // weight gradients: rows of the accumulators live in lanes 0..31 (warp 0)
-    if (threadIdx.x < 32) {
-      float v[16];
-      for (int h = 0; h < 2; ++h) {
-        tc::tmem_ld16(lane_addr + C_GW3 + 16 * h, v);
-        if (row < 3)
-          for (int c = 0; c < 16; ++c) atomicAdd(&G[kOffW3 + row * 32 + 16 * h + c], v[c]);
-        tc::tmem_ld16(lane_addr + C_GW2 + 16 * h, v);
-        for (int c = 0; c < 16; ++c) atomicAdd(&G[kOffW2 + row * 32 + 16 * h + c], v[c]);
-      }
-      tc::tmem_ld16(lane_addr + C_GW1, v);
-      for (int c = 0; c < 6; ++c) atomicAdd(&G[kOffW1 + row * 16 + c], v[c]);
-      atomicAdd(&G[kOffB1 + row], S.gb1[row]);
-      atomicAdd(&G[kOffB2 + row], S.gb2[row]);
-      if (row < 3) atomicAdd(&G[kOffB3 + row], S.gb3[row]);
-      if (row == 0) atomicAdd(loss, S.loss);
+  }
+  // this CTA's partial gradient, every entry of the padded layout written once: rows of the
+  // accumulators live in lanes 0..31 (warp 0).  The padded entries are exact zeros (zero input
+  // columns 6..15, zero output rows 3..15); a CTA without a completed tile writes zeros.
+  if (threadIdx.x < 32) {
+    const bool have = ok && tiles_done > 0;
+    float* g = Gp + size_t(blockIdx.x) * kParams;
+    float v[16];
+    for (int h = 0; h < 2; ++h) {
+      if (have) tc::tmem_ld16(lane_addr + C_GW3 + 16 * h, v);
+      if (row < 16)
+        for (int c = 0; c < 16; ++c) g[kOffW3 + row * 32 + 16 * h + c] = have ? v[c] : 0.f;
+      if (have) tc::tmem_ld16(lane_addr + C_GW2 + 16 * h, v);
+      for (int c = 0; c < 16; ++c) g[kOffW2 + row * 32 + 16 * h + c] = have ? v[c] : 0.f;
     }
+    if (have) tc::tmem_ld16(lane_addr + C_GW1, v);
+    for (int c = 0; c < 16; ++c) g[kOffW1 + row * 16 + c] = have ? v[c] : 0.f;
+    g[kOffB1 + row] = have ? ((S.gb1[0][row] + S.gb1[1][row]) + S.gb1[2][row]) + S.gb1[3][row] : 0.f;
+    g[kOffB2 + row] = have ? ((S.gb2[0][row] + S.gb2[1][row]) + S.gb2[2][row]) + S.gb2[3][row] : 0.f;
+    if (row < 16)
+      g[kOffB3 + row] = have ? ((S.gb3[0][row] + S.gb3[1][row]) + S.gb3[2][row]) + S.gb3[3][row] : 0.f;
+    if (row == 0) Lp[blockIdx.x] = have ? ((S.loss[0] + S.loss[1]) + S.loss[2]) + S.loss[3] : 0.f;
   }
   teardown(S, tbase);
 }
 
 // Probabilities of the three cut-off bits for n rows (rounds of kCRound rows per CTA).
 __global__ void __launch_bounds__(128, 4) k_predict(Weights W, const uint16_t* __restrict__ X, long n,
-                                                    float* __restrict__ P, int* __restrict__ err) {
+                                                    float* __restrict__ P, int* __restrict__ err,
+                                                    uint32_t limit) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   SmemC& S = *reinterpret_cast<SmemC*>(smem_raw);
   setup(S, W);
@@ -480,7 +489,7 @@ __global__ void __launch_bounds__(128, 4) k_predict(Weights W, const uint16_t* _
       const int k = t * 128 + int(threadIdx.x);
       in[t] = k < m ? *reinterpret_cast<const uint4*>(X + (base + k) * 8) : make_uint4(0u, 0u, 0u, 0u);
     }
-    ok = forward_rows(S, tbase, phase, in, m, z);
+    ok = forward_rows(S, tbase, phase, in, m, z, limit);
     if (ok)
 #pragma unroll
       for (int t = 0; t < kCT; ++t) {
@@ -666,7 +675,7 @@ __global__ void __launch_bounds__(128, 4) k_route_rows(Weights W, const uint4* _
                                                        const unsigned long long* __restrict__ nrows,
                                                        long cap, long nxf, uint8_t* __restrict__ mx,
                                                        uint8_t* __restrict__ my, float zthr,
-                                                       int* __restrict__ err) {
+                                                       int* __restrict__ err, uint32_t limit) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   SmemC& S = *reinterpret_cast<SmemC*>(smem_raw);
   const long n = long(min(*nrows, (unsigned long long)cap));
@@ -692,7 +701,7 @@ __global__ void __launch_bounds__(128, 4) k_route_rows(Weights W, const uint4* _
     const int m = int(n - base < kCRound ? n - base : kCRound);
     fetch(rd + gridDim.x, next);  // in flight during this round's products
     float z[kCT][3];
-    ok = forward_rows(S, tbase, phase, in, m, z);
+    ok = forward_rows(S, tbase, phase, in, m, z, limit);
     if (ok)
 #pragma unroll
       for (int t = 0; t < kCT; ++t) {
@@ -714,7 +723,7 @@ __global__ void __launch_bounds__(128, 4) k_route_rows(Weights W, const uint4* _
   teardown(S, tbase);
 }
 
-// Adam on the FP32 master parameters (padded layout), then the BF16 images; zeroes G.
+// Adam on the FP32 master parameters (padded layout), then the BF16 images.
 __global__ void k_adam(float* __restrict__ P, float* __restrict__ G, float* __restrict__ M,
                        float* __restrict__ V, float lr, float b1, float b2, float eps, int t) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -726,7 +735,22 @@ __global__ void k_adam(float* __restrict__ P, float* __restrict__ G, float* __re
   V[i] = v;
   const float mh = m / (1.f - powf(b1, float(t))), vh = v / (1.f - powf(b2, float(t)));
   P[i] -= lr * mh / (sqrtf(vh) + eps);
-  G[i] = 0.f;
+}
+
+// G = the sum of the nblk per-CTA partial gradients, added in CTA order; *loss += the sum of the
+// partial losses in CTA order (one thread).  Deterministic for a given grid.
+__global__ void k_reduce_grad(const float* __restrict__ Gp, const float* __restrict__ Lp, int nblk,
+                              float* __restrict__ G, float* __restrict__ loss) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < kParams) {
+    float s = 0.f;
+    for (int b = 0; b < nblk; ++b) s += Gp[size_t(b) * kParams + i];
+    G[i] = s;
+  } else if (i == kParams) {
+    float s = 0.f;
+    for (int b = 0; b < nblk; ++b) s += Lp[b];
+    *loss += s;
+  }
 }
 
 __global__ void k_images(const float* __restrict__ P, Weights W) {
@@ -780,13 +804,16 @@ using namespace hteno::mlp;
 struct hteno_mlp {
   Weights W{};          // device images
   float* P = nullptr;   // FP32 master parameters (padded)
-  float* G = nullptr;   // gradient accumulator (padded)
+  float* G = nullptr;   // gradient (padded), the ordered sum of the per-CTA partials
+  float* Gp = nullptr;  // per-CTA partial gradients [2 * sms][kParams] and partial losses
+  float* Lp = nullptr;
   float* M = nullptr;   // Adam moments
   float* V = nullptr;
   float* loss = nullptr;
   int* err = nullptr;
   void* img = nullptr;  // backing store of W
   int t = 0;            // Adam step
+  uint32_t wait_limit = kWaitLimit;  // polls of a tensor-core completion wait
   int sms = 148;
   cudaStream_t stream = nullptr;
   std::string msg;
@@ -875,7 +902,7 @@ int mlp_classify(hteno_mlp* m, const Geo& G, const double* q, uint8_t* mx, uint8
   }
   const float zthr = std::log(thr / (1.0f - thr));  // sigmoid(z) > thr  <=>  z > logit(thr)
   k_route_rows<<<4 * m->sms, 128, mlp::kSmemCBytes, st>>>(m->W, rows, nrows, cap, nxf, mx, my, zthr,
-                                                          m->err);
+                                                          m->err, m->wait_limit);
   return cudaGetLastError() == cudaSuccess ? HTENO_OK : HTENO_ERR_CUDA;
 }
 
@@ -898,26 +925,27 @@ int hteno_mlp_create(unsigned long long seed, hteno_mlp** out) {
   if (!m) return HTENO_ERR_OOM;
   auto fail = [&](int code) {
     cudaFree(m->P); cudaFree(m->G); cudaFree(m->M); cudaFree(m->V); cudaFree(m->loss);
-    cudaFree(m->err); cudaFree(m->img);
+    cudaFree(m->err); cudaFree(m->img); cudaFree(m->Gp); cudaFree(m->Lp);
     if (m->stream) cudaStreamDestroy(m->stream);
     delete m;
     return code;
   };
   if (set_attr() != HTENO_OK) return fail(HTENO_ERR_CUDA);
   if (cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking) != cudaSuccess) return fail(HTENO_ERR_CUDA);
+  int dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&m->sms, cudaDevAttrMultiProcessorCount, dev);
   const size_t pb = kParams * sizeof(float);
   if (cudaMalloc(&m->P, pb) || cudaMalloc(&m->G, pb) || cudaMalloc(&m->M, pb) || cudaMalloc(&m->V, pb) ||
       cudaMalloc(&m->loss, sizeof(float)) || cudaMalloc(&m->err, sizeof(int)) ||
-      cudaMalloc(&m->img, kImageBytes))
+      cudaMalloc(&m->img, kImageBytes) || cudaMalloc(&m->Gp, 2 * size_t(m->sms) * pb) ||
+      cudaMalloc(&m->Lp, 2 * size_t(m->sms) * sizeof(float)))
     return fail(HTENO_ERR_OOM);
   char* b = static_cast<char*>(m->img);
   m->W.w1 = b; m->W.w2 = b + 1024; m->W.w3 = b + 3072; m->W.w3t = b + 4096; m->W.w2t = b + 5120;
   m->W.b1 = reinterpret_cast<float*>(b + 7168);
   m->W.b2 = m->W.b1 + 32;
   m->W.b3 = m->W.b2 + 32;
-  int dev = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&m->sms, cudaDevAttrMultiProcessorCount, dev);
   // He-uniform initialisation of the weights, zero biases
   std::mt19937_64 rng(seed);
   std::vector<float> c(kPublicParams, 0.f), p(kParams);
@@ -940,7 +968,7 @@ int hteno_mlp_destroy(hteno_mlp* m) {
   if (!m) return HTENO_ERR_INVALID_ARG;
   cudaStreamSynchronize(m->stream);
   cudaFree(m->P); cudaFree(m->G); cudaFree(m->M); cudaFree(m->V); cudaFree(m->loss);
-  cudaFree(m->err); cudaFree(m->img);
+  cudaFree(m->err); cudaFree(m->img); cudaFree(m->Gp); cudaFree(m->Lp);
   cudaStreamDestroy(m->stream);
   delete m;
   return HTENO_OK;
@@ -976,11 +1004,12 @@ int hteno_mlp_get_params(hteno_mlp* m, float* params) {
 // the public layout (host), *loss = mean loss.
 int hteno_mlp_grad(hteno_mlp* m, const uint16_t* x, const uint8_t* y, long n, float* grads, float* loss) {
   if (!m || !x || !y || n <= 0 || !grads) return HTENO_ERR_INVALID_ARG;
-  cudaMemsetAsync(m->G, 0, kParams * sizeof(float), m->stream);
   cudaMemsetAsync(m->loss, 0, sizeof(float), m->stream);
   const long tiles = (n + 127) / 128;
   const int grid = int(std::min<long>(tiles, 2L * m->sms));
-  k_train<<<grid, 128, mlp::smem_bytes(), m->stream>>>(m->W, x, y, n, n, m->G, m->loss, m->err);
+  k_train<<<grid, 128, mlp::smem_bytes(), m->stream>>>(m->W, x, y, n, n, m->Gp, m->Lp, m->err,
+                                                       m->wait_limit);
+  k_reduce_grad<<<(kParams + 256) / 256, 256, 0, m->stream>>>(m->Gp, m->Lp, grid, m->G, m->loss);
   int rc = merr(m, cudaGetLastError(), "k_train");
   if (rc) return rc;
   rc = check_err(m);
@@ -993,7 +1022,6 @@ int hteno_mlp_grad(hteno_mlp* m, const uint16_t* x, const uint8_t* y, long n, fl
   if (e != cudaSuccess) return merr(m, e, "grad copy");
   from_padded(g.data(), grads);
   if (loss) *loss = l / float(n);
-  cudaMemsetAsync(m->G, 0, kParams * sizeof(float), m->stream);
   return HTENO_OK;
 }
 
@@ -1009,8 +1037,9 @@ int hteno_mlp_train(hteno_mlp* m, const uint16_t* x, const uint8_t* y, long n, i
       const long nb = std::min(batch, n - off);
       const long tiles = (nb + 127) / 128;
       const int grid = int(std::min<long>(tiles, 2L * m->sms));
-      k_train<<<grid, 128, mlp::smem_bytes(), m->stream>>>(m->W, x + off * 8, y + off, nb, nb, m->G,
-                                                           m->loss, m->err);
+      k_train<<<grid, 128, mlp::smem_bytes(), m->stream>>>(m->W, x + off * 8, y + off, nb, nb, m->Gp,
+                                                           m->Lp, m->err, m->wait_limit);
+      k_reduce_grad<<<(kParams + 256) / 256, 256, 0, m->stream>>>(m->Gp, m->Lp, grid, m->G, m->loss);
       ++m->t;
       k_adam<<<(kParams + 255) / 256, 256, 0, m->stream>>>(m->P, m->G, m->M, m->V, lr, 0.9f, 0.999f,
                                                            1e-8f, m->t);
@@ -1033,7 +1062,7 @@ int hteno_mlp_predict(hteno_mlp* m, const uint16_t* x, long n, float* p) {
   if (!m || !x || n <= 0 || !p) return HTENO_ERR_INVALID_ARG;
   const long rounds = (n + mlp::kCRound - 1) / mlp::kCRound;
   const int grid = int(std::min<long>(rounds, 4L * m->sms));
-  k_predict<<<grid, 128, mlp::kSmemCBytes, m->stream>>>(m->W, x, n, p, m->err);
+  k_predict<<<grid, 128, mlp::kSmemCBytes, m->stream>>>(m->W, x, n, p, m->err, m->wait_limit);
   const int rc = merr(m, cudaGetLastError(), "k_predict");
   return rc ? rc : check_err(m);
 }
@@ -1044,6 +1073,12 @@ int hteno_mlp_pack(hteno_mlp* m, const float* in, uint16_t* out, long n) {
   k_pack_inputs<<<unsigned((n + 255) / 256), 256, 0, m->stream>>>(in, out, n);
   const int rc = merr(m, cudaGetLastError(), "pack");
   return rc ? rc : merr(m, cudaStreamSynchronize(m->stream), "pack");
+}
+
+int hteno_mlp_set_wait_limit(hteno_mlp* m, unsigned int polls) {
+  if (!m) return HTENO_ERR_INVALID_ARG;
+  m->wait_limit = polls;
+  return HTENO_OK;
 }
 
 const char* hteno_mlp_last_error(hteno_mlp* m) { return m ? m->msg.c_str() : "null handle"; }

@@ -263,6 +263,7 @@ int hteno_set_state(hteno_solver* s, const double* q, int where) {
   s->hstate->steps = 0;
   s->hstate->done = 0;
   s->hstate->status = 0;
+  s->hstate->uniform = 0;
   cudaError_t e = cudaMemcpyAsync(s->dstate, s->hstate, sizeof(StepState), cudaMemcpyHostToDevice,
                                   s->stream);
   if (e != cudaSuccess) return cuda_error(s, e, "state reset");
@@ -357,6 +358,16 @@ int hteno_get_status(hteno_solver* s, int* flags) {
   if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
   if (e != cudaSuccess) return cuda_error(s, e, "get_status");
   *flags = s->hstate->status;
+  return HTENO_OK;
+}
+
+int hteno_get_uniform_cells(hteno_solver* s, long long* cells) {
+  if (!s || !cells) return HTENO_ERR_INVALID_ARG;
+  cudaError_t e = cudaMemcpyAsync(s->hstate, s->dstate, sizeof(StepState), cudaMemcpyDeviceToHost,
+                                  s->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+  if (e != cudaSuccess) return cuda_error(s, e, "get_uniform_cells");
+  *cells = static_cast<long long>(s->hstate->uniform);
   return HTENO_OK;
 }
 

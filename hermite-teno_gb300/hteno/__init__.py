@@ -95,6 +95,7 @@ def lib() -> ctypes.CDLL:
         L.hteno_measure_fma_peak.argtypes = [i, _D]
         L.hteno_get_status.argtypes = [vp, ctypes.POINTER(i)]
         L.hteno_set_strict.argtypes = [vp, i]
+        L.hteno_get_uniform_cells.argtypes = [vp, ctypes.POINTER(ctypes.c_longlong)]
         L.hteno_residual_noalloc.argtypes = [ctypes.POINTER(Config), vp, vp, vp]
         L.hteno_batch_create.argtypes = [ctypes.POINTER(Config), i, ctypes.POINTER(vp)]
         L.hteno_batch_destroy.argtypes = [vp]
@@ -121,6 +122,7 @@ def lib() -> ctypes.CDLL:
         L.hteno_mlp_train.argtypes = [vp, vp, vp, l, i, l, ctypes.c_float, vp]
         L.hteno_mlp_predict.argtypes = [vp, vp, l, vp]
         L.hteno_mlp_pack.argtypes = [vp, vp, vp, l]
+        L.hteno_mlp_set_wait_limit.argtypes = [vp, ctypes.c_uint]
         L.hteno_mlp_last_error.restype = ctypes.c_char_p
         L.hteno_mlp_last_error.argtypes = [vp]
         _lib = L
@@ -222,6 +224,13 @@ class Solver:
         f = ctypes.c_int()
         _check(lib().hteno_get_status(self.h, ctypes.byref(f)), self.h)
         return f.value
+
+    def uniform_cells(self) -> int:
+        """Cell-stages since set_state whose exactly zero residual was taken without computing
+        their faces (uniform regions, FV 2D)."""
+        n = ctypes.c_longlong()
+        _check(lib().hteno_get_uniform_cells(self.h, ctypes.byref(n)), self.h)
+        return n.value
 
     def set_strict(self, on: bool = True) -> None:
         _check(lib().hteno_set_strict(self.h, int(bool(on))), self.h)
@@ -391,6 +400,10 @@ class Mlp:
     def predict(self, x, out):
         self._check(lib().hteno_mlp_predict(self.h, x.data_ptr(), x.shape[0], out.data_ptr()))
         return out
+
+    def set_wait_limit(self, polls: int) -> None:
+        """Polls of each tensor-core completion wait before a call reports a timeout (test hook)."""
+        self._check(lib().hteno_mlp_set_wait_limit(self.h, int(polls)))
 
     def pack(self, xf, out):
         self._check(lib().hteno_mlp_pack(self.h, xf.data_ptr(), out.data_ptr(), xf.shape[0]))

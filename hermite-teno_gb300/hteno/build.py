@@ -94,7 +94,8 @@ def build_oracle(with_reference: bool | None = None) -> Path:
     """Compile the CPU oracle (test infrastructure) and, where the reference sources are present,
     the reference itself against the project's Eigen-subset header (oracle/_ref)."""
     _run(["make", "-s", "-C", str(ORACLE_DIR), "oracle"])
-    ref_src = os.environ.get("HTENO_REFERENCE_DIR", "/root/reference")
+    # the reference tree: HTENO_REFERENCE_DIR, else a "reference" directory beside the repository
+    ref_src = os.environ.get("HTENO_REFERENCE_DIR") or str(REPO_DIR.parent / "reference")
     if with_reference is None:
         with_reference = Path(ref_src, "FV_System2D.cpp").exists()
     if with_reference:

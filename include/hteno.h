@@ -138,6 +138,13 @@ int hteno_launches_per_step(hteno_solver* s, int* launches);
 int hteno_get_status(hteno_solver* s, int* flags);
 int hteno_set_strict(hteno_solver* s, int on);
 
+/* Cell-stages since the last hteno_set_state whose residual the FV 2D stepping took as exactly
+ * zero without computing their faces (uniform regions: the plain path's cells whose 7 x 7
+ * neighbourhood holds one tame state, the mixed path's tiles of one tame float state; the same
+ * bits as computing them).  A measurement aid with no reference counterpart: the reference
+ * computes every face. */
+int hteno_get_uniform_cells(hteno_solver* s, long long* cells);
+
 /* Message of the last failed call on this handle ("" if none). */
 const char* hteno_last_error(hteno_solver* s);
 const char* hteno_status_string(int status);
@@ -255,6 +262,12 @@ int hteno_mlp_train(hteno_mlp* m, const unsigned short* x, const unsigned char* 
 int hteno_mlp_predict(hteno_mlp* m, const unsigned short* x, long n, float* p);
 /* float rows [n][6] (device) -> BF16 rows [n][8] (device). */
 int hteno_mlp_pack(hteno_mlp* m, const float* in, unsigned short* out, long n);
+/* Polls of each tensor-core completion wait of the classifier's kernels before the call gives up
+ * with HTENO_ERR_TIMEOUT (default 2^22, far beyond any completion).  The kernel that gives up
+ * still waits, with the default bound, for its own products in flight and frees its tensor
+ * memory, so the handle stays usable.  A test hook for the bounded-wait path; no reference
+ * counterpart. */
+int hteno_mlp_set_wait_limit(hteno_mlp* m, unsigned int polls);
 const char* hteno_mlp_last_error(hteno_mlp* m);
 
 /* Learned routing of a mixed-precision FV 2D solver: before every step the classifier marks,
@@ -304,7 +317,9 @@ int hteno_measure_fma_peak(int kind, double* tflops);
  * code inside another framework's stream capture or memory pool, or hosts whose device footprint
  * must stay fixed after start-up.  No reference counterpart: the reference has no device and no
  * allocation constraints.
- *   cfg: dims 2, scheme FV, precision FP64; q, rhs: DEVICE pointers [4][ny][nx]; stream may be
+ *   cfg: dims 2, scheme FV, precision FP64, any recon (0..7) and flux, bc zero-gradient or
+ *   periodic (HTENO_BC_TAYLOR and HTENO_BC_DOUBLE_MACH need ghost face rows that the fixed array
+ *   does not hold: HTENO_ERR_UNSUPPORTED); q, rhs: DEVICE pointers [4][ny][nx]; stream may be
  *   NULL.  Asynchronous.
  * Limits: nx * ny <= HTENO_NOALLOC_MAX_CELLS and nx + ny <= HTENO_NOALLOC_MAX_EDGE; larger grids
  * return HTENO_ERR_INVALID_ARG.  Its work buffers live in one fixed array (about 6 MB) inside

@@ -27,6 +27,7 @@ def test_reference_arm_json_line(oracle):
     assert d["warmup"] >= 3  # the contract's minimum warm-up is enforced
     assert d["higher_is_better"] is True and d["dtype"] == "f64" and d["data"] == "synthetic"
     assert d["config"]["workload"].startswith("fv2d_fourquadrant_1024x1024")
+    assert d["config"]["timed_from_step"] == d["warmup"]  # timed after W steps from the initial state
     cb = d["cpu_baseline"]
     assert cb["kind"] in ("port", "reference") and cb["cores"] >= 1 and cb["value"] == d["value"]
     assert cb["unit"] == d["unit"] and cb["sample"]

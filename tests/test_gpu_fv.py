@@ -236,17 +236,28 @@ def periodic_box(nx, ny):
     return np.ascontiguousarray(ic.conservative2(1.0 + inside, 0.5 + 0 * X, -0.3 + 0 * X, 1.0 + 1.5 * inside))
 
 
-def test_fv2d_full_size_properties(hteno_lib, cuda):
-    """The 1024^2 benchmark configuration (HLLC, 200 steps): deterministic and positive; with
-    periodic boundaries the totals are conserved to rounding."""
+def test_fv2d_full_size_matches_oracle(hteno_lib, cuda, oracle):
+    """The 2D benchmark configuration exactly as specified: 1024^2 seeded four-quadrant data
+    (seed 0), TENO5 + HLLC, CFL 0.4, zero-gradient, 200 steps.  The GPU FP64 state against the
+    CPU oracle run on the host cores (OpenMP) inside the test: <= 1e-12 relative L-inf per
+    conserved variable, and bit for bit (the plain path reproduces the oracle's rounding).  A
+    second GPU run is identical (deterministic) and the density stays positive."""
     from hteno import ic
 
     q = ic.four_quadrant(1024, 1024, 0)
     a, t1, n1 = gpu_run2d(hteno_lib, q, 200, flux=1)
+    want, t_o, n_o = oracle.fv2d_run(q, 200, flux=1)
+    assert n1 == n_o == 200 and t1 == t_o
+    assert rel_linf(a, want) <= TOL
+    np.testing.assert_array_equal(a, want)
     b, t2, n2 = gpu_run2d(hteno_lib, q, 200, flux=1)
-    assert n1 == 200 and t1 == t2
+    assert n2 == 200 and t1 == t2
     np.testing.assert_array_equal(a, b)
     assert a[0].min() > 0
+
+
+def test_fv2d_full_size_properties(hteno_lib, cuda):
+    """With periodic boundaries the totals of a 1024^2 run are conserved to rounding."""
     p = periodic_box(1024, 1024)
     c, _, _ = gpu_run2d(hteno_lib, p, 50, flux=1, bc=1)
     assert np.isfinite(c).all() and c[0].min() > 0

@@ -62,6 +62,27 @@ def test_hermite2d_matches_oracle_bitwise(hteno_lib, cuda, oracle):
         np.testing.assert_array_equal(a, b)
 
 
+def test_hermite2d_full_size_matches_oracle(hteno_lib, cuda, oracle):
+    """The Hermite benchmark configuration at its stated size: 2048^2, 32 seeded Gaussian density
+    blobs on rho = p = 1 with a Mach-2 shock entering from x = 0, moments by face differences,
+    Rusanov, plain FP64, 3 steps; against the CPU oracle on the host cores: <= 1e-12 relative
+    L-inf per field, and bit for bit."""
+    from hteno import ic
+
+    n = 2048
+    f = ic.blobs_shock_fn(5)
+    x = (np.arange(n) + 0.5) / n
+    X, Y = np.meshgrid(x, x)
+    q = np.ascontiguousarray(f(X, Y))
+    v, w = ic.face_difference_moments(f, n, n, 0.0, 1.0, 0.0, 1.0)
+    qo, vo, wo, to, no = oracle.hermite2d_run(q, v, w, 3)
+    qg, vg, wg, tg, ng = run2(hteno_lib, q, v, w, 3, flux=hteno_lib.FLUX_RUSANOV)
+    assert ng == no == 3 and tg == to
+    for a, b in ((qg, qo), (vg, vo), (wg, wo)):
+        assert rel_linf(a, b) <= TOL
+        np.testing.assert_array_equal(a, b)
+
+
 def test_hermite2d_limiter_chunks_bitwise(hteno_lib, cuda, oracle):
     """Lines longer than the limiter's shared-memory chunk (64 cells) and line counts that are not
     multiples of its 32-line blocks: the chunked Gauss-Seidel sweep reproduces the oracle's."""

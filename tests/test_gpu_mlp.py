@@ -106,3 +106,49 @@ def test_mlp_learns_a_separable_rule(hteno_lib, cuda, mref):
     bits = np.stack([(y[ntr:] >> k) & 1 for k in range(3)], axis=1)
     acc = ((pr > 0.5) == bits).mean()
     assert loss < 0.5 * loss0 and acc >= 0.95, (loss0, loss, acc)
+
+
+def test_mlp_training_is_deterministic(hteno_lib, cuda, mref):
+    """Per-CTA partial gradients summed in CTA order: two trainings from the same seed on the same
+    rows give the same parameters bit for bit (and so the same router)."""
+    rng = np.random.default_rng(9)
+    n = 70000
+    x = rng.standard_normal((n, 6)) * 0.5
+    y = rng.integers(0, 8, size=n).astype(np.uint8)
+    _, xb = bf16_bits(x, mref)
+    xd, yd = to_dev(cuda, xb), to_dev(cuda, y)
+    params, losses = [], []
+    for _ in range(2):
+        with hteno_lib.Mlp(seed=4) as m:
+            losses.append(m.train(xd, yd, epochs=3, batch=8192, lr=3e-3))
+            params.append(m.params())
+    np.testing.assert_array_equal(params[0], params[1])
+    assert losses[0] == losses[1]
+
+
+def test_mlp_wait_timeout_reported_and_handle_recovers(hteno_lib, cuda, mref):
+    """The bounded tensor-core waits: with a limit of 0 polls every main-loop wait gives up at once;
+    the kernels then wait (with the default bound) for their own products in flight, free their
+    tensor memory and return, and the call reports HTENO_ERR_TIMEOUT.  The same handle then
+    predicts and computes gradients normally."""
+    rng = np.random.default_rng(3)
+    n = 1000
+    xv, xb = bf16_bits(rng.standard_normal((n, 6)) * 0.5, mref)
+    y = rng.integers(0, 8, size=n).astype(np.uint8)
+    p = random_params(rng, mref)
+    with hteno_lib.Mlp() as m:
+        m.set_params(p)
+        xd, yd = to_dev(cuda, xb), to_dev(cuda, y)
+        out = cuda.empty((n, 3), dtype=cuda.float32, device="cuda")
+        m.set_wait_limit(0)
+        for call in (lambda: m.predict(xd, out), lambda: m.grad(xd, yd)):
+            with pytest.raises(hteno_lib.HtenoError) as e:
+                call()
+            assert e.value.code == 6  # HTENO_ERR_TIMEOUT
+        m.set_wait_limit(1 << 22)
+        m.predict(xd, out)
+        got = out.cpu().numpy()
+        g, loss = m.grad(xd, yd)
+    assert np.abs(got - mref.predict(p.astype(np.float64), xv)).max() <= 2e-3
+    loss_ref, g_ref = mref.loss_and_grad(p.astype(np.float64), xv, y.astype(np.int64))
+    assert loss == pytest.approx(loss_ref, rel=1e-4)

@@ -19,3 +19,15 @@ def test_shock_shift_and_errors():
     qa, qb = np.stack([a] * 4), np.stack([b] * 4)
     l1, linf = metrics.density_errors(qb, qa)
     assert l1 == 2 * 20 / 600 and linf == 1.0
+
+
+def test_shock_shift_beyond_the_first_window():
+    """A jump displaced by more than the search window is still measured (the window widens)."""
+    from hteno import metrics
+
+    a = np.zeros((8, 64))
+    a[:, 20:] = 1.0
+    for d in (3, 4, 5, 9, 17, 30):
+        b = np.zeros((8, 64))
+        b[:, 20 + d:] = 1.0
+        assert metrics.shock_shift(b, a) == d, d
