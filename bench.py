@@ -68,6 +68,10 @@ def parse():
                          "arms run from the same initial state to the FP64 arm's end time")
     ap.add_argument("--c5-epochs", type=int, default=10)
     ap.add_argument("--c5-audit-every", type=int, default=50)
+    ap.add_argument("--c5-classify-every", type=int, default=1,
+                    help="the classifier runs every this many steps; its masks serve the steps between")
+    ap.add_argument("--c5-margin", type=int, default=-1,
+                    help="erosion of the route masks in faces (default ceil(cfl * classify-every))")
     ap.add_argument("--c5-threshold", type=float, default=0.99,
                     help="routing threshold: a stencil takes the linear weights when all three "
                          "predicted cut-off probabilities exceed it")
@@ -299,16 +303,18 @@ def hermite_path(hteno, torch, stream, steps, world, n=2048):
                            precision=prec)
         with hteno.Solver(cfg) as s:
             s.set_stream(stream.cuda_stream)
+            if prec == hteno.PREC_MIXED:  # steps the mixed arm takes to the FP64 arm's end time
+                s.set_state(q)
+                s.set_moments(v, w)
+                s.step(1 << 20, ref[0])
+                nmix = s.time()[1]
             s.set_state(q)
             s.set_moments(v, w)
             ev0 = torch.cuda.Event(enable_timing=True)
             ev1 = torch.cuda.Event(enable_timing=True)
             torch.cuda.synchronize()
             ev0.record(stream)
-            if prec == hteno.PREC_FP64:
-                s.step_async(steps)
-            else:
-                s.step(1 << 20, ref[0])  # to the FP64 arm's end time
+            s.step_async(steps if prec == hteno.PREC_FP64 else nmix, ref[0] if ref else float("inf"))
             ev1.record(stream)
             ev1.synchronize()
             s.sync()
@@ -358,16 +364,16 @@ def learned_path(hteno, torch, stream, args, world, n=4096):
                        "deterministic": "per-CTA partial gradients summed in CTA order"}
     del x, y
     q = ic.four_quadrant(n, n, 7)
+    margin = args.c5_margin if args.c5_margin >= 0 else int(np.ceil(0.4 * args.c5_classify_every - 1e-9))
+    if args.c5_classify_every == 1 and args.c5_margin < 0:
+        margin = 0
 
-    def timed_run(s, nsteps=None, t_end=None):
+    def timed_run(s, nsteps, t_end=float("inf")):
         ev0 = torch.cuda.Event(enable_timing=True)
         ev1 = torch.cuda.Event(enable_timing=True)
         torch.cuda.synchronize()
         ev0.record(stream)
-        if nsteps is not None:
-            s.step_async(nsteps)
-        else:
-            s.step(1 << 20, t_end)
+        s.step_async(nsteps, t_end)
         ev1.record(stream)
         ev1.synchronize()
         s.sync()
@@ -389,11 +395,12 @@ def learned_path(hteno, torch, stream, args, world, n=4096):
             s.set_stream(stream.cuda_stream)
             if router is not None:
                 s.set_router(router, args.c5_threshold, args.c5_audit_every)
+                s.set_router_schedule(args.c5_classify_every, margin)
+            s.set_state(q)  # (the tile tuner runs when the state is first set)
+            s.step(1 << 20, t_ref)  # untimed: the number of steps this arm takes to the end time
+            nsteps = s.time()[1]
             s.set_state(q)
-            s.step_async(2)  # warm-up (the tile tuner ran when the state was first set)
-            s.sync()
-            s.set_state(q)
-            ms, (t_end, nsteps, _) = timed_run(s, t_end=t_ref)
+            ms, (t_end, nsteps, _) = timed_run(s, nsteps, t_ref)
             st = s.router_stats() if router is not None else None
             got = s.get_state()
             uc = s.uniform_cells()
@@ -414,7 +421,8 @@ def learned_path(hteno, torch, stream, args, world, n=4096):
                            "misrouted_of_routed": st["misrouted"] / max(1, st["routed"]),
                            "plain_teno_smooth_fraction": st["smooth"] / max(1, st["seen"]),
                            "audited_steps": st["audits"], "threshold": args.c5_threshold,
-                           "audit_every": args.c5_audit_every}
+                           "audit_every": args.c5_audit_every, "classify_every": args.c5_classify_every,
+                           "margin_faces": margin}
         out[name] = d
     m.close()
     out["learned_vs_fp32_plain"] = out["fp32_plain"]["ms_per_step"] / out["fp32_learned"]["ms_per_step"]
@@ -595,6 +603,8 @@ def run_gpu(args):
     # advances one step and reads the state back
     e2e = None
     if not args.no_e2e:
+        # the same K steps as the timed region: the host holds the state, each step uploads it,
+        # advances it and downloads the result, which is the next step's input
         hq = torch.from_numpy(start_state).pin_memory()
         hout = torch.empty_like(hq).pin_memory()
         e2e_steps = max(1, args.steps)
@@ -605,6 +615,7 @@ def run_gpu(args):
             solver.set_state(hq)
             solver.step(1)
             solver.get_state(hout)
+            hq, hout = hout, hq
         el = time.perf_counter() - t0
         el = allreduce_max(torch, world, el)
         nbytes = q.nbytes

@@ -157,7 +157,8 @@ void fv2d_fused_residual(hteno_solver* s, const Geo& G, const double* q, double*
 const char* fv2d_fused_variant_name(int v);
 // Tensor-core classifier (mlp.cu): route masks of a grid from its state; timeout status.
 int mlp_classify(hteno_mlp* m, const Geo& G, const double* q, uint8_t* mx, uint8_t* my, float thr,
-                 uint4* rows, unsigned long long* nrows, long cap, cudaStream_t st);
+                 uint4* rows, unsigned long long* nrows, long cap, cudaStream_t st,
+                 const StepState* sst);
 int mlp_status(hteno_mlp* m, cudaStream_t st);
 
 // Training stencils of the learned classifier from the current FP64 state (fv2d_fp64.cu).

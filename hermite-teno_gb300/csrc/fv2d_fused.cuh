@@ -3,7 +3,10 @@
 // the conserved state once and writes it once.
 //
 //   A  load the tile plus a 3-cell halo of q (double) into shared memory as float, with the
-//      primitives u, v, H, sqrt|rho| of every loaded cell (calcPrimitiveVariable, :226-263)
+//      primitives u, v, H, sqrt|rho| of every loaded cell (calcPrimitiveVariable, :226-263);
+//      tiles whose halo lies inside the grid are staged by one TMA box copy of the four planes
+//      (a tensor map over this GPU's own state buffer), the others cell by cell with the
+//      boundary condition applied
 //   B  x faces of rows -2 .. TY+1: Roe average, L projection of the 6-cell stencil, TENO5 (or
 //      teno5i / linear) for 4 fields on both sides -> 8 characteristic values per face
 //   C  x faces of rows 0 .. TY-1: GL3 across rows r-2 .. r+2 (each face in its own basis, as
@@ -21,8 +24,11 @@
 // thread reads.  Included by the translation units that launch it (single-grid and batched).
 #pragma once
 
+#include <cuda.h>  // CUtensorMap
+
 #include "fv2d_common.cuh"
 #include "mixed_conv.cuh"
+#include "tc_ptx.cuh"
 
 namespace hteno {
 namespace fused {
@@ -54,11 +60,27 @@ template <int TX, int TY>
 struct Smem {
   float q[4][TY + 6][TX + 6];
   float p[4][TY + 6][TX + 6];  // u, v, H, sqrt|rho|
-  float c[8][Shape<TX, TY>::FN];
+  // c, fx, fy are dead during phase A: the TMA box of the double state (stage_box) lands there
+  alignas(128) float c[8][Shape<TX, TY>::FN];
   float fx[4][TY][TX + 1];
   float fy[4][TY + 1][TX];
   float wtab[2][8][3];  // TENO weights per cut-off pattern, minus and plus side
+  alignas(8) uint64_t bar;  // completion of the TMA box
 };
+
+// The TMA box of a tile: columns i0 - 4 .. i0 + TX + 3 (an even start: the box's x offset times
+// 8 bytes must be a multiple of 16), rows j0 - 3 .. j0 + TY + 2, the four conserved planes.
+template <int TX, int TY>
+struct Box {
+  static constexpr int X = TX + 8, Y = TY + 6;
+  static constexpr unsigned kBytes = unsigned(X) * Y * 4 * sizeof(double);
+};
+template <int TX, int TY>
+__device__ __forceinline__ double (*stage_box(Smem<TX, TY>& S))[Box<TX, TY>::Y][Box<TX, TY>::X] {
+  static_assert(Box<TX, TY>::kBytes <= sizeof(S.c) + sizeof(S.fx) + sizeof(S.fy), "TMA box fits");
+  return reinterpret_cast<double (*)[Box<TX, TY>::Y][Box<TX, TY>::X]>(&S.c[0][0]);
+}
+constexpr uint32_t kTmaWaitLimit = 1u << 20;  // polls of the TMA box's mbarrier before giving up
 
 template <int TX, int TY>
 constexpr size_t smem_bytes() {
@@ -189,6 +211,9 @@ struct StageArgs {
   const uint8_t* my = nullptr;
   unsigned long long* audit = nullptr;  // [5] RouteCount sums when auditing this stage
   bool skip_uniform = true;  // tiles of one tame float state get their (exactly zero) residual directly
+  // tensor map of qin ([4][ny][nx] doubles, box Box<TX, TY>) for TMA staging of interior tiles;
+  // null: every tile loads cell by cell
+  const CUtensorMap* tmap = nullptr;
 };
 
 // A float state whose fluxes stay finite through the characteristic round trip: density and
@@ -227,6 +252,49 @@ __device__ __forceinline__ double tile_stage(const DevConst& C, const Geo& G, in
   // A: state and primitives of the tile and its halo (ghosts as the boundary routine fills them)
   const bool ghosts = G.bc >= HTENO_BC_TAYLOR;
   const double tm = a.st ? a.st->t : G.t0;
+  // interior tiles (box inside the grid, no ghost cell in the halo): one TMA copy of the box
+  const bool use_tma = a.tmap != nullptr && !ghosts && i0 >= 4 && i0 + TX + 4 <= G.nx && j0 >= 3 &&
+                       j0 + TY + 3 <= G.ny;
+  if (use_tma) {
+    auto box = stage_box(S);
+    if (tid == 0) {
+      tc::mbar_init(&S.bar, 1);
+      tc::fence_mbar_init();
+    }
+    __syncthreads();
+    if (tid == 0) {
+      tc::fence_proxy_async();  // earlier generic accesses to the box region come first
+      tc::mbar_arrive_expect_tx(&S.bar, Box<TX, TY>::kBytes);
+      tc::tma_load_3d(&box[0][0][0], a.tmap, i0 - 4, j0 - 3, 0, &S.bar);
+    }
+    // bounded wait; on giving up (never expected) the block flags the step, waits once more
+    // for its copy in flight, and leaves this tile unwritten
+    const bool late = __syncthreads_or(!tc::mbar_wait(&S.bar, 0, kTmaWaitLimit));
+    if (late) {
+      tc::mbar_wait(&S.bar, 0, kTmaWaitLimit);
+      if (tid == 0 && a.st) atomicOr(&a.st->status, 4);
+      __syncthreads();
+      bad |= 4;
+      return 0.0;
+    }
+    if (tid == 0 && a.st) atomicAdd(&a.st->tma_tiles, 1ull);
+    for (int it = tid; it < Sh::W * Sh::H; it += NT) {
+      const int y = it / Sh::W, x = it - y * Sh::W;
+      const float r = d2f(box[0][y][x + 1]), mx = d2f(box[1][y][x + 1]);
+      const float my = d2f(box[2][y][x + 1]), e = d2f(box[3][y][x + 1]);
+      S.q[0][y][x] = r;
+      S.q[1][y][x] = mx;
+      S.q[2][y][x] = my;
+      S.q[3][y][x] = e;
+      const float ir = Cst<float>::rcp(r);
+      const float u = mx * ir, v = my * ir;
+      const float p = (e - 0.5f * fmaf(my, v, mx * u)) * g1;
+      S.p[0][y][x] = u;
+      S.p[1][y][x] = v;
+      S.p[2][y][x] = (e + p) * ir;
+      S.p[3][y][x] = Cst<float>::sqrt_(fabsf(r));
+    }
+  } else {
   for (int it = tid; it < Sh::W * Sh::H; it += NT) {
     const int y = it / Sh::W, x = it - y * Sh::W;
     float r, mx, my, e;
@@ -256,6 +324,7 @@ __device__ __forceinline__ double tile_stage(const DevConst& C, const Geo& G, in
     S.p[1][y][x] = v;
     S.p[2][y][x] = (e + p) * ir;
     S.p[3][y][x] = Cst<float>::sqrt_(fabsf(r));
+  }
   }
   __syncthreads();
 

@@ -23,8 +23,10 @@ struct StepState {
   unsigned long long maxbits;  // running max wave speed (bit pattern of a non-negative double)
   long long steps;   // completed steps
   int done;          // 1 once t >= t_final: the remaining launches of the call are no-ops
-  int status;        // bit 0: NaN seen; bit 1: non-positive density/pressure seen
+  int status;        // bit 0: NaN seen; bit 1: non-positive density/pressure seen;
+                     // bit 2: a bounded device-side wait gave up (the step's results are void)
   unsigned long long uniform;  // cell-stages given their exactly zero residual (uniform regions)
+  unsigned long long tma_tiles;  // mixed FV 2D tiles staged by a TMA box copy
 };
 
 // Per-device upload of the constant block of one translation unit.
@@ -70,6 +72,12 @@ struct hteno_solver {
 
   int launches_per_step = 0;
   int tile_variant = -1;  // mixed FV 2D: tile shape picked by the tuner (-1: not yet)
+  // mixed FV 2D: TMA tensor maps (CUtensorMap, 128 bytes each) of the three stage inputs, made
+  // for the tile shape tmap_variant; tma false (HTENO_TMA=0) loads every tile cell by cell
+  alignas(64) unsigned char tmap[3][128] = {};
+  int tmap_variant = -1;
+  bool tmap_ok = false;
+  bool tma = true;
   uint8_t* deep = nullptr;  // plain FV 2D: cells of uniform 7 x 7 neighbourhoods (per stage)
   bool uniform_skip = true;  // FV 2D: uniform regions take their exactly zero residual directly
   double* ghost_faces = nullptr;  // plain FV 2D with HTENO_BC_TAYLOR / _DOUBLE_MACH: ghost face rows
@@ -78,6 +86,9 @@ struct hteno_solver {
   hteno_mlp* router = nullptr;
   float router_thr = 0.9f;
   int audit_every = 0;
+  int router_every = 1;    // classify every router_every steps; the masks serve the steps between
+  int router_margin = 0;   // a route bit is kept only where it is set on every face this near
+  uint8_t* route_tmp = nullptr;  // erosion scratch (one mask)
   long router_steps = 0;
   uint8_t* route_x = nullptr;
   uint8_t* route_y = nullptr;

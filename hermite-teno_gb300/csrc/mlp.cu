@@ -568,7 +568,9 @@ struct RouteTile {
 template <int DIR>
 __global__ void __launch_bounds__(256, 6) k_route_prep(Geo G, const double* __restrict__ q, int tiles_a,
                                                     uint4* __restrict__ rows,
-                                                    unsigned long long* __restrict__ nrows, long cap) {
+                                                    unsigned long long* __restrict__ nrows, long cap,
+                                                    const StepState* __restrict__ sst) {
+  if (sst && sst->done) return;  // a step after the stop time: no rows (uniform over the block)
   constexpr int A = RouteTile<DIR>::A, B = RouteTile<DIR>::B, L = A + 5, NC = L * B;
   static_assert(A * B == 256, "one face per thread");
   __shared__ float sq[4][NC];  // conserved values, float
@@ -887,7 +889,8 @@ namespace hteno {
 // (x faces, then y faces) lists the non-flat stencils (at most `cap` rows, scratch owned by the caller), k_route_rows runs
 // the network on them.  *nrows receives the number of non-flat stencils.
 int mlp_classify(hteno_mlp* m, const Geo& G, const double* q, uint8_t* mx, uint8_t* my, float thr,
-                 uint4* rows, unsigned long long* nrows, long cap, cudaStream_t st) {
+                 uint4* rows, unsigned long long* nrows, long cap, cudaStream_t st,
+                 const StepState* sst) {
   const long nxf = long(G.nx + 1) * G.ny, nyf = long(G.ny + 1) * G.nx;
   cudaMemsetAsync(mx, 0, size_t(nxf), st);
   cudaMemsetAsync(my, 0, size_t(nyf), st);
@@ -897,8 +900,8 @@ int mlp_classify(hteno_mlp* m, const Geo& G, const double* q, uint8_t* mx, uint8
     using T2 = RouteTile<2>;
     const int ta1 = (G.nx + 1 + T1::A - 1) / T1::A, tb1 = (G.ny + T1::B - 1) / T1::B;
     const int ta2 = (G.ny + 1 + T2::A - 1) / T2::A, tb2 = (G.nx + T2::B - 1) / T2::B;
-    k_route_prep<1><<<unsigned(ta1) * unsigned(tb1), 256, 0, st>>>(G, q, ta1, rows, nrows, cap);
-    k_route_prep<2><<<unsigned(ta2) * unsigned(tb2), 256, 0, st>>>(G, q, ta2, rows, nrows, cap);
+    k_route_prep<1><<<unsigned(ta1) * unsigned(tb1), 256, 0, st>>>(G, q, ta1, rows, nrows, cap, sst);
+    k_route_prep<2><<<unsigned(ta2) * unsigned(tb2), 256, 0, st>>>(G, q, ta2, rows, nrows, cap, sst);
   }
   const float zthr = std::log(thr / (1.0f - thr));  // sigmoid(z) > thr  <=>  z > logit(thr)
   k_route_rows<<<4 * m->sms, 128, mlp::kSmemCBytes, st>>>(m->W, rows, nrows, cap, nxf, mx, my, zthr,

@@ -104,6 +104,7 @@ int copy_out(hteno_solver* s, double* dst, const double* src, size_t n, int wher
 void release(hteno_solver* s) {
   cudaFree(s->route_x);
   cudaFree(s->route_y);
+  cudaFree(s->route_tmp);
   cudaFree(s->audit);
   cudaFree(s->route_rows);
   cudaFree(s->deep);
@@ -196,6 +197,9 @@ int hteno_create(const hteno_config* cfg, hteno_solver** out) {
   // HTENO_UNIFORM_SKIP=0 computes uniform regions in full (a check that skipping them is exact)
   const char* us = std::getenv("HTENO_UNIFORM_SKIP");
   s->uniform_skip = !(us && us[0] == '0');
+  // HTENO_TMA=0 stages every tile of the mixed FV 2D kernel cell by cell (the same bits)
+  const char* tma = std::getenv("HTENO_TMA");
+  s->tma = !(tma && tma[0] == '0');
 
   auto fail = [&](int code) {
     release(s);
@@ -264,6 +268,7 @@ int hteno_set_state(hteno_solver* s, const double* q, int where) {
   s->hstate->done = 0;
   s->hstate->status = 0;
   s->hstate->uniform = 0;
+  s->hstate->tma_tiles = 0;
   cudaError_t e = cudaMemcpyAsync(s->dstate, s->hstate, sizeof(StepState), cudaMemcpyHostToDevice,
                                   s->stream);
   if (e != cudaSuccess) return cuda_error(s, e, "state reset");
@@ -314,6 +319,8 @@ int hteno_sync(hteno_solver* s) {
                                   s->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
   if (e != cudaSuccess) return cuda_error(s, e, "sync");
+  if (s->hstate->status & 4)
+    return set_error(s, HTENO_ERR_TIMEOUT, "a bounded device-side wait gave up (TMA tile copy)");
   if (s->strict && (s->hstate->status & 1))
     return set_error(s, HTENO_ERR_NAN, "NaN in the conserved state");
   if (s->strict && (s->hstate->status & 2))
@@ -361,13 +368,14 @@ int hteno_get_status(hteno_solver* s, int* flags) {
   return HTENO_OK;
 }
 
-int hteno_get_uniform_cells(hteno_solver* s, long long* cells) {
-  if (!s || !cells) return HTENO_ERR_INVALID_ARG;
+int hteno_get_counters(hteno_solver* s, long long* counters) {
+  if (!s || !counters) return HTENO_ERR_INVALID_ARG;
   cudaError_t e = cudaMemcpyAsync(s->hstate, s->dstate, sizeof(StepState), cudaMemcpyDeviceToHost,
                                   s->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
-  if (e != cudaSuccess) return cuda_error(s, e, "get_uniform_cells");
-  *cells = static_cast<long long>(s->hstate->uniform);
+  if (e != cudaSuccess) return cuda_error(s, e, "get_counters");
+  counters[0] = static_cast<long long>(s->hstate->uniform);
+  counters[1] = static_cast<long long>(s->hstate->tma_tiles);
   return HTENO_OK;
 }
 

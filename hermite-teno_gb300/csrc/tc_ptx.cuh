@@ -1,6 +1,7 @@
 // Thin inline-PTX layer for the 5th-generation tensor cores (tcgen05) used by the learned
 // stencil classifier: tensor-memory allocation, BF16 MMAs with shared-memory operand
-// descriptors, completion through mbarriers (bounded waits), and tensor-memory loads.
+// descriptors, completion through mbarriers (bounded waits), and tensor-memory loads; plus the
+// bulk tensor copies (TMA) that stage the fused stage kernel's tiles.
 //
 // Operand layout (both A and B "K-major", no swizzle): an R x K bf16 operand is stored as 8 x 8
 // core matrices of 128 contiguous bytes (8 rows of 16 bytes); core matrices follow each other
@@ -90,6 +91,36 @@ __device__ __forceinline__ void fence_after() {
 // Generic-proxy shared-memory writes become visible to the tensor cores' (async proxy) reads.
 __device__ __forceinline__ void fence_proxy_async() {
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+// ---- bulk tensor copies (TMA) ------------------------------------------------------------------
+
+// An initialised mbarrier becomes visible to the async proxy (the TMA unit that completes it).
+__device__ __forceinline__ void fence_mbar_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+// Arrive on the mbarrier (count 1) and expect `bytes` of transaction completions in this phase.
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* mbar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
+               :
+               : "r"(smem_u32(mbar)), "r"(bytes)
+               : "memory");
+}
+
+// One box of a 3D tensor map, starting at element (x, y, z), into shared memory at dst (box
+// layout: x fastest); completion counted in bytes on the mbarrier.  x * element size must be a
+// multiple of 16 bytes; dst 128-byte aligned.  The map is a kernel parameter (__grid_constant__)
+// of this GPU's own memory; no multicast.
+__device__ __forceinline__ void tma_load_3d(void* dst, const void* tmap, int x, int y, int z,
+                                            uint64_t* mbar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes "
+      "[%0], [%1, {%2, %3, %4}], [%5];"
+      :
+      : "r"(smem_u32(dst)), "l"(reinterpret_cast<uint64_t>(tmap)), "r"(x), "r"(y), "r"(z),
+        "r"(smem_u32(mbar))
+      : "memory");
 }
 
 // Warp-wide: allocate `ncols` tensor-memory columns, address written to *dst (shared).

@@ -95,7 +95,7 @@ def lib() -> ctypes.CDLL:
         L.hteno_measure_fma_peak.argtypes = [i, _D]
         L.hteno_get_status.argtypes = [vp, ctypes.POINTER(i)]
         L.hteno_set_strict.argtypes = [vp, i]
-        L.hteno_get_uniform_cells.argtypes = [vp, ctypes.POINTER(ctypes.c_longlong)]
+        L.hteno_get_counters.argtypes = [vp, ctypes.POINTER(ctypes.c_longlong)]
         L.hteno_residual_noalloc.argtypes = [ctypes.POINTER(Config), vp, vp, vp]
         L.hteno_batch_create.argtypes = [ctypes.POINTER(Config), i, ctypes.POINTER(vp)]
         L.hteno_batch_destroy.argtypes = [vp]
@@ -112,6 +112,7 @@ def lib() -> ctypes.CDLL:
         L.hteno_batch_last_error.argtypes = [vp]
         L.hteno_set_router.argtypes = [vp, vp, ctypes.c_float, i]
         L.hteno_router_stats.argtypes = [vp, ctypes.POINTER(ctypes.c_longlong)]
+        L.hteno_set_router_schedule.argtypes = [vp, i, i]
         L.hteno_kxrcf.argtypes = [vp, vp]
         L.hteno_harvest.argtypes = [vp, d, ctypes.c_ulonglong, vp, vp, l, ctypes.POINTER(l)]
         L.hteno_mlp_create.argtypes = [ctypes.c_ulonglong, ctypes.POINTER(vp)]
@@ -225,12 +226,15 @@ class Solver:
         _check(lib().hteno_get_status(self.h, ctypes.byref(f)), self.h)
         return f.value
 
+    def counters(self) -> dict:
+        """Work counters since set_state (FV 2D): cell-stages whose exactly zero residual was taken
+        without computing their faces, and mixed-path tiles staged by a TMA box copy."""
+        a = (ctypes.c_longlong * 2)()
+        _check(lib().hteno_get_counters(self.h, a), self.h)
+        return {"uniform_cells": a[0], "tma_tiles": a[1]}
+
     def uniform_cells(self) -> int:
-        """Cell-stages since set_state whose exactly zero residual was taken without computing
-        their faces (uniform regions, FV 2D)."""
-        n = ctypes.c_longlong()
-        _check(lib().hteno_get_uniform_cells(self.h, ctypes.byref(n)), self.h)
-        return n.value
+        return self.counters()["uniform_cells"]
 
     def set_strict(self, on: bool = True) -> None:
         _check(lib().hteno_set_strict(self.h, int(bool(on))), self.h)
@@ -261,6 +265,11 @@ class Solver:
         self._router = mlp
         _check(lib().hteno_set_router(self.h, mlp.h if mlp is not None else None, float(threshold),
                                       int(audit_every)), self.h)
+
+    def set_router_schedule(self, classify_every: int = 1, margin: int = 0) -> None:
+        """Classify every `classify_every` steps; keep a route bit only where it is set on every
+        face within `margin` faces (call after set_router)."""
+        _check(lib().hteno_set_router_schedule(self.h, int(classify_every), int(margin)), self.h)
 
     def router_stats(self) -> dict:
         a = (ctypes.c_longlong * 7)()

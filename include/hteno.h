@@ -138,12 +138,15 @@ int hteno_launches_per_step(hteno_solver* s, int* launches);
 int hteno_get_status(hteno_solver* s, int* flags);
 int hteno_set_strict(hteno_solver* s, int on);
 
-/* Cell-stages since the last hteno_set_state whose residual the FV 2D stepping took as exactly
- * zero without computing their faces (uniform regions: the plain path's cells whose 7 x 7
- * neighbourhood holds one tame state, the mixed path's tiles of one tame float state; the same
- * bits as computing them).  A measurement aid with no reference counterpart: the reference
- * computes every face. */
-int hteno_get_uniform_cells(hteno_solver* s, long long* cells);
+/* Work counters since the last hteno_set_state (FV 2D stepping), a measurement aid with no
+ * reference counterpart (the reference computes every face):
+ *   counters[0]: cell-stages whose residual was taken as exactly zero without computing their
+ *                faces (uniform regions: the plain path's cells whose 7 x 7 neighbourhood holds
+ *                one tame state, the mixed path's tiles of one tame float state; the same bits
+ *                as computing them);
+ *   counters[1]: mixed-path tiles whose state was staged by one TMA box copy (interior tiles of
+ *                grids with an even nx; the others load cell by cell). */
+int hteno_get_counters(hteno_solver* s, long long* counters);
 
 /* Message of the last failed call on this handle ("" if none). */
 const char* hteno_last_error(hteno_solver* s);
@@ -280,6 +283,16 @@ const char* hteno_mlp_last_error(hteno_mlp* m);
  * classifier must outlive its use by the solver.  HTENO_ERR_UNSUPPORTED unless the solver is
  * mixed-precision FV 2D with teno5 or teno5i and has fewer than 2^29 faces. */
 int hteno_set_router(hteno_solver* s, hteno_mlp* m, float threshold, int audit_every);
+/* Classification schedule of a router (defaults 1 and 0: every step, masks used as classified).
+ * The classifier runs on the step-start state every `classify_every` steps and its masks serve
+ * the steps up to the next classification; a stencil's route bit is then kept only where the
+ * same bit is set on every face within `margin` faces along and across the face direction
+ * (faces within `margin` of the grid's edge keep none).  A discontinuity moves at most
+ * cfl * classify_every cells between classifications, so margin >= ceil(cfl * classify_every)
+ * keeps every routed stencil clear of any discontinuity the classifier saw.  The next step after
+ * this call (or after hteno_set_state) classifies.  HTENO_ERR_UNSUPPORTED without a router.
+ * No reference counterpart (the reference has no learned sensor). */
+int hteno_set_router_schedule(hteno_solver* s, int classify_every, int margin);
 /* stats[7]: audited stencils, routed, misrouted (routed though plain TENO cut a candidate),
  * all-smooth by plain TENO, flat (a window of equal float values: the stage kernel takes the
  * linear weights for it without the network or the indicators -- plain TENO keeps all three

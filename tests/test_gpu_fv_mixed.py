@@ -139,6 +139,40 @@ def test_mixed_uniform_tiles_exact(hteno_lib, cuda, case):
     np.testing.assert_array_equal(got, full)
 
 
+@pytest.mark.parametrize("nx,ny,bc,tile", [(160, 96, 0, None), (128, 72, 1, "6"), (96, 96, 0, "4"),
+                                          (161, 90, 0, None)])
+def test_mixed_tma_tiles_same_bits(hteno_lib, cuda, nx, ny, bc, tile):
+    """Interior tiles staged by a TMA box copy of the four state planes give the same bits as the
+    cell-by-cell loads (HTENO_TMA=0), for several tile shapes and both copy boundaries; a grid with
+    an odd nx (row stride not a multiple of 16 bytes) loads every tile cell by cell."""
+    from hteno import ic
+
+    q = ic.four_quadrant(nx, ny, 21)
+    cfg = hteno_lib.config(dims=2, nx=nx, ny=ny, flux=1, bc=bc, precision=1)
+
+    def go():
+        with hteno_lib.Solver(cfg) as s:
+            s.set_state(q)
+            s.step(30)
+            return s.get_state(), s.counters(), s.time()
+
+    try:
+        if tile is not None:
+            os.environ["HTENO_FV2D_TILE"] = tile
+        got, c, t = go()
+        os.environ["HTENO_TMA"] = "0"
+        want, c0, t0 = go()
+    finally:
+        os.environ.pop("HTENO_TMA", None)
+        os.environ.pop("HTENO_FV2D_TILE", None)
+    assert t == t0 and c0["tma_tiles"] == 0
+    np.testing.assert_array_equal(got, want)
+    if nx % 2:
+        assert c["tma_tiles"] == 0
+    else:
+        assert c["tma_tiles"] > 0
+
+
 @pytest.mark.parametrize("bc,fn,shape,box", [
     (2, "rayleigh_taylor", (40, 150), (0.0, 0.25, 0.0, 1.0)),
     (3, "double_mach", (160, 41), (0.0, 4.0, 0.0, 1.0))])

@@ -130,6 +130,38 @@ def test_router_all_and_nothing(hteno_lib, cuda):
         assert np.abs(got_all[0] - want_lin[0]).mean() <= 0.1 * np.abs(want_teno[0] - want_lin[0]).mean() + 1e-6
 
 
+def test_router_schedule(hteno_lib, cuda):
+    """Classification every k steps with eroded masks: a network that routes nothing still
+    reproduces the plain run bit for bit; one that routes everything routes fewer stencils once
+    the masks are eroded (faces near the grid's edge keep no route), and every step is audited."""
+    from hteno import ic
+
+    h = hteno_lib
+    q = ic.four_quadrant(70, 52, 8)
+    want_teno, _ = run_mixed(h, q, 6)
+
+    def run_sched(router, every, margin):
+        cfg = h.config(dims=2, nx=70, ny=52, flux=1, precision=1)
+        with h.Solver(cfg) as s:
+            s.set_router(router, 0.9, 1)
+            s.set_router_schedule(every, margin)
+            s.set_state(q)
+            s.step(6)
+            return s.get_state(), s.router_stats()
+
+    with constant_classifier(h, 20.0) as all_smooth, constant_classifier(h, -20.0) as none:
+        got, st = run_sched(none, 4, 2)
+        np.testing.assert_array_equal(got, want_teno)
+        assert st["routed"] == 0 and st["audits"] == 6
+        _, st1 = run_sched(all_smooth, 1, 0)
+        got3, st3 = run_sched(all_smooth, 3, 2)
+        assert st3["audits"] == 6 and 0 < st3["routed"] < st1["routed"]
+        assert np.isfinite(got3).all()
+    with pytest.raises(h.HtenoError):
+        with h.Solver(h.config(dims=2, nx=70, ny=52, flux=1, precision=1)) as s:
+            s.set_router_schedule(2, 1)  # no router set
+
+
 def test_trained_router_gains(hteno_lib, cuda):
     """Train on rows harvested from plain runs (fresh seeds), then route a mixed 256^2 run: most
     stencils skip the nonlinear weights, few are misrouted, and the density error against FP64
