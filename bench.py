@@ -68,10 +68,11 @@ def parse():
                          "arms run from the same initial state to the FP64 arm's end time")
     ap.add_argument("--c5-epochs", type=int, default=10)
     ap.add_argument("--c5-audit-every", type=int, default=50)
-    ap.add_argument("--c5-classify-every", type=int, default=1,
-                    help="the classifier runs every this many steps; its masks serve the steps between")
+    ap.add_argument("--c5-classify-every", type=int, default=10,
+                    help="second learned arm: the classifier runs every this many steps and its masks "
+                         "serve the steps between (the first learned arm classifies every step)")
     ap.add_argument("--c5-margin", type=int, default=-1,
-                    help="erosion of the route masks in faces (default ceil(cfl * classify-every))")
+                    help="erosion of the second arm's route masks in faces (default ceil(cfl * classify-every))")
     ap.add_argument("--c5-threshold", type=float, default=0.99,
                     help="routing threshold: a stencil takes the linear weights when all three "
                          "predicted cut-off probabilities exceed it")
@@ -365,8 +366,6 @@ def learned_path(hteno, torch, stream, args, world, n=4096):
     del x, y
     q = ic.four_quadrant(n, n, 7)
     margin = args.c5_margin if args.c5_margin >= 0 else int(np.ceil(0.4 * args.c5_classify_every - 1e-9))
-    if args.c5_classify_every == 1 and args.c5_margin < 0:
-        margin = 0
 
     def timed_run(s, nsteps, t_end=float("inf")):
         ev0 = torch.cuda.Event(enable_timing=True)
@@ -390,12 +389,15 @@ def learned_path(hteno, torch, stream, args, world, n=4096):
                    "ms_per_step": ms64 / n64, "steps": n64, "t_end": t_ref,
                    "uniform_cell_fraction": u64 / (3.0 * n * n * n64)}
     cfg32 = hteno.config(dims=2, nx=n, ny=n, flux=hteno.FLUX_HLLC, precision=hteno.PREC_MIXED)
-    for name, router in (("fp32_plain", None), ("fp32_learned", m)):
+    arms = (("fp32_plain", None, 1, 0), ("fp32_learned", m, 1, 0),
+            ("fp32_learned_every%d" % args.c5_classify_every, m, args.c5_classify_every, margin))
+    end_state = None
+    for name, router, every, marg in arms:
         with hteno.Solver(cfg32) as s:
             s.set_stream(stream.cuda_stream)
             if router is not None:
                 s.set_router(router, args.c5_threshold, args.c5_audit_every)
-                s.set_router_schedule(args.c5_classify_every, margin)
+                s.set_router_schedule(every, marg)
             s.set_state(q)  # (the tile tuner runs when the state is first set)
             s.step(1 << 20, t_ref)  # untimed: the number of steps this arm takes to the end time
             nsteps = s.time()[1]
@@ -403,6 +405,8 @@ def learned_path(hteno, torch, stream, args, world, n=4096):
             ms, (t_end, nsteps, _) = timed_run(s, nsteps, t_ref)
             st = s.router_stats() if router is not None else None
             got = s.get_state()
+            if router is None:
+                end_state = got
             uc = s.uniform_cells()
             l1, linf = density_errors(got, ref)
             shift = shock_shift(got, ref)
@@ -421,11 +425,30 @@ def learned_path(hteno, torch, stream, args, world, n=4096):
                            "misrouted_of_routed": st["misrouted"] / max(1, st["routed"]),
                            "plain_teno_smooth_fraction": st["smooth"] / max(1, st["seen"]),
                            "audited_steps": st["audits"], "threshold": args.c5_threshold,
-                           "audit_every": args.c5_audit_every, "classify_every": args.c5_classify_every,
-                           "margin_faces": margin}
+                           "audit_every": args.c5_audit_every, "classify_every": every,
+                           "margin_faces": marg}
         out[name] = d
     m.close()
     out["learned_vs_fp32_plain"] = out["fp32_plain"]["ms_per_step"] / out["fp32_learned"]["ms_per_step"]
+    sched = "fp32_learned_every%d" % args.c5_classify_every
+    out["learned_every_vs_fp32_plain"] = out["fp32_plain"]["ms_per_step"] / out[sched]["ms_per_step"]
+    # the ceiling of any router: 5 steps from the FP32 arm's end state with every stencil
+    # reconstructed by TENO5, then with every stencil taking the linear weights (what routing
+    # everything would save at the most; not a valid scheme at discontinuities)
+    ceil = {}
+    for rname, recon in (("teno5", hteno.RECON_TENO5), ("linear", hteno.RECON_LINEAR)):
+        c = hteno.config(dims=2, nx=n, ny=n, flux=hteno.FLUX_HLLC, precision=hteno.PREC_MIXED, recon=recon)
+        with hteno.Solver(c) as s:
+            s.set_stream(stream.cuda_stream)
+            s.set_state(end_state)
+            s.step(1)
+            s.set_state(end_state)
+            ms, _ = timed_run(s, 5)
+        ceil[rname + "_ms_per_step"] = ms / 5
+    ceil["max_saving"] = 1.0 - ceil["linear_ms_per_step"] / ceil["teno5_ms_per_step"]
+    ceil["note"] = ("5 steps from the FP32 arm's end state: every stencil by TENO5 vs every stencil by the "
+                    "linear weights; no router can save more than max_saving of a step")
+    out["routing_ceiling"] = ceil
     out["window"] = (f"every arm from the initial state: FP64 {args.c5_steps} steps, the FP32 arms to the "
                      "FP64 arm's end time; errors at that time")
     return out

@@ -194,6 +194,19 @@ def entropy_wave_2d(nx, ny, t=0.0, xl=-1.0, xr=1.0, yb=-1.0, yt=1.0, rho=1.0, u=
     return cell_average_2d(q, nx, ny, xl, xr, yb, yt)
 
 
+def smooth_waves_2d(nx, ny, gamma=1.4):
+    """Point values [4][ny][nx] of a smooth periodic flow on [0,1]^2 (a synthetic workload with no
+    discontinuity): rho = 1 + 0.2 sin(2 pi x) sin(2 pi y), u = 0.5 + 0.1 sin(2 pi y),
+    v = -0.3 + 0.1 cos(2 pi x), p = 1 + 0.1 cos(2 pi (x + y))."""
+    X, Y = cell_centres(nx, ny, 0.0, 1.0, 0.0, 1.0)
+    tp = 2 * np.pi
+    rho = 1 + 0.2 * np.sin(tp * X) * np.sin(tp * Y)
+    u = 0.5 + 0.1 * np.sin(tp * Y)
+    v = -0.3 + 0.1 * np.cos(tp * X)
+    p = 1 + 0.1 * np.cos(tp * (X + Y))
+    return np.ascontiguousarray(conservative2(rho, u, v, p, gamma))
+
+
 def isentropic_vortex_2d(nx, ny, t=0.0, xl=-5.0, xr=5.0, yb=-5.0, yt=5.0, gamma=1.4, b=5.0):
     """FV::System2D::isentropicVortex (FV_System2D.cpp:76-99; conservativeOfIsentropicVortex,
     Equations_Euler2D.cpp:656-666): the vortex of strength b on a (1, 1) mean flow, advected to
