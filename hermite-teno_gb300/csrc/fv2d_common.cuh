@@ -166,6 +166,11 @@ int fv2d_harvest(hteno_solver* s, const Geo& G, const Work<double>& W, double p,
                  unsigned long long seed, uint16_t* X, uint8_t* Y, long cap,
                  unsigned long long* count);
 
+// FP64 judge of learned routing (fv2d_fp64.cu): counts[0] routed stencils of the masks, counts[1]
+// those whose plain FP64 TENO cut-off on the double state drops a candidate.
+int fv2d_audit64(hteno_solver* s, const Geo& G, const double* q, const uint8_t* mx, const uint8_t* my,
+                 long long* counts);
+
 // Bit-reproducible FP64 path (fv2d_fp64.cu)
 int fv2d_fp64_setup(hteno_solver* s);
 void fv2d_fp64_prim(hteno_solver* s, const Geo& G, const Work<double>& W, const double* q,

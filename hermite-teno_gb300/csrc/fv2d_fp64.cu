@@ -219,6 +219,69 @@ __global__ void __launch_bounds__(kFaceThreads) kp_harvest(Geo G, const double* 
   }
 }
 
+// FP64 judge of a mixed-precision solver's learned routing: for every face whose route byte
+// (layout of the mixed stage kernel's masks: x faces [ny][nx+1], y faces [ny+1][nx]) routes a
+// stencil, the face's characteristic stencils in double from the double state (Roe average of
+// the two cells, the 6 cells projected) and, per routed (field, side), the TENO cut-off the plain
+// FP64 solver decides on that stencil.  out[0] += routed stencils, out[1] += those whose cut-off
+// drops a candidate (pattern != 7).
+template <int DIR>
+__global__ void __launch_bounds__(kFaceThreads) kp_audit64(Geo G, const double* __restrict__ q,
+                                                           const uint8_t* __restrict__ mask,
+                                                           unsigned long long* out) {
+  const int nf = DIR == 1 ? G.nx + 1 : G.ny + 1;
+  const int nt = DIR == 1 ? G.ny : G.nx;
+  const long idx = blockIdx.x * long(blockDim.x) + threadIdx.x;
+  int routed = 0, wrong = 0;
+  if (idx < long(nf) * nt) {
+    int f, t;
+    if (DIR == 1) { f = int(idx % nf); t = int(idx / nf); }
+    else { t = int(idx % nt); f = int(idx / nt); }
+    const uint8_t route = mask[DIR == 1 ? size_t(t) * nf + f : size_t(f) * nt + t];
+    if (route) {
+      const size_t nc = size_t(G.nx) * G.ny;
+      const int ns = DIR == 1 ? G.nx : G.ny;
+      auto cell = [&](int s) -> size_t {
+        const int m = bmap(s, ns, G.bc);
+        return DIR == 1 ? size_t(t) * G.nx + m : size_t(m) * G.nx + t;
+      };
+      double qa[4], qb[4], wa[4], wb[4], ha, hb, sra, srb;
+      const size_t ca = cell(f - 1), cb = cell(f);
+      for (int v = 0; v < 4; ++v) {
+        qa[v] = q[v * nc + ca];
+        qb[v] = q[v * nc + cb];
+      }
+      cell_prim(G.g1, qa, wa, ha, sra);
+      cell_prim(G.g1, qb, wb, hb, srb);
+      const par::Eig E = par::eig(G.g1, DIR, sra, wa[1], wa[2], ha, srb, wb[1], wb[2], hb);
+      double ch[4][6];
+      for (int m = 0; m < 6; ++m) {
+        const size_t c = cell(f - 3 + m);
+        const double qq[4] = {q[c], q[nc + c], q[2 * nc + c], q[3 * nc + c]};
+        double cc[4];
+        par::left(E, DIR, qq, cc);
+        for (int r = 0; r < 4; ++r) ch[r][m] = cc[r];
+      }
+      for (int b = 0; b < 8; ++b) {
+        if (!((route >> b) & 1)) continue;
+        const double* v = ch[b >> 1] + (b & 1);  // side 1 reconstructs from cells 1..5
+        double SI[3];
+        par::lagrange_si(v, SI);
+        routed += 1;
+        wrong += par::teno_decide(v, SI, G.recon == HTENO_RECON_TENO5I) != 7;
+      }
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    routed += __shfl_xor_sync(0xffffffffu, routed, o);
+    wrong += __shfl_xor_sync(0xffffffffu, wrong, o);
+  }
+  if ((threadIdx.x & 31) == 0 && routed) {
+    atomicAdd(out, (unsigned long long)routed);
+    if (wrong) atomicAdd(out + 1, (unsigned long long)wrong);
+  }
+}
+
 // kp_faces for boundaries whose ghosts are not copies of interior cells (HTENO_BC_TAYLOR,
 // _DOUBLE_MACH): every state comes from bc_state(), the primitives of the two Roe cells are
 // computed from their states (calcPrimitiveVariable covers the ghosts, :231-262), and the face
@@ -512,6 +575,26 @@ void fv2d_fp64_stage(hteno_solver* s, const Geo& G, const Work<double>& W, int s
   kp_update<<<unsigned((nc + 255) / 256), 256, 0, cs>>>(G, stage, W.fx, W.fy, s->q, s->q0,
                                                        W.prim, out, st, deep);
   trace_end(s);
+}
+
+int fv2d_audit64(hteno_solver* s, const Geo& G, const double* q, const uint8_t* mx, const uint8_t* my,
+                 long long* counts) {
+  unsigned long long* d = nullptr;
+  cudaError_t e = cudaMallocAsync(&d, 2 * sizeof(unsigned long long), s->stream);
+  if (e != cudaSuccess) return cuda_error(s, e, "audit counters");
+  cudaMemsetAsync(d, 0, 2 * sizeof(unsigned long long), s->stream);
+  const long nxf = long(G.nx + 1) * G.ny, nyf = long(G.ny + 1) * G.nx;
+  kp_audit64<1><<<unsigned((nxf + kFaceThreads - 1) / kFaceThreads), kFaceThreads, 0, s->stream>>>(G, q, mx, d);
+  kp_audit64<2><<<unsigned((nyf + kFaceThreads - 1) / kFaceThreads), kFaceThreads, 0, s->stream>>>(G, q, my, d);
+  unsigned long long h[2] = {0, 0};
+  e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpyAsync(h, d, sizeof(h), cudaMemcpyDeviceToHost, s->stream);
+  cudaFreeAsync(d, s->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+  if (e != cudaSuccess) return cuda_error(s, e, "FP64 routing audit");
+  counts[0] = (long long)h[0];
+  counts[1] = (long long)h[1];
+  return HTENO_OK;
 }
 
 int fv2d_harvest(hteno_solver* s, const Geo& G, const Work<double>& W, double p,

@@ -29,6 +29,9 @@ __global__ void __launch_bounds__(NT, MINB) k_fused(Geo G, int stage, fused::Sta
   extern __shared__ __align__(128) unsigned char smem[];
   auto& S = *reinterpret_cast<fused::Smem<TX, TY>*>(smem);
   a.tmap = has_tm && (tc::smem_u32(&S.c[0][0]) & 127u) == 0 ? &tm : nullptr;
+  // an audited step that runs (not past the stop time) counts once
+  if (stage == 1 && a.audit && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0)
+    atomicAdd(a.audit + 6, 1ull);
   int bad = 0;
   const double ms = fused::tile_stage<TX, TY, NT>(c_dev, G, blockIdx.x * TX, blockIdx.y * TY,
                                                   stage, a, S, bad);
@@ -196,6 +199,7 @@ int fv2d_fused_setup(hteno_solver* s) {
 // residual evaluations of this state into the scratch buffer.
 int fv2d_fused_prepare(hteno_solver* s, const Geo& G, double* scratch) {
   s->router_steps = 0;  // a new state: the next step classifies (route masks are per state)
+  if (s->audit) cudaMemsetAsync(s->audit, 0, 7 * sizeof(unsigned long long), s->stream);
   k_max_speed<<<304, 256, 0, s->stream>>>(G, s->q, s->dstate);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_error(s, e, "max speed");
@@ -256,7 +260,6 @@ void fv2d_fused_step(hteno_solver* s, const Geo& G, double* qc) {
       a->my = s->route_y;
       a->audit = aud ? s->audit : nullptr;
     }
-    if (aud) ++s->audits;
     ++s->router_steps;
   }
   ensure_maps(s, G, kVariants[s->tile_variant < 0 ? 0 : s->tile_variant], qc);
@@ -301,18 +304,17 @@ int hteno_set_router(hteno_solver* s, hteno_mlp* m, float threshold, int audit_e
     s->route_cap = long(std::min<size_t>(8 * (bx + by), size_t(256) << 20));
     cudaError_t e = cudaMalloc(&s->route_x, (bx + 3) & ~size_t(3));
     if (e == cudaSuccess) e = cudaMalloc(&s->route_y, (by + 3) & ~size_t(3));
-    if (e == cudaSuccess) e = cudaMalloc(&s->audit, 6 * sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMalloc(&s->audit, 7 * sizeof(unsigned long long));
     if (e == cudaSuccess) e = cudaMalloc(&s->route_rows, size_t(s->route_cap) * sizeof(uint4));
     if (e != cudaSuccess) return cuda_error(s, e, "route masks");
   }
-  cudaMemset(s->audit, 0, 6 * sizeof(unsigned long long));
+  cudaMemset(s->audit, 0, 7 * sizeof(unsigned long long));
   cudaMemset(s->route_x, 0, bx);
   cudaMemset(s->route_y, 0, by);
   s->router = m;
   s->router_thr = threshold;
   s->audit_every = audit_every;
   s->router_steps = 0;
-  s->audits = 0;
   s->launches_per_step = 2 + 3 + 2;
   return HTENO_OK;
 }
@@ -332,15 +334,32 @@ int hteno_set_router_schedule(hteno_solver* s, int classify_every, int margin) {
   return HTENO_OK;
 }
 
+int hteno_router_audit64(hteno_solver* s, long long* counts) {
+  if (!s || !counts) return HTENO_ERR_INVALID_ARG;
+  if (!s->router || !s->route_x) return set_error(s, HTENO_ERR_UNSUPPORTED, "no router set");
+  const Geo G = geo_of(s);
+  int rc = mlp_classify(s->router, G, s->q, s->route_x, s->route_y, s->router_thr, s->route_rows,
+                        s->audit + 5, s->route_cap, s->stream, nullptr);
+  if (rc != HTENO_OK) return set_error(s, rc, "classification");
+  if (s->router_margin > 0) {
+    erode_mask(s, s->route_x, G.ny, G.nx + 1);
+    erode_mask(s, s->route_y, G.ny + 1, G.nx);
+  }
+  rc = fv2d_audit64(s, G, s->q, s->route_x, s->route_y, counts);
+  if (rc != HTENO_OK) return rc;
+  rc = mlp_status(s->router, s->stream);
+  return rc == HTENO_OK ? HTENO_OK : set_error(s, rc, "classifier tensor-core wait timed out");
+}
+
 int hteno_router_stats(hteno_solver* s, long long* stats) {
   if (!s || !stats) return HTENO_ERR_INVALID_ARG;
   if (!s->router || !s->audit) return set_error(s, HTENO_ERR_UNSUPPORTED, "no router set");
-  unsigned long long h[6] = {0, 0, 0, 0, 0, 0};
+  unsigned long long h[7] = {0, 0, 0, 0, 0, 0, 0};
   cudaError_t e = cudaMemcpyAsync(h, s->audit, sizeof(h), cudaMemcpyDeviceToHost, s->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
   if (e != cudaSuccess) return cuda_error(s, e, "router stats");
   for (int k = 0; k < 5; ++k) stats[k] = (long long)h[k];
-  stats[5] = s->audits;
+  stats[5] = (long long)h[6];
   stats[6] = (long long)h[5];
   const int rc = mlp_status(s->router, s->stream);
   return rc == HTENO_OK ? HTENO_OK : set_error(s, rc, "classifier tensor-core wait timed out");

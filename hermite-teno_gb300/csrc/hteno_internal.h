@@ -92,10 +92,9 @@ struct hteno_solver {
   long router_steps = 0;
   uint8_t* route_x = nullptr;
   uint8_t* route_y = nullptr;
-  unsigned long long* audit = nullptr;  // [6]: seen, routed, misrouted, smooth, flat; rows asked
+  unsigned long long* audit = nullptr;  // [7]: seen, routed, misrouted, smooth, flat; rows asked; audited steps
   uint4* route_rows = nullptr;          // non-flat stencils handed to the network
   long route_cap = 0;
-  long audits = 0;
   bool strict = false;
   std::string err;
 

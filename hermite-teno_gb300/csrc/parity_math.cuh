@@ -146,15 +146,14 @@ __device__ __forceinline__ int cutoff_pattern(const double* SI, double tau, doub
   return pat;
 }
 
-// One side of teno5 (:481-511) / teno5i (:1235-1263) given the candidates p and stencil v.
-__device__ __forceinline__ double teno_side_si(const DevConst& C, const double* p, const double* v,
-                                               const double* SI, int side, bool improved) {
+// The cut-off pattern of one side of teno5 (:481-511) / teno5i (:1235-1263) for the window v with
+// indicators SI (bit k set: candidate k kept).
+__device__ __forceinline__ int teno_decide(const double* v, const double* SI, bool improved) {
   // All three indicators exactly zero (constant data): the three ratios 1 + tau/(0 + epsz) are
   // equal whatever tau is, and the cut-off keeps all candidates (pattern 7) -- decided without
   // tau, same bits.  (Equal values alone do not suffice: 3u - 4u + u can leave a rounding
   // residue in one indicator.)
-  if (SI[0] == 0.0 && SI[1] == 0.0 && SI[2] == 0.0)
-    return catchnan(dot3v(p, side ? C.wtab_p[7] : C.wtab_m[7]));
+  if (SI[0] == 0.0 && SI[1] == 0.0 && SI[2] == 0.0) return 7;
   double tau;
   if (!improved) {
     const double b35 = lagrange_b35(v);
@@ -164,7 +163,13 @@ __device__ __forceinline__ double teno_side_si(const DevConst& C, const double* 
     tau = (tau < SI[1]) ? SI[1] : tau;
     tau = (tau < SI[2]) ? SI[2] : tau;
   }
-  const int pat = cutoff_pattern(SI, tau, HTENO_LAG_EPSZ, HTENO_LAG_CT);
+  return cutoff_pattern(SI, tau, HTENO_LAG_EPSZ, HTENO_LAG_CT);
+}
+
+// One side of teno5 / teno5i given the candidates p and stencil v.
+__device__ __forceinline__ double teno_side_si(const DevConst& C, const double* p, const double* v,
+                                               const double* SI, int side, bool improved) {
+  const int pat = teno_decide(v, SI, improved);
   const double* w = side ? C.wtab_p[pat] : C.wtab_m[pat];
   return catchnan(dot3v(p, w));
 }

@@ -113,6 +113,7 @@ def lib() -> ctypes.CDLL:
         L.hteno_set_router.argtypes = [vp, vp, ctypes.c_float, i]
         L.hteno_router_stats.argtypes = [vp, ctypes.POINTER(ctypes.c_longlong)]
         L.hteno_set_router_schedule.argtypes = [vp, i, i]
+        L.hteno_router_audit64.argtypes = [vp, ctypes.POINTER(ctypes.c_longlong)]
         L.hteno_kxrcf.argtypes = [vp, vp]
         L.hteno_harvest.argtypes = [vp, d, ctypes.c_ulonglong, vp, vp, l, ctypes.POINTER(l)]
         L.hteno_mlp_create.argtypes = [ctypes.c_ulonglong, ctypes.POINTER(vp)]
@@ -270,6 +271,13 @@ class Solver:
         """Classify every `classify_every` steps; keep a route bit only where it is set on every
         face within `margin` faces (call after set_router)."""
         _check(lib().hteno_set_router_schedule(self.h, int(classify_every), int(margin)), self.h)
+
+    def router_audit64(self) -> dict:
+        """Classify the current state and count the routed stencils whose plain FP64 TENO cut-off
+        (on the double state) would drop a candidate."""
+        a = (ctypes.c_longlong * 2)()
+        _check(lib().hteno_router_audit64(self.h, a), self.h)
+        return {"routed": a[0], "misrouted64": a[1]}
 
     def router_stats(self) -> dict:
         a = (ctypes.c_longlong * 7)()

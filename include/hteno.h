@@ -297,8 +297,17 @@ int hteno_set_router_schedule(hteno_solver* s, int classify_every, int margin);
  * all-smooth by plain TENO, flat (a window of equal float values: the stage kernel takes the
  * linear weights for it without the network or the indicators -- plain TENO keeps all three
  * candidates there), number of audited steps, and the number of stencils the last
- * classification handed to the network.  Also reports a classifier timeout. */
+ * classification handed to the network; sums since the last hteno_set_router or hteno_set_state.
+ * Also reports a classifier timeout. */
 int hteno_router_stats(hteno_solver* s, long long* stats);
+
+/* The FP64 judge of the routing: classifies the solver's current state as a step does (with the
+ * schedule's erosion), then, for every stencil the masks route, evaluates in double from the
+ * double state (Roe average and projection in double) the TENO cut-off the plain FP64 solver
+ * decides (cutOff, Schemes_Lagrange.cpp:1141-1149).  counts[0] = routed stencils, counts[1] =
+ * those the FP64 cut-off would not reconstruct with all three candidates.  Synchronous; the masks
+ * it leaves are those of the current state.  No reference counterpart. */
+int hteno_router_audit64(hteno_solver* s, long long* counts);
 
 /* ---- Tracing: per-kernel CUDA-event timing of hteno_step ---------------------------------- */
 

@@ -162,40 +162,148 @@ def test_router_schedule(hteno_lib, cuda):
             s.set_router_schedule(2, 1)  # no router set
 
 
-def test_trained_router_gains(hteno_lib, cuda):
-    """Train on rows harvested from plain runs (fresh seeds), then route a mixed 256^2 run: most
-    stencils skip the nonlinear weights, few are misrouted, and the density error against FP64
-    stays within the mixed path's bound."""
-    from hteno import ic, learned
+def host_misrouted64(oracle, q, bc):
+    """Stencils of every face whose FP64 TENO5 cut-off, computed on the host from the oracle's Roe
+    eigenvectors, drops a candidate; and the number of stencils."""
+    ny, nx = q.shape[1], q.shape[2]
+    bad = total = 0
+    for d in (1, 2):
+        nf, nt, ns = (nx + 1, ny, nx) if d == 1 else (ny + 1, nx, ny)
+        f, t = np.meshgrid(np.arange(nf), np.arange(nt), indexing="ij")
+        f, t = f.ravel(), t.ravel()
+
+        def cells(off):
+            s = (f - 1 + off) % ns if bc == 1 else np.clip(f - 1 + off, 0, ns - 1)
+            return q[:, t, s].T if d == 1 else q[:, s, t].T  # [n, 4]
+
+        _, L = oracle.roe2d(1.4, d, np.ascontiguousarray(cells(0)), np.ascontiguousarray(cells(1)))
+        L = L.reshape(-1, 4, 4)
+        ch = np.stack([np.einsum("nrv,nv->nr", L, cells(m - 2)) for m in range(6)], axis=2)  # [n, 4, 6]
+        for r in range(4):
+            bad += int((teno5_pattern(ch[:, r, 0:5]) != 7).sum())
+            bad += int((teno5_pattern(ch[:, r, 1:6]) != 7).sum())  # the + side: cells 1..5
+        total += 8 * f.size
+    return bad, total
+
+
+def test_router_audit64_matches_host(hteno_lib, cuda, oracle):
+    """The FP64 judge of the routing: with every stencil routed on a periodic state without flat
+    stencils, it counts every stencil as routed, and the stencils whose plain FP64 cut-off drops a
+    candidate agree with a host computation from the oracle's eigenvectors (up to decisions at the
+    cut-off threshold, which rounding can move).  A router that routes nothing routes nothing."""
+    from hteno import ic
+
+    h = hteno_lib
+    q = ic.smooth_waves_2d(48, 40)
+    q[0] += 0.05 * (np.arange(48)[None, :] % 7 == 0)  # a few kinks, so that some cut-offs drop
+    q = np.ascontiguousarray(q)
+    want, total = host_misrouted64(oracle, q, 1)
+    cfg = h.config(dims=2, nx=48, ny=40, flux=1, bc=1, precision=1)
+    with constant_classifier(h, 20.0) as all_smooth, constant_classifier(h, -20.0) as none:
+        with h.Solver(cfg) as s:
+            s.set_router(all_smooth, 0.9, 0)
+            s.set_state(q)
+            got = s.router_audit64()
+            s.set_router(none, 0.9, 0)
+            got0 = s.router_audit64()
+    assert got["routed"] == total
+    assert 0 < want < total and abs(got["misrouted64"] - want) <= 0.005 * total + 2, (got, want)
+    assert got0["routed"] == 0 and got0["misrouted64"] == 0
+
+
+@pytest.fixture(scope="module")
+def trained(hteno_lib, cuda):
+    """A classifier trained on rows the plain FP64 solver records from 256^2 four-quadrant runs
+    with fresh seeds (and the Sod tube)."""
+    from hteno import learned
 
     h = hteno_lib
     x, y = learned.harvest_runs(h, cuda, seeds=[41, 42], n=256, snapshots=(0, 15, 30), keep=1.0)
     assert x.shape[0] > 50000
-    with h.Mlp(seed=1) as m:
-        loss0 = m.grad(x, y)[1]
-        loss = m.train(x, y, epochs=10, batch=8192, lr=3e-3)
-        acc, routed, mis = learned.accuracy(m, cuda, x, y, 0.9)
-        assert loss < 0.7 * loss0 and acc > 0.85 and mis < 0.05, (loss0, loss, acc, routed, mis)
-        q = ic.four_quadrant(256, 256, 99)
-        cfg = h.config(dims=2, nx=256, ny=256, flux=1)
-        with h.Solver(cfg) as s:
-            s.set_state(q)
-            s.step(30)
-            t_ref, _, _ = s.time()
-            ref = s.get_state()
-        cfg = h.config(dims=2, nx=256, ny=256, flux=1, precision=1)
-        with h.Solver(cfg) as s:
-            s.set_router(m, 0.99, 5)
-            s.set_state(q)
-            s.step(1000, t_ref)
-            st = s.router_stats()
-            got = s.get_state()
-    from hteno import metrics
+    m = h.Mlp(seed=1)
+    loss0 = m.grad(x, y)[1]
+    loss = m.train(x, y, epochs=10, batch=8192, lr=3e-3)
+    acc, routed, mis = learned.accuracy(m, cuda, x, y, 0.9)
+    assert loss < 0.7 * loss0 and acc > 0.85 and mis < 0.05, (loss0, loss, acc, routed, mis)
+    yield m
+    m.close()
 
+
+def test_trained_router_accuracy(hteno_lib, cuda, trained):
+    """Route a mixed 256^2 four-quadrant run: the density error against FP64 stays within the
+    mixed path's bound and no shock moves by more than one cell; the network routes non-flat
+    stencils, and the FP64 judge finds few of them misrouted."""
+    from hteno import ic, metrics
+
+    h = hteno_lib
+    q = ic.four_quadrant(256, 256, 99)
+    with h.Solver(h.config(dims=2, nx=256, ny=256, flux=1)) as s:
+        s.set_state(q)
+        s.step(30)
+        t_ref, _, _ = s.time()
+        ref = s.get_state()
+    with h.Solver(h.config(dims=2, nx=256, ny=256, flux=1, precision=1)) as s:
+        s.set_router(trained, 0.99, 5)
+        s.set_state(q)
+        s.step(1000, t_ref)
+        st = s.router_stats()
+        got = s.get_state()
+        a64 = s.router_audit64()
     l1 = np.abs(got[0] - ref[0]).mean()
     assert l1 <= 1e-4, l1  # the accuracy bound of the learned path against FP64
     assert metrics.shock_shift(got[0], ref[0]) <= 1  # no shock moves by more than one cell
-    # the network does route stencils that are not flat.  (The audit's "misrouted" compares with
-    # the float cut-off of the stage kernel, which on small-amplitude smooth data is decided by
-    # float rounding; the labels the network learned are the FP64 solver's.)
     assert st["routed"] > 0 and st["flat"] > 0, st
+    assert a64["routed"] > 0 and a64["misrouted64"] <= 0.05 * a64["routed"], a64
+
+
+def step_kernels_ms(h, s, steps):
+    """Per-step time of the stage kernels (CUDA events around each launch) and of the classifier."""
+    import ctypes
+
+    lib = h.lib()
+    lib.hteno_enable_kernel_timing(s.h, 1)
+    s.step(steps)
+    kt = (h.KernelTime * 16)()
+    cnt = ctypes.c_int()
+    lib.hteno_kernel_timing(s.h, kt, 16, ctypes.byref(cnt))
+    lib.hteno_enable_kernel_timing(s.h, 0)
+    ms = {kt[k].name.decode(): kt[k].ms / steps for k in range(cnt.value) if kt[k].launches}
+    return sum(v for k, v in ms.items() if k.startswith("fused")), ms.get("classify", 0.0)
+
+
+def test_trained_router_gains(hteno_lib, cuda, trained):
+    """What the trained network gains over plain TENO, on a fixed case with no flat stencil: a
+    smooth periodic flow on 1024^2.  The network routes nearly every stencil to the linear
+    weights, the stage kernels skip the nonlinear weights there and run faster than plain TENO's,
+    and the solution is the plain mixed solution to float rounding (TENO keeps all three
+    candidates on smooth data too).  Classified every 20 steps with masks eroded by 8 faces, the
+    classifier's share is small enough that whole steps are faster as well."""
+    from hteno import ic
+
+    h = hteno_lib
+    n = 1024
+    q = ic.smooth_waves_2d(n, n)
+    cfg = h.config(dims=2, nx=n, ny=n, flux=1, bc=1, precision=1)
+    with h.Solver(cfg) as s:
+        s.set_state(q)
+        s.step(5)
+        plain_stage, _ = step_kernels_ms(h, s, 40)
+        s.set_state(q)
+        s.step(45)
+        want = s.get_state()
+    with h.Solver(cfg) as s:
+        s.set_router(trained, 0.99, 0)
+        s.set_router_schedule(20, 8)
+        s.set_state(q)
+        s.step(5)
+        routed_stage, classify = step_kernels_ms(h, s, 40)
+        s.set_state(q)
+        s.step(40)
+        st = s.router_audit64()
+        s.set_state(q)
+        s.step(45)
+        got = s.get_state()
+    assert st["routed"] >= 0.9 * 8 * 2 * n * (n + 1) and st["misrouted64"] <= 1e-4 * st["routed"], st
+    assert np.abs(got[0] - want[0]).max() <= 1e-5 * np.abs(want[0]).max()
+    assert routed_stage <= 0.97 * plain_stage, (routed_stage, plain_stage)
+    assert routed_stage + classify <= plain_stage, (routed_stage, classify, plain_stage)
