@@ -411,24 +411,34 @@ def learned_path(hteno, torch, stream, args, world, n=4096):
             l1, linf = density_errors(got, ref)
             shift = shock_shift(got, ref)
             shares = kernel_shares(hteno, s, 2)  # a separate pass after the timed run
+            a64 = None
+            if router is not None:  # the FP64 judge at 5 points of an untimed replay of the run
+                s.set_state(q)
+                a64 = {"routed": 0, "misrouted64": 0, "snapshots": 0}
+                for _ in range(5):
+                    s.step(nsteps // 5, t_ref)
+                    a = s.router_audit64()
+                    a64["routed"] += a["routed"]
+                    a64["misrouted64"] += a["misrouted64"]
+                    a64["snapshots"] += 1
+                a64["misrouted64_of_routed"] = a64["misrouted64"] / max(1, a64["routed"])
         d = {"value": n * n * nsteps * world / (ms / 1e3) / 1e6, "unit": UNIT,
              "ms_per_step": ms / nsteps, "steps": nsteps, "t_end": t_end,
              "speedup_vs_fp64": (ms64 / n64) / (ms / nsteps),
              "l1_rho_vs_fp64": l1, "linf_rho_vs_fp64": linf, "shock_shift_cells": shift,
              "uniform_cell_fraction": uc / (3.0 * n * n * nsteps), "kernel_shares": shares}
         if st is not None:
-            nonflat_smooth = max(1, st["smooth"] - st["flat"])
             d["router"] = {"audited_stencils": st["seen"], "routed_fraction": st["routed"] / max(1, st["seen"]),
                            "flat_fraction": st["flat"] / max(1, st["seen"]),
-                           "routed_of_nonflat_smooth": st["routed"] / nonflat_smooth,
+                           "routed_of_nonflat": st["routed"] / max(1, st["seen"] - st["flat"]),
                            "network_rows_last_step": st["network_rows"],
-                           "misrouted_of_routed": st["misrouted"] / max(1, st["routed"]),
+                           "misrouted_of_routed_float": st["misrouted"] / max(1, st["routed"]),
+                           "fp64_judge": a64,
                            "plain_teno_smooth_fraction": st["smooth"] / max(1, st["seen"]),
                            "audited_steps": st["audits"], "threshold": args.c5_threshold,
                            "audit_every": args.c5_audit_every, "classify_every": every,
                            "margin_faces": marg}
         out[name] = d
-    m.close()
     out["learned_vs_fp32_plain"] = out["fp32_plain"]["ms_per_step"] / out["fp32_learned"]["ms_per_step"]
     sched = "fp32_learned_every%d" % args.c5_classify_every
     out["learned_every_vs_fp32_plain"] = out["fp32_plain"]["ms_per_step"] / out[sched]["ms_per_step"]
@@ -449,8 +459,61 @@ def learned_path(hteno, torch, stream, args, world, n=4096):
     ceil["note"] = ("5 steps from the FP32 arm's end state: every stencil by TENO5 vs every stencil by the "
                     "linear weights; no router can save more than max_saving of a step")
     out["routing_ceiling"] = ceil
+    out["smooth_2048"] = learned_smooth(hteno, torch, stream, world, m)
+    m.close()
     out["window"] = (f"every arm from the initial state: FP64 {args.c5_steps} steps, the FP32 arms to the "
                      "FP64 arm's end time; errors at that time")
+    return out
+
+
+def learned_smooth(hteno, torch, stream, world, m, n=2048, steps=100):
+    """What the trained network gains where the data allow it: a smooth periodic flow on n x n (no
+    discontinuity, no flat stencil), FP64 over `steps` steps from the initial state, FP32 and FP32
+    + learned routing (classified every 20 steps, masks eroded by 8 faces) from the same state to
+    the FP64 arm's end time, each timed over its whole run; density errors against FP64."""
+    from hteno import ic
+
+    q = ic.smooth_waves_2d(n, n)
+    out = {"workload": f"fv2d_smooth_waves_{n}x{n}_periodic_teno5_hllc"}
+
+    def timed(s, k, t_end=float("inf")):
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        s.step_async(k, t_end)
+        ev1.record(stream)
+        ev1.synchronize()
+        s.sync()
+        return ev0.elapsed_time(ev1)
+
+    c64 = hteno.config(dims=2, nx=n, ny=n, flux=hteno.FLUX_HLLC, bc=hteno.BC_PERIODIC, precision=hteno.PREC_FP64)
+    with hteno.Solver(c64) as s:
+        s.set_stream(stream.cuda_stream)
+        s.set_state(q)
+        ms = timed(s, steps)
+        t_ref = s.time()[0]
+        ref = s.get_state()
+    out["fp64"] = {"value": n * n * steps * world / (ms / 1e3) / 1e6, "unit": UNIT, "ms_per_step": ms / steps}
+    c32 = hteno.config(dims=2, nx=n, ny=n, flux=hteno.FLUX_HLLC, bc=hteno.BC_PERIODIC, precision=hteno.PREC_MIXED)
+    for name, router in (("fp32_plain", None), ("fp32_learned_every20", m)):
+        with hteno.Solver(c32) as s:
+            s.set_stream(stream.cuda_stream)
+            if router is not None:
+                s.set_router(router, 0.99, 0)
+                s.set_router_schedule(20, 8)
+            s.set_state(q)
+            s.step(1 << 20, t_ref)
+            k = s.time()[1]
+            s.set_state(q)
+            ms = timed(s, k, t_ref)
+            l1, linf = density_errors(s.get_state(), ref)
+            d = {"value": n * n * k * world / (ms / 1e3) / 1e6, "unit": UNIT, "ms_per_step": ms / k, "steps": k,
+                 "l1_rho_vs_fp64": l1, "linf_rho_vs_fp64": linf}
+            if router is not None:
+                d["fp64_judge_end"] = s.router_audit64()
+            out[name] = d
+    out["learned_vs_fp32_plain"] = out["fp32_plain"]["ms_per_step"] / out["fp32_learned_every20"]["ms_per_step"]
     return out
 
 

@@ -29,6 +29,8 @@ struct BInst {
   double* q1;  // stage-1 state
   double* q2;  // stage-2 state (residual scratch while tuning)
   StepState* st;
+  int has_tm;  // tm valid: TMA staging of the instance's interior tiles
+  alignas(64) CUtensorMap tm[3];  // of q, q1, q2 for the tile shape in use (stages 1, 2, 3 read them)
 };
 
 // One launch per stage over every tile of every instance: block b takes jobs b, b + grid, ...
@@ -36,8 +38,13 @@ template <int TX, int TY, int NT, int MINB>
 __global__ void __launch_bounds__(NT, MINB) k_batch_stage(const BInst* __restrict__ inst,
                                                     const int4* __restrict__ jobs, int njobs,
                                                     int stage) {
-  extern __shared__ __align__(16) unsigned char smem[];
+  extern __shared__ __align__(128) unsigned char smem[];
   auto& S = *reinterpret_cast<fused::Smem<TX, TY>*>(smem);
+  // TMA box copies (tensor maps in the instance records, global memory): one mbarrier per block,
+  // its phase tracked across the block's tiles
+  const bool tma_ok = stage != 0 && (tc::smem_u32(&S.c[0][0]) & 127u) == 0;
+  uint32_t phase = 0;
+  if (tma_ok) fused::tma_setup(S);
   for (int j = blockIdx.x; j < njobs; j += gridDim.x) {
     const int4 job = jobs[j];
     const BInst& I = inst[job.x];
@@ -48,8 +55,10 @@ __global__ void __launch_bounds__(NT, MINB) k_batch_stage(const BInst* __restric
     else if (stage == 2) a = fused::StageArgs{I.q1, I.q, I.q2, I.st};
     else a = fused::StageArgs{I.q2, I.q, I.q, I.st};
     a.skip_uniform = stage != 0;  // stage 0 only times tile shapes: the full work
+    a.tmap = tma_ok && I.has_tm ? &I.tm[stage - 1] : nullptr;
     int bad = 0;
-    const double ms = fused::tile_stage<TX, TY, NT>(c_dev, I.G, job.y, job.z, stage, a, S, bad);
+    const double ms = fused::tile_stage<TX, TY, NT>(c_dev, I.G, job.y, job.z, stage, a, S, bad, phase);
+    if (bad & 4) break;  // a box copy that did not complete: no further copies into this block
     if (stage == 3) {
       block_max_to(ms, &I.st->maxbits);
       if (bad) atomicOr(&I.st->status, bad);
@@ -158,6 +167,8 @@ struct hteno_batch {
   int grid[kNumBVariants] = {0};
   int variant = -1;
   int forced = -1;
+  int maps_variant = -1;  // tile shape the instances' tensor maps were made for
+  bool tma = true;        // HTENO_TMA=0: every tile loads cell by cell
   cudaStream_t stream = nullptr;
   bool own_stream = false;
   cudaGraphExec_t graph = nullptr;
@@ -234,10 +245,35 @@ int tune(hteno_batch* b) {
   return HTENO_OK;
 }
 
+// Tensor maps of every instance's three state buffers for the tile shape in use (boxes of
+// TX + 8 x TY + 6 cells x 4 planes), in the instance records the stage kernel reads.
+int ensure_maps(hteno_batch* b) {
+  if (b->maps_variant == b->variant) return HTENO_OK;
+  const BVariant& V = kBVariants[b->variant];
+  for (int i = 0; i < b->n; ++i) {
+    BInst& I = b->hinst[i];
+    I.has_tm = 0;
+    if (b->tma && I.G.bc < HTENO_BC_TAYLOR)
+      I.has_tm = fused::encode_box_map(&I.tm[0], I.q, I.G.nx, I.G.ny, V.tx + 8, V.ty + 6) &&
+                 fused::encode_box_map(&I.tm[1], I.q1, I.G.nx, I.G.ny, V.tx + 8, V.ty + 6) &&
+                 fused::encode_box_map(&I.tm[2], I.q2, I.G.nx, I.G.ny, V.tx + 8, V.ty + 6);
+  }
+  cudaError_t e = cudaMemcpyAsync(b->dinst, b->hinst.data(), b->n * sizeof(BInst), cudaMemcpyHostToDevice,
+                                  b->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+  if (e != cudaSuccess) return bcuda(b, e, "instance tensor maps");
+  b->maps_variant = b->variant;
+  return HTENO_OK;
+}
+
 // Capture one step into a graph on the batch's stream (rebuilt when the stream changes).
 int ensure_graph(hteno_batch* b) {
   if (b->variant < 0) {
     const int rc = tune(b);
+    if (rc) return rc;
+  }
+  {
+    const int rc = ensure_maps(b);
     if (rc) return rc;
   }
   if (b->graph && b->graph_stream == b->stream) return HTENO_OK;
@@ -364,6 +400,8 @@ int hteno_batch_create(const hteno_config* cfgs, int n, hteno_batch** out) {
     const int v = std::atoi(e);
     if (v >= 0 && v < kNumBVariants) b->forced = v;
   }
+  const char* tma = std::getenv("HTENO_TMA");
+  b->tma = !(tma && tma[0] == '0');
   *out = b;
   return HTENO_OK;
 }
@@ -466,6 +504,14 @@ int hteno_batch_get_time(hteno_batch* b, int i, double* t, long* steps, int* sta
   if (t) *t = s.t;
   if (steps) *steps = long(s.steps);
   if (status) *status = s.status;
+  return HTENO_OK;
+}
+
+int hteno_batch_get_counters(hteno_batch* b, int i, long long* counters) {
+  if (!b || i < 0 || i >= b->n || !counters) return HTENO_ERR_INVALID_ARG;
+  const StepState& s = b->hstate[i];
+  counters[0] = (long long)s.uniform;
+  counters[1] = (long long)s.tma_tiles;
   return HTENO_OK;
 }
 

@@ -32,9 +32,11 @@ __global__ void __launch_bounds__(NT, MINB) k_fused(Geo G, int stage, fused::Sta
   // an audited step that runs (not past the stop time) counts once
   if (stage == 1 && a.audit && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0)
     atomicAdd(a.audit + 6, 1ull);
+  uint32_t phase = 0;
+  if (a.tmap) fused::tma_setup(S);
   int bad = 0;
   const double ms = fused::tile_stage<TX, TY, NT>(c_dev, G, blockIdx.x * TX, blockIdx.y * TY,
-                                                  stage, a, S, bad);
+                                                  stage, a, S, bad, phase);
   if (stage == 3) {
     block_max_to(ms, &a.st->maxbits);
     if (bad) atomicOr(&a.st->status, bad);
@@ -100,29 +102,6 @@ void launch_v(cudaStream_t cs, const Geo& G, int stage, const fused::StageArgs& 
                                                                           tm ? 1 : 0);
 }
 
-// Tensor map of one [4][ny][nx] double state buffer for variant V's box; false when the grid
-// cannot be staged by TMA (nx odd: the row stride is not a multiple of 16 bytes) or encoding fails.
-bool encode_box_map(CUtensorMap* m, const double* base, int nx, int ny, int box_x, int box_y) {
-  static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
-  static bool looked = false;
-  if (!looked) {
-    looked = true;
-    void* fn = nullptr;
-    cudaDriverEntryPointQueryResult q;
-    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) ==
-            cudaSuccess && q == cudaDriverEntryPointSuccess)
-      encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
-  }
-  if (!encode || (nx & 1) || (reinterpret_cast<uintptr_t>(base) & 15)) return false;
-  const cuuint64_t dims[3] = {cuuint64_t(nx), cuuint64_t(ny), 4};
-  const cuuint64_t strides[2] = {cuuint64_t(nx) * sizeof(double), cuuint64_t(nx) * ny * sizeof(double)};
-  const cuuint32_t box[3] = {cuuint32_t(box_x), cuuint32_t(box_y), 4};
-  const cuuint32_t estr[3] = {1, 1, 1};
-  return encode(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3, const_cast<double*>(base), dims, strides, box, estr,
-                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-                CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
-}
-
 template <int TX, int TY, int NT, int MINB>
 cudaError_t prepare_v() {
   return cudaFuncSetAttribute(k_fused<TX, TY, NT, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -158,7 +137,7 @@ void ensure_maps(hteno_solver* s, const Geo& G, const Variant& V, const double* 
   const double* bufs[3] = {s->q, s->q0, qc};
   s->tmap_ok = true;
   for (int k = 0; k < 3; ++k)
-    s->tmap_ok = s->tmap_ok && encode_box_map(reinterpret_cast<CUtensorMap*>(s->tmap[k]), bufs[k], G.nx,
+    s->tmap_ok = s->tmap_ok && fused::encode_box_map(reinterpret_cast<CUtensorMap*>(s->tmap[k]), bufs[k], G.nx,
                                               G.ny, V.tx + 8, V.ty + 6);
 }
 
@@ -181,6 +160,30 @@ void launch_stage(hteno_solver* s, const Geo& G, int stage, const fused::StageAr
 }
 
 }  // namespace
+
+// Tensor map of one [4][ny][nx] double state buffer for a box_x x box_y x 4 box; false when the
+// grid cannot be staged by TMA (nx odd: the row stride is not a multiple of 16 bytes) or encoding
+// fails.
+bool fused::encode_box_map(CUtensorMap* m, const double* base, int nx, int ny, int box_x, int box_y) {
+  static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+  static bool looked = false;
+  if (!looked) {
+    looked = true;
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess && q == cudaDriverEntryPointSuccess)
+      encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+  }
+  if (!encode || (nx & 1) || (reinterpret_cast<uintptr_t>(base) & 15)) return false;
+  const cuuint64_t dims[3] = {cuuint64_t(nx), cuuint64_t(ny), 4};
+  const cuuint64_t strides[2] = {cuuint64_t(nx) * sizeof(double), cuuint64_t(nx) * ny * sizeof(double)};
+  const cuuint32_t box[3] = {cuuint32_t(box_x), cuuint32_t(box_y), 4};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  return encode(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3, const_cast<double*>(base), dims, strides, box, estr,
+                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
 
 size_t fv2d_fused_work_bytes(int nx, int ny) { return 4 * size_t(nx) * ny * sizeof(double) + 256; }
 

@@ -82,6 +82,10 @@ __device__ __forceinline__ double (*stage_box(Smem<TX, TY>& S))[Box<TX, TY>::Y][
 }
 constexpr uint32_t kTmaWaitLimit = 1u << 20;  // polls of the TMA box's mbarrier before giving up
 
+// Tensor map of one [4][ny][nx] double state buffer with a box_x x box_y x 4 box (fv2d_fused.cu);
+// false when the grid cannot be staged by TMA (odd nx) or encoding fails.
+bool encode_box_map(CUtensorMap* m, const double* base, int nx, int ny, int box_x, int box_y);
+
 template <int TX, int TY>
 constexpr size_t smem_bytes() {
   return sizeof(Smem<TX, TY>);
@@ -228,13 +232,26 @@ __device__ __forceinline__ bool tame_state(float r, float mx, float my, float e,
   return r >= lo && r <= hi && p >= lo && p <= hi && u * u + v * v <= 64.0f * (gamma * p * ir);
 }
 
+// The block's TMA mbarrier (S.bar), initialised once per launch before its first tile when a
+// tensor map may be used; tma_phase then tracks the parity of the block's next box copy.
+template <int TX, int TY>
+__device__ __forceinline__ void tma_setup(Smem<TX, TY>& S) {
+  if (threadIdx.x == 0) {
+    tc::mbar_init(&S.bar, 1);
+    tc::fence_mbar_init();
+  }
+  __syncthreads();
+}
+
 // The tile at (i0, j0) of grid G.  Every thread of the block must call it (barriers inside).
 // Returns this thread's max wave speed over the cells it updated (stage 3) and ORs health flags
-// into *bad.
+// into *bad (bit 2: the tile's TMA copy did not complete within the bounded wait; the tile is
+// left unwritten and the caller must stop using the block's shared memory for box copies).
+// tma_phase: parity of the block's next TMA box copy (tma_setup ran), flipped by each copy.
 template <int TX, int TY, int NT>
 __device__ __forceinline__ double tile_stage(const DevConst& C, const Geo& G, int i0, int j0,
                                              int stage, const StageArgs& a, Smem<TX, TY>& S,
-                                             int& bad) {
+                                             int& bad, uint32_t& tma_phase) {
   typedef Shape<TX, TY> Sh;
   RouteCount rc;
   // routing is a run-time switch (uniform per launch): the same machine code serves the plain and
@@ -257,11 +274,7 @@ __device__ __forceinline__ double tile_stage(const DevConst& C, const Geo& G, in
                        j0 + TY + 3 <= G.ny;
   if (use_tma) {
     auto box = stage_box(S);
-    if (tid == 0) {
-      tc::mbar_init(&S.bar, 1);
-      tc::fence_mbar_init();
-    }
-    __syncthreads();
+    __syncthreads();  // every thread is done with the box region (a previous tile's fluxes)
     if (tid == 0) {
       tc::fence_proxy_async();  // earlier generic accesses to the box region come first
       tc::mbar_arrive_expect_tx(&S.bar, Box<TX, TY>::kBytes);
@@ -269,14 +282,15 @@ __device__ __forceinline__ double tile_stage(const DevConst& C, const Geo& G, in
     }
     // bounded wait; on giving up (never expected) the block flags the step, waits once more
     // for its copy in flight, and leaves this tile unwritten
-    const bool late = __syncthreads_or(!tc::mbar_wait(&S.bar, 0, kTmaWaitLimit));
+    const bool late = __syncthreads_or(!tc::mbar_wait(&S.bar, tma_phase, kTmaWaitLimit));
     if (late) {
-      tc::mbar_wait(&S.bar, 0, kTmaWaitLimit);
+      tc::mbar_wait(&S.bar, tma_phase, kTmaWaitLimit);
       if (tid == 0 && a.st) atomicOr(&a.st->status, 4);
       __syncthreads();
       bad |= 4;
       return 0.0;
     }
+    tma_phase ^= 1u;
     if (tid == 0 && a.st) atomicAdd(&a.st->tma_tiles, 1ull);
     for (int it = tid; it < Sh::W * Sh::H; it += NT) {
       const int y = it / Sh::W, x = it - y * Sh::W;

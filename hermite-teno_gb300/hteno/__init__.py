@@ -108,6 +108,7 @@ def lib() -> ctypes.CDLL:
         L.hteno_batch_sync.argtypes = [vp]
         L.hteno_batch_get_time.argtypes = [vp, i, _D, ctypes.POINTER(l), ctypes.POINTER(i)]
         L.hteno_batch_tile.argtypes = [vp, ctypes.POINTER(i), ctypes.POINTER(i), ctypes.POINTER(i)]
+        L.hteno_batch_get_counters.argtypes = [vp, i, ctypes.POINTER(ctypes.c_longlong)]
         L.hteno_batch_last_error.restype = ctypes.c_char_p
         L.hteno_batch_last_error.argtypes = [vp]
         L.hteno_set_router.argtypes = [vp, vp, ctypes.c_float, i]
@@ -351,6 +352,11 @@ class Batch:
         t, n, st = ctypes.c_double(), ctypes.c_long(), ctypes.c_int()
         self._check(lib().hteno_batch_get_time(self.h, i, ctypes.byref(t), ctypes.byref(n), ctypes.byref(st)))
         return t.value, n.value, st.value
+
+    def counters(self, i: int) -> dict:
+        a = (ctypes.c_longlong * 2)()
+        self._check(lib().hteno_batch_get_counters(self.h, i, a))
+        return {"uniform_cells": a[0], "tma_tiles": a[1]}
 
     def tile(self):
         tx, ty, nt = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()

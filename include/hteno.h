@@ -219,6 +219,9 @@ int hteno_batch_step_async(hteno_batch* b, int nsteps, double t_final);
 int hteno_batch_sync(hteno_batch* b);
 /* Time, completed steps and health flags of instance i as of the last hteno_batch_sync. */
 int hteno_batch_get_time(hteno_batch* b, int i, double* t, long* steps, int* status);
+/* Work counters of instance i as of the last hteno_batch_sync, as hteno_get_counters reports
+ * them for a solver (uniform cell-stages, tiles staged by TMA), since its last set_state. */
+int hteno_batch_get_counters(hteno_batch* b, int i, long long* counters);
 /* Tile shape in use (tunes first if needed). */
 int hteno_batch_tile(hteno_batch* b, int* tx, int* ty, int* threads);
 const char* hteno_batch_last_error(hteno_batch* b);

@@ -92,3 +92,28 @@ def test_batch_tuner_picks_a_candidate(hteno_lib, cuda):
     with b:
         tx, ty, nt = b.tile()
         assert (tx, ty, nt) in {(32, 16, 256), (32, 8, 256), (16, 16, 256), (64, 8, 256), (32, 32, 512), (16, 8, 128)}
+
+
+def test_batch_tma_same_bits(hteno_lib, cuda):
+    """Interior tiles of the batch's instances staged by TMA box copies (tensor maps in the instance
+    records) give the same bits as cell-by-cell loads (HTENO_TMA=0), for three forced tile shapes;
+    an instance with an odd nx (row stride not a multiple of 16 bytes) loads cell by cell."""
+    sizes = [(250, 128), (130, 70), (96, 96), (64, 64), (161, 90)]
+    for v in (0, 4, 6):
+        outs = []
+        try:
+            os.environ["HTENO_FV2D_TILE"] = str(v)
+            for tma in ("1", "0"):
+                os.environ["HTENO_TMA"] = tma
+                b, _, _ = make_batch(hteno_lib, sizes, seed0=31)
+                with b:
+                    b.step(12)
+                    outs.append([b.get_state(k) for k in range(len(sizes))])
+                    tiles = b.counters(0)["tma_tiles"]  # the 250 x 128 instance
+                    assert (tiles > 0) == (tma == "1"), (v, tma, tiles)
+                    assert b.counters(4)["tma_tiles"] == 0
+        finally:
+            os.environ.pop("HTENO_TMA", None)
+            os.environ.pop("HTENO_FV2D_TILE", None)
+        for a, c in zip(outs[0], outs[1]):
+            np.testing.assert_array_equal(a, c)
