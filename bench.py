@@ -72,7 +72,7 @@ def parse():
                     help="second learned arm: the classifier runs every this many steps and its masks "
                          "serve the steps between (the first learned arm classifies every step)")
     ap.add_argument("--c5-margin", type=int, default=-1,
-                    help="erosion of the second arm's route masks in faces (default ceil(cfl * classify-every))")
+                    help="erosion of the second arm's route masks in faces (default 2 ceil(cfl * classify-every))")
     ap.add_argument("--c5-threshold", type=float, default=0.99,
                     help="routing threshold: a stencil takes the linear weights when all three "
                          "predicted cut-off probabilities exceed it")
@@ -365,7 +365,8 @@ def learned_path(hteno, torch, stream, args, world, n=4096):
                        "deterministic": "per-CTA partial gradients summed in CTA order"}
     del x, y
     q = ic.four_quadrant(n, n, 7)
-    margin = args.c5_margin if args.c5_margin >= 0 else int(np.ceil(0.4 * args.c5_classify_every - 1e-9))
+    # twice the distance a discontinuity can travel between classifications (cfl 0.4)
+    margin = args.c5_margin if args.c5_margin >= 0 else 2 * int(np.ceil(0.4 * args.c5_classify_every - 1e-9))
 
     def timed_run(s, nsteps, t_end=float("inf")):
         ev0 = torch.cuda.Event(enable_timing=True)
@@ -414,14 +415,16 @@ def learned_path(hteno, torch, stream, args, world, n=4096):
             a64 = None
             if router is not None:  # the FP64 judge at 5 points of an untimed replay of the run
                 s.set_state(q)
-                a64 = {"routed": 0, "misrouted64": 0, "snapshots": 0}
+                a64 = {"routed": 0, "misrouted64": 0, "routed_resolved": 0, "misrouted64_resolved": 0,
+                       "snapshots": 0}
                 for _ in range(5):
                     s.step(nsteps // 5, t_ref)
                     a = s.router_audit64()
-                    a64["routed"] += a["routed"]
-                    a64["misrouted64"] += a["misrouted64"]
+                    for key in ("routed", "misrouted64", "routed_resolved", "misrouted64_resolved"):
+                        a64[key] += a[key]
                     a64["snapshots"] += 1
                 a64["misrouted64_of_routed"] = a64["misrouted64"] / max(1, a64["routed"])
+                a64["misrouted64_of_routed_resolved"] = a64["misrouted64_resolved"] / max(1, a64["routed_resolved"])
         d = {"value": n * n * nsteps * world / (ms / 1e3) / 1e6, "unit": UNIT,
              "ms_per_step": ms / nsteps, "steps": nsteps, "t_end": t_end,
              "speedup_vs_fp64": (ms64 / n64) / (ms / nsteps),

@@ -167,7 +167,8 @@ int fv2d_harvest(hteno_solver* s, const Geo& G, const Work<double>& W, double p,
                  unsigned long long* count);
 
 // FP64 judge of learned routing (fv2d_fp64.cu): counts[0] routed stencils of the masks, counts[1]
-// those whose plain FP64 TENO cut-off on the double state drops a candidate.
+// those whose plain FP64 TENO cut-off on the double state drops a candidate; counts[2], [3] the
+// same over the stencils whose variation is resolved in float.
 int fv2d_audit64(hteno_solver* s, const Geo& G, const double* q, const uint8_t* mx, const uint8_t* my,
                  long long* counts);
 

@@ -224,7 +224,11 @@ __global__ void __launch_bounds__(kFaceThreads) kp_harvest(Geo G, const double* 
 // stencil, the face's characteristic stencils in double from the double state (Roe average of
 // the two cells, the 6 cells projected) and, per routed (field, side), the TENO cut-off the plain
 // FP64 solver decides on that stencil.  out[0] += routed stencils, out[1] += those whose cut-off
-// drops a candidate (pattern != 7).
+// drops a candidate (pattern != 7); out[2], out[3]: the same over the routed stencils whose
+// variation is resolved in float (max - min of the 5-value window above 2^-16 of its largest
+// magnitude, ~500 float ulps).  Below that the window's shape -- and the cut-off decided on it --
+// is set by the rounding noise the float fluxes leave in the state, and linear weights there
+// change the solution by no more than that noise.
 template <int DIR>
 __global__ void __launch_bounds__(kFaceThreads) kp_audit64(Geo G, const double* __restrict__ q,
                                                            const uint8_t* __restrict__ mask,
@@ -232,7 +236,7 @@ __global__ void __launch_bounds__(kFaceThreads) kp_audit64(Geo G, const double* 
   const int nf = DIR == 1 ? G.nx + 1 : G.ny + 1;
   const int nt = DIR == 1 ? G.ny : G.nx;
   const long idx = blockIdx.x * long(blockDim.x) + threadIdx.x;
-  int routed = 0, wrong = 0;
+  int routed = 0, wrong = 0, routed_r = 0, wrong_r = 0;
   if (idx < long(nf) * nt) {
     int f, t;
     if (DIR == 1) { f = int(idx % nf); t = int(idx / nf); }
@@ -267,18 +271,31 @@ __global__ void __launch_bounds__(kFaceThreads) kp_audit64(Geo G, const double* 
         const double* v = ch[b >> 1] + (b & 1);  // side 1 reconstructs from cells 1..5
         double SI[3];
         par::lagrange_si(v, SI);
+        const int bad = par::teno_decide(v, SI, G.recon == HTENO_RECON_TENO5I) != 7;
+        double lo = v[0], hi = v[0];
+        for (int m = 1; m < 5; ++m) {
+          lo = fmin(lo, v[m]);
+          hi = fmax(hi, v[m]);
+        }
+        const int res = (hi - lo) > 0x1p-16 * fmax(fabs(lo), fabs(hi));
         routed += 1;
-        wrong += par::teno_decide(v, SI, G.recon == HTENO_RECON_TENO5I) != 7;
+        wrong += bad;
+        routed_r += res;
+        wrong_r += res & bad;
       }
     }
   }
   for (int o = 16; o > 0; o >>= 1) {
     routed += __shfl_xor_sync(0xffffffffu, routed, o);
     wrong += __shfl_xor_sync(0xffffffffu, wrong, o);
+    routed_r += __shfl_xor_sync(0xffffffffu, routed_r, o);
+    wrong_r += __shfl_xor_sync(0xffffffffu, wrong_r, o);
   }
   if ((threadIdx.x & 31) == 0 && routed) {
     atomicAdd(out, (unsigned long long)routed);
     if (wrong) atomicAdd(out + 1, (unsigned long long)wrong);
+    if (routed_r) atomicAdd(out + 2, (unsigned long long)routed_r);
+    if (wrong_r) atomicAdd(out + 3, (unsigned long long)wrong_r);
   }
 }
 
@@ -580,20 +597,19 @@ void fv2d_fp64_stage(hteno_solver* s, const Geo& G, const Work<double>& W, int s
 int fv2d_audit64(hteno_solver* s, const Geo& G, const double* q, const uint8_t* mx, const uint8_t* my,
                  long long* counts) {
   unsigned long long* d = nullptr;
-  cudaError_t e = cudaMallocAsync(&d, 2 * sizeof(unsigned long long), s->stream);
+  cudaError_t e = cudaMallocAsync(&d, 4 * sizeof(unsigned long long), s->stream);
   if (e != cudaSuccess) return cuda_error(s, e, "audit counters");
-  cudaMemsetAsync(d, 0, 2 * sizeof(unsigned long long), s->stream);
+  cudaMemsetAsync(d, 0, 4 * sizeof(unsigned long long), s->stream);
   const long nxf = long(G.nx + 1) * G.ny, nyf = long(G.ny + 1) * G.nx;
   kp_audit64<1><<<unsigned((nxf + kFaceThreads - 1) / kFaceThreads), kFaceThreads, 0, s->stream>>>(G, q, mx, d);
   kp_audit64<2><<<unsigned((nyf + kFaceThreads - 1) / kFaceThreads), kFaceThreads, 0, s->stream>>>(G, q, my, d);
-  unsigned long long h[2] = {0, 0};
+  unsigned long long h[4] = {0, 0, 0, 0};
   e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaMemcpyAsync(h, d, sizeof(h), cudaMemcpyDeviceToHost, s->stream);
   cudaFreeAsync(d, s->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
   if (e != cudaSuccess) return cuda_error(s, e, "FP64 routing audit");
-  counts[0] = (long long)h[0];
-  counts[1] = (long long)h[1];
+  for (int k = 0; k < 4; ++k) counts[k] = (long long)h[k];
   return HTENO_OK;
 }
 

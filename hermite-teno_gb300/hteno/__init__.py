@@ -276,9 +276,9 @@ class Solver:
     def router_audit64(self) -> dict:
         """Classify the current state and count the routed stencils whose plain FP64 TENO cut-off
         (on the double state) would drop a candidate."""
-        a = (ctypes.c_longlong * 2)()
+        a = (ctypes.c_longlong * 4)()
         _check(lib().hteno_router_audit64(self.h, a), self.h)
-        return {"routed": a[0], "misrouted64": a[1]}
+        return {"routed": a[0], "misrouted64": a[1], "routed_resolved": a[2], "misrouted64_resolved": a[3]}
 
     def router_stats(self) -> dict:
         a = (ctypes.c_longlong * 7)()

@@ -308,8 +308,11 @@ int hteno_router_stats(hteno_solver* s, long long* stats);
  * schedule's erosion), then, for every stencil the masks route, evaluates in double from the
  * double state (Roe average and projection in double) the TENO cut-off the plain FP64 solver
  * decides (cutOff, Schemes_Lagrange.cpp:1141-1149).  counts[0] = routed stencils, counts[1] =
- * those the FP64 cut-off would not reconstruct with all three candidates.  Synchronous; the masks
- * it leaves are those of the current state.  No reference counterpart. */
+ * those the FP64 cut-off would not reconstruct with all three candidates; counts[2], counts[3] =
+ * the same over the routed stencils whose variation is resolved in float (max - min of the
+ * window above 2^-16 of its largest magnitude): on the others the window's shape, and the cut-off
+ * decided on it, is the rounding noise of the float fluxes.  Synchronous; the masks it leaves
+ * are those of the current state.  No reference counterpart. */
 int hteno_router_audit64(hteno_solver* s, long long* counts);
 
 /* ---- Tracing: per-kernel CUDA-event timing of hteno_step ---------------------------------- */

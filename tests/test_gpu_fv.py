@@ -381,3 +381,16 @@ def test_fv2d_alternative_reconstructions(hteno_lib, cuda, oracle, recon):
         np.testing.assert_array_equal(got, want)
     mixed, _, _ = gpu_run2d(hteno_lib, q, 1000, t_final=t_o, flux=1, recon=recon, precision=1)
     assert np.abs(mixed[0] - want[0]).mean() <= 1e-4
+
+
+def test_fv2d_4096_matches_oracle(hteno_lib, cuda, oracle):
+    """The 4096^2 grid of the learned-routing configuration (four-quadrant data, seed 7, TENO5 +
+    HLLC, plain FP64) for 3 steps against the CPU oracle on the host cores: bit for bit."""
+    from hteno import ic
+
+    q = ic.four_quadrant(4096, 4096, 7)
+    want, t_o, n_o = oracle.fv2d_run(q, 3, flux=1)
+    got, t_g, n_g = gpu_run2d(hteno_lib, q, 3, flux=1)
+    assert n_g == n_o == 3 and t_g == t_o
+    assert rel_linf(got, want) <= TOL
+    np.testing.assert_array_equal(got, want)

@@ -253,7 +253,10 @@ def test_trained_router_accuracy(hteno_lib, cuda, trained):
     assert l1 <= 1e-4, l1  # the accuracy bound of the learned path against FP64
     assert metrics.shock_shift(got[0], ref[0]) <= 1  # no shock moves by more than one cell
     assert st["routed"] > 0 and st["flat"] > 0, st
-    assert a64["routed"] > 0 and a64["misrouted64"] <= 0.05 * a64["routed"], a64
+    # among routed stencils whose variation float resolves, the FP64 cut-off rarely disagrees
+    # (on noise-level windows the cut-off is decided by the float fluxes' rounding noise)
+    assert a64["routed_resolved"] > 0, a64
+    assert a64["misrouted64_resolved"] <= 0.05 * a64["routed_resolved"], a64
 
 
 def step_kernels_ms(h, s, steps):
