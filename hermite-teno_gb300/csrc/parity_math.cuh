@@ -22,7 +22,16 @@
 namespace hteno {
 namespace par {
 
-__device__ __forceinline__ double catchnan(double x) { return isnan(x) ? 1e-15 : x; }
+// Tests on a double's bits, on the integer pipes: the FP64 pipe (1/64 of the FP32 rate on GB300)
+// is left to the arithmetic.  Exactly the IEEE predicates: x == 0.0 (either sign), isnan(x).
+__device__ __forceinline__ bool zero_bits(double x) {
+  return (static_cast<unsigned long long>(__double_as_longlong(x)) << 1) == 0ull;
+}
+__device__ __forceinline__ bool nan_bits(double x) {
+  return (static_cast<unsigned long long>(__double_as_longlong(x)) & 0x7fffffffffffffffull) >
+         0x7ff0000000000000ull;
+}
+__device__ __forceinline__ double catchnan(double x) { return nan_bits(x) ? 1e-15 : x; }
 
 // dot of a 3-vector of coefficients with u[0..2], left to right (Eigen .dot in the reference)
 __device__ __forceinline__ double dot3(double c0, double c1, double c2, const double* u) {
@@ -153,7 +162,9 @@ __device__ __forceinline__ int teno_decide(const double* v, const double* SI, bo
   // equal whatever tau is, and the cut-off keeps all candidates (pattern 7) -- decided without
   // tau, same bits.  (Equal values alone do not suffice: 3u - 4u + u can leave a rounding
   // residue in one indicator.)
-  if (SI[0] == 0.0 && SI[1] == 0.0 && SI[2] == 0.0) return 7;
+  // The full arithmetic below gives pattern 7 on such a window too (three equal ratios), so the
+  // shortcut is taken only when every active lane of the warp can take it: a warp never runs both.
+  if (zero_bits(SI[0]) && zero_bits(SI[1]) && zero_bits(SI[2])) return 7;
   double tau;
   if (!improved) {
     const double b35 = lagrange_b35(v);
@@ -352,7 +363,10 @@ static __device__ __noinline__ void gl3(const DevConst& C, const double* u, doub
   cg[1] = u[1] - 2.0 * u[2] + u[3];
   bg[2] = 3.0 * u[2] - 4.0 * u[3] + u[4];
   cg[2] = u[2] - 2.0 * u[3] + u[4];
-  if (bg[0] == 0.0 && bg[1] == 0.0 && bg[2] == 0.0 && cg[0] == 0.0 && cg[1] == 0.0 && cg[2] == 0.0) {
+  // (taken only when every active lane of the warp can take it: the full arithmetic gives the same
+  // bits on constant data, and a warp then never runs both)
+  if (__all_sync(__activemask(), zero_bits(bg[0]) && zero_bits(bg[1]) && zero_bits(bg[2]) &&
+                                     zero_bits(cg[0]) && zero_bits(cg[1]) && zero_bits(cg[2]))) {
     // every indicator is zero: the normalised weights are the constants gl3flat, which the host
     // computed with these same operations -- the same bits without the 24 divisions
     double p[3];
@@ -501,7 +515,7 @@ __device__ __forceinline__ void right(const Eig& e, int dir, const double* c, do
 __device__ __forceinline__ void hllc(double g1, int dir, const double* ql, const double* qr,
                                      double* F) {
   const int d1 = dir - 1;
-  double wl[4], wr[4], fl[4], fr[4], qs[4];
+  double wl[4], wr[4], fl[4], qs[4];
   primitive(g1, ql, wl);
   primitive(g1, qr, wr);
   const double hl = (ql[3] + wl[3]) / wl[0];
@@ -521,28 +535,34 @@ __device__ __forceinline__ void hllc(double g1, int dir, const double* ql, const
   const double sm = (qr[dir] * (sr - wr[dir]) - ql[dir] * (sl - wl[dir]) + wl[3] - wr[3]) /
                     (wr[0] * (sr - wr[dir]) - wl[0] * (sl - wl[dir]));
   const double ps = wl[3] + wl[0] * (wl[dir] - sl) * (wl[dir] - sm);
-  if (sl > 0.0) {
-    flux(dir, ql, wl, F);
-  } else if (sl <= 0.0 && sm > 0.0) {
-    flux(dir, ql, wl, fl);
-    const double nom = sl - wl[dir], den = sl - sm;
-    qs[0] = wl[0] * nom / den;
-    qs[1] = dir == 1 ? (nom * ql[1] + ps - wl[3]) / den : nom * ql[1] / den;
-    qs[2] = dir == 2 ? (nom * ql[2] + ps - wl[3]) / den : nom * ql[2] / den;
-    qs[3] = (nom * ql[3] - wl[3] * wl[dir] + ps * sm) / den;
+  // The reference's four regions (:408-427).  The two star regions run the same expressions on
+  // the left or the right operands (the energy term keeps the left pressure in both, as the
+  // reference does), and so do the two outer regions, so the operands are selected first and
+  // one copy of the arithmetic runs: a warp whose faces fall in different regions does not pay
+  // for both.  Same operations in the same order on the same values: the same bits.
+  const bool outer_l = sl > 0.0;
+  const bool star_l = !outer_l && sl <= 0.0 && sm > 0.0;
+  const bool star_r = !outer_l && !star_l && sm <= 0.0 && sr >= 0.0;
+  const bool use_l = outer_l || star_l;
+  double q[4], w[4];
 #pragma unroll
-    for (int k = 0; k < 4; ++k) F[k] = fl[k] + sl * (qs[k] - ql[k]);
-  } else if (sm <= 0.0 && sr >= 0.0) {
-    flux(dir, qr, wr, fr);
-    const double nom = sr - wr[dir], den = sr - sm;
-    qs[0] = wr[0] * nom / den;
-    qs[1] = dir == 1 ? (nom * qr[1] + ps - wr[3]) / den : nom * qr[1] / den;
-    qs[2] = dir == 2 ? (nom * qr[2] + ps - wr[3]) / den : nom * qr[2] / den;
-    qs[3] = (nom * qr[3] - wl[3] * wr[dir] + ps * sm) / den;
+  for (int k = 0; k < 4; ++k) {
+    q[k] = use_l ? ql[k] : qr[k];
+    w[k] = use_l ? wl[k] : wr[k];
+  }
+  flux(dir, q, w, fl);
+  if (star_l || star_r) {
+    const double s = use_l ? sl : sr;
+    const double nom = s - w[dir], den = s - sm;
+    qs[0] = w[0] * nom / den;
+    qs[1] = dir == 1 ? (nom * q[1] + ps - w[3]) / den : nom * q[1] / den;
+    qs[2] = dir == 2 ? (nom * q[2] + ps - w[3]) / den : nom * q[2] / den;
+    qs[3] = (nom * q[3] - wl[3] * w[dir] + ps * sm) / den;
 #pragma unroll
-    for (int k = 0; k < 4; ++k) F[k] = fr[k] + sr * (qs[k] - qr[k]);
+    for (int k = 0; k < 4; ++k) F[k] = fl[k] + s * (qs[k] - q[k]);
   } else {
-    flux(dir, qr, wr, F);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) F[k] = fl[k];
   }
 }
 
