@@ -10,13 +10,15 @@
 // multiply-add is fused.  Divisions and square roots are IEEE correctly rounded, as on the CPU.
 //
 // The one deliberate difference: the TENO cut-off weights (1 + tau/(SI+eps))^6 / sum only select
-// one of 8 cut-off patterns, so they are evaluated with reciprocals and a multiply chain; when a
-// weight lies within a relative 1e-10 of the threshold, the decision is recomputed with the
-// reference's divisions and pow.  The reconstructed values use the pattern's weights from a table
+// one of 8 cut-off patterns, so they are evaluated with reciprocals, the ratios to the largest
+// and a float multiply chain; when a weight lies within a relative 1e-5 of the threshold (ten
+// times the float chain's error bound), the decision is recomputed with the reference's
+// divisions and pow.  The reconstructed values use the pattern's weights from a table
 // built with the reference's own normalisation, so they are bit-identical.
 #pragma once
 
 #include "device_math.cuh"
+#include "mixed_conv.cuh"
 #include "hermite_math.cuh"
 
 namespace hteno {
@@ -119,30 +121,46 @@ __device__ __forceinline__ double decision_rcp(double x) {
   return fma(y, fma(-x, y, 1.0), y);
 }
 
-// Cut-off pattern of the reference's cutOff() (:1141-1149) given SI and tau.  Fast path with a
-// guard band of 1e-10 relative (the fast path's own error is ~1e-13); inside the band the
-// reference's arithmetic decides.
+// The fast part of a cut-off decision, in float: x_k = r_k / r_max (in (0, 1], or NaN) converted
+// on the integer pipes, a_k = x_k^6, kept where a_k >= ct * (a_0 + a_1 + a_2).  The float path's
+// relative error is below 1e-6 (x_k to 2^-24, six roundings in a_k, two in the sum), so any a_k
+// farther than 1e-5 of the limit from it is decided as exact arithmetic decides it; nearer ones
+// set *near and the caller takes the reference's own arithmetic.  NaN ratios compare false, as
+// in double.  (The FP64 pipe runs at 1/64 of the float rate on GB300; this part was 24 of the
+// decision's 43 FP64 operations.)
+__device__ __forceinline__ int cutoff_fast(const double* x, double ct, bool* near) {
+  float a[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const float xf = mix::d2f(x[k]);
+    const float x2 = xf * xf;
+    a[k] = (x2 * x2) * x2;
+  }
+  const float lim = float(ct) * ((a[0] + a[1]) + a[2]);
+  int pat = 0;
+  bool nr = false;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    pat |= (a[k] < lim ? 0 : 1) << k;
+    nr |= fabsf(a[k] - lim) <= 1e-5f * lim;
+  }
+  *near = nr;
+  return pat;
+}
+
+// Cut-off pattern of the reference's cutOff() (:1141-1149) given SI and tau.  Fast path (ratios
+// in double, the rest in float, cutoff_fast) with a guard band of 1e-5 relative; inside the band
+// the reference's arithmetic decides.
 __device__ __forceinline__ int cutoff_pattern(const double* SI, double tau, double epsz, double ct) {
-  double r[3], a[3];
+  double r[3], x[3];
 #pragma unroll
   for (int k = 0; k < 3; ++k) r[k] = 1.0 + tau * decision_rcp(SI[k] + epsz);
   const double rm = fmax(fmax(r[0], r[1]), r[2]);
   const double inv = decision_rcp(rm);
 #pragma unroll
-  for (int k = 0; k < 3; ++k) {
-    double x = r[k] * inv;
-    x = x * x;
-    a[k] = x * x * x;
-  }
-  const double S = (a[0] + a[1]) + a[2];
-  const double lim = ct * S;
-  int pat = 0;
-  bool near = false;
-#pragma unroll
-  for (int k = 0; k < 3; ++k) {
-    pat |= (a[k] < lim ? 0 : 1) << k;
-    near |= fabs(a[k] - lim) <= 1e-10 * lim;
-  }
+  for (int k = 0; k < 3; ++k) x[k] = r[k] * inv;
+  bool near;
+  int pat = cutoff_fast(x, ct, &near);
   if (near) {  // reference arithmetic: w_k = pow(1 + tau/(SI_k + epsz), 6) / sum
     double w[3];
 #pragma unroll
@@ -198,21 +216,11 @@ __device__ __forceinline__ double teno_side(const DevConst& C, const double* p, 
 __device__ __forceinline__ int cutoff_from_r(const double* r, double ct) {
   const double rm = fmax(fmax(r[0], r[1]), r[2]);
   const double inv = __drcp_rn(rm);
-  double a[3];
+  double x[3];
 #pragma unroll
-  for (int k = 0; k < 3; ++k) {
-    double x = r[k] * inv;
-    x = x * x;
-    a[k] = x * x * x;
-  }
-  const double lim = ct * ((a[0] + a[1]) + a[2]);
-  int pat = 0;
-  bool near = false;
-#pragma unroll
-  for (int k = 0; k < 3; ++k) {
-    pat |= (a[k] < lim ? 0 : 1) << k;
-    near |= fabs(a[k] - lim) <= 1e-10 * lim;
-  }
+  for (int k = 0; k < 3; ++k) x[k] = r[k] * inv;
+  bool near;
+  int pat = cutoff_fast(x, ct, &near);
   if (near || !(rm < 1e300)) {  // the reference's arithmetic (also for overflowing ratios)
     double w[3];
 #pragma unroll
