@@ -151,3 +151,30 @@ def test_batch_256_configuration(hteno_lib, cuda):
         ref, t_r, _ = single(h, c64, states[k], 1000, t)
         assert t_r == pytest.approx(t, rel=1e-14, abs=0)
         assert np.abs(state[0] - ref[0]).mean() <= 1e-4
+
+
+def test_batch_health_flags_follow_plain_fp64(hteno_lib, cuda):
+    """Instances of the 256-grid configuration that the batch flags as non-physical are flagged by
+    the plain FP64 solver (the reference's arithmetic, bit for bit) in the same steps; a healthy
+    one stays unflagged in both.  Instances 0, 35 and 139: (390 x 487, seed 1000), (511 x 481,
+    seed 1035), (374 x 485, seed 1139)."""
+    from hteno import ic
+
+    h = hteno_lib
+    inst = [((390, 487), 1000), ((511, 481), 1035), ((374, 485), 1139)]
+    cfgs = [h.config(dims=2, nx=nx, ny=ny, flux=1, precision=1) for (nx, ny), _ in inst]
+    states = [ic.four_quadrant(nx, ny, seed) for (nx, ny), seed in inst]
+    with h.Batch(cfgs) as b:
+        for k, q in enumerate(states):
+            b.set_state(k, q)
+        b.step(5)
+        flags = [b.time(k)[2] for k in range(len(inst))]
+    fp64 = []
+    for ((nx, ny), _), q in zip(inst, states):
+        with h.Solver(h.config(dims=2, nx=nx, ny=ny, flux=1)) as s:
+            s.set_state(q)
+            s.step(5)
+            fp64.append(s.status())
+    assert flags[0] == 0 and fp64[0] == 0
+    assert flags[1] and flags[2]
+    assert all(f64 for f, f64 in zip(flags, fp64) if f)

@@ -211,3 +211,15 @@ def test_oracle_matches_reference_live(oracle):
     R.ref_teno5(u.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
                 out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), ctypes.c_long(2000))
     same(oracle.lagrange(0, u), out)
+
+
+def test_fv2d_seeded_quadrants_can_go_nonphysical(oracle):
+    """The reference's own arithmetic leaves the physical states on some seeded four-quadrant
+    data: TENO5 + HLLC at CFL 0.4 without a positivity limiter (the reference's checks are
+    commented out, FV_System2D.cpp:236-250).  Instance 139 of the 256-grid batch configuration
+    (374 x 485, seed 1139) has a negative density after one step, so a health flag on such an
+    instance reports the scheme, not the precision of the path that flags it."""
+    from hteno import ic
+
+    out, t, n = oracle.fv2d_run(ic.four_quadrant(374, 485, 1139), 1)
+    assert n == 1 and out[0].min() < 0.0
