@@ -249,12 +249,17 @@ __global__ void __launch_bounds__(kLimThreads) kh_limit(GeoH G, HermiteK<T> K,
 //   lim = [w0 (p0/lw0 - Q) + w1 p1 + w2 p2] / (w0 + w1 + w2),  w_k = lw_k (1 + tau / (s_k + eps))
 // where only p0 = P - d0/4 and s0 = |(a ud0 + B) ud0 + C|/6720 (ud0 = d0 dif, the smoothness
 // measure fullPointsSI expanded in ud0) depend on d0.  Every other quantity of a cell is computed
-// by all threads of the block in parallel, before the sweep: B, C, s1, s2, E = P/lw0 - Q,
+// off the sweep's chain, before the sweep reaches the cell: B, C, s1, s2, E = P/lw0 - Q,
 // M = lw1 r1 + lw2 r2, L = lw1 p1 + lw2 p2, N = lw1 r1 p1 + lw2 r2 p2 with r_k = 1/(s_k + eps).
 // The sweep then evaluates, per cell,
 //   tau = (|s0 - s1| + |s0 - s2|)^2 / 4,  w0 = lw0 (1 + tau / (s0 + eps)),
 //   lim = (w0 (E - d0 / (4 lw0)) + L + tau N) / (w0 + lw1 + lw2 + tau M).
-constexpr int kLimChunkF = 32;
+// The block's four warps work as a pipeline over chunks of kLimChunkF cells: warp 0 sweeps its
+// 32 lines through chunk s while warps 1-3 load chunk s + 1, precompute its per-cell quantities
+// into the other half of a double buffer, and store the limited values of chunk s - 1; one block
+// barrier per chunk hands the buffers over.  The sweep, the only sequential part, so runs back to
+// back instead of waiting for each chunk's loads, precompute and stores.
+constexpr int kLimChunkF = 16;
 
 __global__ void __launch_bounds__(kLimThreads, 4) kh_limit_f(GeoH G, HermiteK<float> K,
                                                           const double* __restrict__ q,
@@ -264,17 +269,12 @@ __global__ void __launch_bounds__(kLimThreads, 4) kh_limit_f(GeoH G, HermiteK<fl
                                                           float* __restrict__ wt, int nbx,
                                                           const StepState* st) {
   if (st->done) return;
-  constexpr int L = kLimLines, C = kLimChunkF;
+  constexpr int L = kLimLines, C = kLimChunkF, NP = kLimThreads - 32;  // NP producer threads
   constexpr float lw0 = 1.0f - 2e-5f, lw1 = 1e-5f, lw2 = 1e-5f, eps = float(HTENO_LAG_EPS);
-  __shared__ float pre[8][C][L + 1];
-  __shared__ union {
-    struct {
-      float u[C + 2][L + 1];  // cells c0 - 1 .. c0 + cnt (clamped)
-      float d[C][L + 1];      // pre-sweep d of cells c0 + 1 .. c0 + cnt (clamped)
-    } in;
-    double out[C][L + 1];     // limited values of cells c0 .. c0 + cnt - 1
-  } S;
-  __shared__ float outf[C][L + 1];  // the same in float
+  __shared__ float pre[2][8][C][L + 1];
+  __shared__ float su[C + 2][L + 1];  // cells c0 - 1 .. c0 + C of the chunk being prepared (clamped)
+  __shared__ float sd[C][L + 1];      // pre-sweep d of cells c0 + 1 .. c0 + C (clamped)
+  __shared__ float outf[2][C][L + 1];  // limited values (their double copies are exact)
   const bool xd = int(blockIdx.x) < nbx;
   const int b = xd ? int(blockIdx.x) : int(blockIdx.x) - nbx;
   const int nl = xd ? G.ny : G.nx;
@@ -288,63 +288,64 @@ __global__ void __launch_bounds__(kLimThreads, 4) kh_limit_f(GeoH G, HermiteK<fl
     return size_t(e) * nc + (xd ? size_t(l) * G.nx + s : size_t(s) * G.nx + l);
   };
   const int tid = threadIdx.x;
-  const bool sweeper = tid < L && l0 + tid < nl;
+  const bool sweeper_warp = tid < 32;
+  const bool sweeper = sweeper_warp && l0 + tid < nl;
+  const int ptid = tid - 32;
   const float dif = K.dif, rdif = K.rdif;
-  float d0 = sweeper ? mix::d2f(d[at(l0 + tid, 0)]) : 0.f;  // ghost before the first cell
-  // Staging slots of this thread (element tid + 128 j of the chunk's line-major or cell-major
-  // block).  x lines: consecutive threads take consecutive cells of a row; y lines: consecutive
-  // threads take consecutive lines (columns) of a cell row; both coalesce.  u: cells c0 - 1 ..
-  // c0 + cnt of the chunk (row k = 0 .. cnt + 1); d: pre-sweep d of cells c0 + 1 .. c0 + cnt
-  // (row k = 0 .. cnt - 1).  The next chunk's values are loaded into registers while this
-  // chunk is processed.
-  constexpr int NU = ((C + 2) * L + kLimThreads - 1) / kLimThreads, ND = C * L / kLimThreads;
-  auto slot_u = [&](int j, int& l, int& k) {
-    const int el = tid + kLimThreads * j;
-    if (xd) { l = el / (C + 2); k = el - l * (C + 2); }
-    else { l = el % L; k = el / L; }
+  const int nchunks = (n + C - 1) / C;
+  // x lines: consecutive threads take consecutive cells of a row; y lines: consecutive lines
+  // (columns) of a cell row; both coalesce
+  auto slot = [&](int it, int rows, int& l, int& k) {
+    if (xd) { l = it / rows; k = it - l * rows; }
+    else { l = it % L; k = it / L; }
   };
-  auto slot_d = [&](int j, int& l, int& k) {
-    const int el = tid + kLimThreads * j;
-    if (xd) { l = el / C; k = el % C; }
-    else { l = el % L; k = el / L; }
-  };
+  // producers: the raw inputs of a chunk are loaded into registers one step before they are
+  // staged (bu: cells c0 - 1 .. c0 + C, bd: pre-sweep d of cells c0 + 1 .. c0 + C, clamped), so the
+  // loads are in flight during a whole step
+  constexpr int NU = ((C + 2) * L + NP - 1) / NP, ND = (C * L + NP - 1) / NP;
   double bu[NU], bd[ND];
   auto fetch = [&](int c) {
-    const int m = min(C, n - c);
+    const int c0 = c * C, cnt = min(C, n - c0);
 #pragma unroll
     for (int j = 0; j < NU; ++j) {
+      const int it = ptid + NP * j;
       int l, k;
-      slot_u(j, l, k);
-      bu[j] = (l < L && l0 + l < nl && k < m + 2) ? q[at(l0 + l, min(max(c - 1 + k, 0), n - 1))] : 0.0;
+      slot(it, C + 2, l, k);
+      bu[j] = (it < (C + 2) * L && l0 + l < nl && k < cnt + 2)
+                  ? q[at(l0 + l, min(max(c0 - 1 + k, 0), n - 1))] : 0.0;
     }
 #pragma unroll
     for (int j = 0; j < ND; ++j) {
+      const int it = ptid + NP * j;
       int l, k;
-      slot_d(j, l, k);
-      bd[j] = (l < L && l0 + l < nl && k < m) ? d[at(l0 + l, min(c + 1 + k, n - 1))] : 0.0;
+      slot(it, C, l, k);
+      bd[j] = (it < C * L && l0 + l < nl && k < cnt) ? d[at(l0 + l, min(c0 + 1 + k, n - 1))] : 0.0;
     }
   };
-  fetch(0);
-  for (int c0 = 0; c0 < n; c0 += C) {
-    const int cnt = min(C, n - c0);
+  // producers: stage the fetched chunk c, start fetching chunk c + 1, then compute chunk c's
+  // per-cell quantities into pre[buf]
+  auto prepare = [&](int c, int buf) {
+    const int c0 = c * C, cnt = min(C, n - c0);
 #pragma unroll
     for (int j = 0; j < NU; ++j) {
+      const int it = ptid + NP * j;
       int l, k;
-      slot_u(j, l, k);
-      if (l < L && k < cnt + 2) S.in.u[k][l] = mix::d2f(bu[j]);
+      slot(it, C + 2, l, k);
+      if (it < (C + 2) * L && k < cnt + 2) su[k][l] = mix::d2f(bu[j]);
     }
 #pragma unroll
     for (int j = 0; j < ND; ++j) {
+      const int it = ptid + NP * j;
       int l, k;
-      slot_d(j, l, k);
-      if (l < L && k < cnt) S.in.d[k][l] = mix::d2f(bd[j]);
+      slot(it, C, l, k);
+      if (it < C * L && k < cnt) sd[k][l] = mix::d2f(bd[j]);
     }
-    if (c0 + C < n) fetch(c0 + C);  // in flight during the precompute and the sweep
-    __syncthreads();
-    for (int it = tid; it < cnt * L; it += kLimThreads) {
+    if (c + 1 < nchunks) fetch(c + 1);
+    asm volatile("bar.sync 1, %0;" ::"n"(NP));
+    for (int it = ptid; it < cnt * L; it += NP) {
       const int l = it % L, k = it / L;
-      const float u0 = S.in.u[k][l], u1 = S.in.u[k + 1][l], u2 = S.in.u[k + 2][l];
-      const float ud2 = S.in.d[k][l] * dif;
+      const float u0 = su[k][l], u1 = su[k + 1][l], u2 = su[k + 2][l];
+      const float ud2 = sd[k][l] * dif;
       const float p1 = (u1 - u0) * rdif, p2 = (u2 - u1) * rdif;
       const float s1 = (u0 - u1) * (u0 - u1), s2 = (u1 - u2) * (u1 - u2);
       const float r1 = 1.0f / (s1 + eps), r2 = 1.0f / (s2 + eps);
@@ -353,42 +354,58 @@ __global__ void __launch_bounds__(kLimThreads, 4) kh_limit_f(GeoH G, HermiteK<fl
       const float Cc = ((-1029270.0f * u0 + 2129184.0f * u1 - 1099914.0f * u2 + 281121.0f * ud2) * ud2 +
                         (1099445.0f * u2 - 4317056.0f * u1 + 2118166.0f * u0) * u2 +
                         4317056.0f * (u1 - u0) * u1 + 1099445.0f * u0 * u0) * k6720;
-      const float P = 0.75f * (u2 - u0) * rdif - 0.25f * S.in.d[k][l];
-      pre[0][k][l] = B;
-      pre[1][k][l] = Cc;
-      pre[2][k][l] = s1;
-      pre[3][k][l] = s2;
-      pre[4][k][l] = P * (1.0f / lw0) - ((lw1 / lw0) * p1 + (lw2 / lw0) * p2);
-      pre[5][k][l] = lw1 * r1 + lw2 * r2;
-      pre[6][k][l] = lw1 * p1 + lw2 * p2;
-      pre[7][k][l] = lw1 * r1 * p1 + lw2 * r2 * p2;
+      const float P = 0.75f * (u2 - u0) * rdif - 0.25f * sd[k][l];
+      pre[buf][0][k][l] = B;
+      pre[buf][1][k][l] = Cc;
+      pre[buf][2][k][l] = s1;
+      pre[buf][3][k][l] = s2;
+      pre[buf][4][k][l] = P * (1.0f / lw0) - ((lw1 / lw0) * p1 + (lw2 / lw0) * p2);
+      pre[buf][5][k][l] = lw1 * r1 + lw2 * r2;
+      pre[buf][6][k][l] = lw1 * p1 + lw2 * p2;
+      pre[buf][7][k][l] = lw1 * r1 * p1 + lw2 * r2 * p2;
     }
-    __syncthreads();  // the staged inputs are consumed: S.out may overwrite them
-    if (sweeper) {
-      constexpr float a = 281121.0f / 6720.0f, c4 = 0.25f / lw0;
-      for (int k = 0; k < cnt; ++k) {
-        const float ud0 = d0 * dif;
-        const float s0 = fabsf(fmaf(fmaf(a, ud0, pre[0][k][tid]), ud0, pre[1][k][tid]));
-        const float t = fabsf(s0 - pre[2][k][tid]) + fabsf(s0 - pre[3][k][tid]);
-        const float tau = 0.25f * t * t;
-        const float w0 = lw0 * fmaf(tau, __fdividef(1.0f, s0 + eps), 1.0f);
-        const float num = fmaf(w0, fmaf(-c4, d0, pre[4][k][tid]), fmaf(tau, pre[7][k][tid], pre[6][k][tid]));
-        const float den = w0 + fmaf(tau, pre[5][k][tid], lw1 + lw2);
-        d0 = __fdividef(num, den);
-        S.out[k][tid] = mix::f2d(d0);
-        outf[k][tid] = d0;
-      }
-    }
-    __syncthreads();
-#pragma unroll
-    for (int j = 0; j < ND; ++j) {
+  };
+  // producers: the limited values of chunk c (in outf[buf]) to global memory
+  auto store = [&](int c, int buf) {
+    const int c0 = c * C, cnt = min(C, n - c0);
+    for (int it = ptid; it < cnt * L; it += NP) {
       int l, k;
-      slot_d(j, l, k);
-      if (l < L && l0 + l < nl && k < cnt) {
+      slot(it, cnt, l, k);
+      if (l0 + l < nl) {
         const size_t o = at(l0 + l, c0 + k);
-        d[o] = S.out[k][l];
-        dt[o] = outf[k][l];
+        const float x = outf[buf][k][l];
+        d[o] = mix::f2d(x);
+        dt[o] = x;
       }
+    }
+  };
+  float d0 = sweeper ? mix::d2f(d[at(l0 + tid, 0)]) : 0.f;  // ghost before the first cell
+  if (!sweeper_warp) {
+    fetch(0);
+    prepare(0, 0);
+  }
+  __syncthreads();
+  for (int s = 0; s <= nchunks; ++s) {
+    if (sweeper_warp) {
+      if (s < nchunks && sweeper) {
+        const int cnt = min(C, n - s * C), buf = s & 1;
+        constexpr float a = 281121.0f / 6720.0f, c4 = 0.25f / lw0;
+        for (int k = 0; k < cnt; ++k) {
+          const float ud0 = d0 * dif;
+          const float s0 = fabsf(fmaf(fmaf(a, ud0, pre[buf][0][k][tid]), ud0, pre[buf][1][k][tid]));
+          const float t = fabsf(s0 - pre[buf][2][k][tid]) + fabsf(s0 - pre[buf][3][k][tid]);
+          const float tau = 0.25f * t * t;
+          const float w0 = lw0 * fmaf(tau, __fdividef(1.0f, s0 + eps), 1.0f);
+          const float num = fmaf(w0, fmaf(-c4, d0, pre[buf][4][k][tid]),
+                                 fmaf(tau, pre[buf][7][k][tid], pre[buf][6][k][tid]));
+          const float den = w0 + fmaf(tau, pre[buf][5][k][tid], lw1 + lw2);
+          d0 = __fdividef(num, den);
+          outf[buf][k][tid] = d0;
+        }
+      }
+    } else {
+      if (s + 1 < nchunks) prepare(s + 1, (s + 1) & 1);
+      if (s >= 1) store(s - 1, (s - 1) & 1);
     }
     __syncthreads();
   }
