@@ -16,10 +16,11 @@ value is the sum over ranks divided by the slowest rank's time.
 reference's own sources cannot be built on the GPU host), rank 0 only.
 
 Besides the headline line's plain FP64 value, "paths" reports the other measured workloads:
-the mixed-precision path on the same grid (with its density error against FP64), the
-Hermite-WENO 2048^2 blob/shock case (FP64 and mixed), the 4096^2 learned-routing case (FP64,
-FP32, FP32 + learned classifier, with training and audit figures) and the batch of 256 uneven
-grids.  --no-mixed / --no-hermite / --no-learned / --no-batch skip them.
+the plain FP64 stage as one fused launch on the same timed steps (checked bit for bit against
+the headline run), the mixed-precision path on the same grid (with its density error against
+FP64), the Hermite-WENO 2048^2 blob/shock case (FP64 and mixed), the 4096^2 learned-routing case
+(FP64, FP32, FP32 + learned classifier, with training and audit figures) and the batch of 256
+uneven grids.  --no-fused / --no-mixed / --no-hermite / --no-learned / --no-batch skip them.
 """
 from __future__ import annotations
 
@@ -63,6 +64,7 @@ def parse():
                     help="steps of both Hermite arms (the same window from the initial state)")
     ap.add_argument("--hermite-n", type=int, default=2048, help="grid side of the Hermite 2D path")
     ap.add_argument("--no-learned", action="store_true")
+    ap.add_argument("--no-fused", action="store_true")
     ap.add_argument("--c5-steps", type=int, default=500,
                     help="steps of the 4096^2 learned-routing case: the FP64 arm runs them, the FP32 "
                          "arms run from the same initial state to the FP64 arm's end time")
@@ -271,6 +273,41 @@ def batch_path(hteno, torch, stream, steps, world):
                     "pressure in some RK stage, which the plain FP64 solver (the reference's "
                     "arithmetic bit for bit, no positivity limiter) does on the same seeded data "
                     "within these steps: 14 of the 256, every grid flagged here among them"}
+
+
+def fused_fp64_path(hteno, torch, cfg, stream, start_state, ref_state, steps, value_plain, kernels,
+                    ncell, world):
+    """The plain FP64 stage as one fused launch per stage (hteno_set_fp64_fused, tiles of 32 x 16
+    cells with face values and fluxes in shared memory) on the headline's timed window: the same
+    K steps from the same start state, timed with CUDA events, and its state compared with the
+    five-launch path's bit for bit."""
+    with hteno.Solver(cfg) as s:
+        s.set_stream(stream.cuda_stream)
+        s.set_fp64_fused(True)
+        s.set_state(start_state)
+        s.step_async(steps)  # warm-up over the same steps
+        s.sync()
+        s.set_state(start_state)  # dt follows from the state alone: the timed steps again
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        s.step_async(steps)
+        ev1.record(stream)
+        ev1.synchronize()
+        s.sync()
+        ms = ev0.elapsed_time(ev1)
+        same = bool(np.array_equal(s.get_state(), ref_state))
+        launches = s.launches_per_step()
+    value = ncell * steps * world / (ms / 1e3) / 1e6
+    five = sum(k["bytes_per_launch"] * k["launches"] for k in kernels) / steps / ncell
+    return {"value": value, "unit": UNIT, "ms_per_step": ms / steps, "vs_five_launch": value / value_plain,
+            "same_bits_as_five_launch": same, "launches_per_step": launches,
+            "hbm_bytes_per_cell_update": {"fused": 3 * 193.0, "five_launch": five},
+            "note": "one launch per stage reads the state once (3-cell halo) and writes it once; the "
+                    "tile's halo face rows and columns and its edge fluxes are computed again by the "
+                    "neighbouring tiles (+12.6 % FP64 instructions, measured), and the FP64-bound "
+                    "stage pays for that: the five-launch path stays the default"}
 
 
 def kernel_shares(hteno, solver, steps):
@@ -719,6 +756,9 @@ def run_gpu(args):
     # workload, advanced to the same time as the plain path; density error against the plain
     # FP64 state, which is bit-identical to the CPU oracle
     paths = {}
+    if not args.no_fused:
+        paths["fp64_fused"] = fused_fp64_path(hteno, torch, cfg, stream, start_state, ref_state,
+                                              args.steps, value, kernels, ncell, world)
     if not args.no_mixed:
         paths["fp32_mixed"] = mixed_path(hteno, torch, q, stream, args, t_plain, ref_state, ms_max, world)
     if not args.no_sod and rank == 0:

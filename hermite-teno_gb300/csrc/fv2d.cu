@@ -3,7 +3,8 @@
 // Rusanov at the Gauss points, SSP-RK3.  Host dispatch of the two precisions:
 //
 //   plain FP64 (fv2d_fp64.cu): bit-reproducible; 5 launches per stage (faces x/y, flux x/y,
-//     update) through per-face work arrays;
+//     update) through per-face work arrays, or one fused launch per stage over 32 x 32 tiles
+//     (hteno_set_fp64_fused, the same bits);
 //   mixed (fv2d_fused.cu): reconstruction and fluxes in float, state and RK accumulation in
 //     double; one fused launch per stage over tiles held in shared memory.
 //
@@ -51,7 +52,8 @@ int fv2d_step_async(hteno_solver* s, int nsteps) {
       fv2d_fused_step(s, G, static_cast<double*>(s->work));
     } else {
       const Work<double> W = carve<double>(s->work, G.nx, G.ny);
-      for (int stage = 1; stage <= 3; ++stage) fv2d_fp64_stage(s, G, W, stage, s->q, nullptr);
+      if (s->fused64) fv2d_fp64_fused_step(s, G, W);
+      else for (int stage = 1; stage <= 3; ++stage) fv2d_fp64_stage(s, G, W, stage, s->q, nullptr);
     }
     k_end_step<<<1, 1, 0, s->stream>>>(s->dstate);
   }

@@ -512,6 +512,274 @@ __global__ void kp_update(Geo G, int stage, const double* __restrict__ fx,
   if (bad && st) atomicOr(&st->status, bad);
 }
 
+// ---- one fused launch per stage (hteno_set_fp64_fused) -------------------------------------------
+// The five launches of a stage (uniform test, faces x/y, fluxes x/y, update) as one kernel over
+// tiles of TX x TY cells, face values and fluxes in shared memory, the same arithmetic in the same
+// order as the launches above (the same bits).  Per tile: (A) the state with a 3-cell halo; (B) the
+// uniform cells of the tile (kp_deep's test); (C) the x face values of rows -2 .. TY+1 that the x
+// fluxes of non-uniform cells read, (D) those x fluxes, (E) their difference times dy per cell;
+// (F, G) the same for y; (H) the residual and the SSP-RK3 stage.  The Roe average of a face is
+// computed again for its flux rather than kept, and 32 x 16 tiles (104 KB of shared memory) let two
+// tiles share an SM, so that one tile's phases fill the other's barrier waits.  Stage buffers: a stage reads its input state and primitives with halos from
+// qin / pin, the step-start state pointwise from qbase, and writes qout / pout; stage 3 writes the
+// state in place over the step-start copy, which only the owning thread reads.  Zero-gradient and
+// periodic boundaries (the halo is mapped as every stencil maps it).
+constexpr int kS64X = 32, kS64Y = 16, kS64Threads = 256;  // two tiles per SM
+
+template <int TX, int TY>
+struct S64Smem {
+  static constexpr int C = (TY + 4) * (TX + 1) > (TY + 1) * (TX + 4) ? (TY + 4) * (TX + 1)
+                                                                      : (TY + 1) * (TX + 4);
+  static constexpr int F = (TY + 1) * (TX + 1);
+  double q[4][TY + 6][TX + 6];
+  double c[8][C];   // face values of one direction (x: rows -2 .. TY+1 x TX+1; y: TY+1 x columns -2 .. TX+1)
+  double f[4][F];   // fluxes of one direction
+  double rx[4][TY][TX];  // (fx_i - fx_i+1) * dy of each cell
+  unsigned char deep[TY][TX];
+  unsigned char fneed[F];
+};
+
+template <int TX, int TY, int NT>
+__global__ void __launch_bounds__(NT, 2) kp_stage64(Geo G, int stage, const double* __restrict__ qin,
+                                                  const double* qbase, double* qout,
+                                                  const double* __restrict__ pin,
+                                                  double* __restrict__ pout, StepState* st,
+                                                  int skip_uniform) {
+  if (st->done) return;
+  extern __shared__ __align__(16) unsigned char s64raw[];
+  S64Smem<TX, TY>& S = *reinterpret_cast<S64Smem<TX, TY>*>(s64raw);
+  constexpr int XF = TX + 1, YC = TX + 4;
+  const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY;
+  const int wx = min(TX, G.nx - i0), wy = min(TY, G.ny - j0);
+  const size_t nc = size_t(G.nx) * G.ny;
+  const int tid = threadIdx.x;
+  auto row = [&](int j) { return cmap_any(j0 + j, G.ny, G.bc); };
+  auto col = [&](int i) { return cmap_any(i0 + i, G.nx, G.bc); };
+  // A: state tile, halo 3
+  for (int it = tid; it < (TY + 6) * (TX + 6); it += NT) {
+    const int y = it / (TX + 6), x = it - y * (TX + 6);
+    const size_t k = size_t(row(y - 3)) * G.nx + col(x - 3);
+#pragma unroll
+    for (int v = 0; v < 4; ++v) S.q[v][y][x] = qin[v * nc + k];
+  }
+  __syncthreads();
+  // B: uniform cells (kp_deep)
+  int nd = 0;
+  for (int it = tid; it < TY * TX; it += NT) {
+    const int ty = it / TX, tx = it - ty * TX;
+    bool u = false;
+    if (skip_uniform && ty < wy && tx < wx) {
+      const double qc[4] = {S.q[0][ty + 3][tx + 3], S.q[1][ty + 3][tx + 3], S.q[2][ty + 3][tx + 3],
+                            S.q[3][ty + 3][tx + 3]};
+      double w[4];
+      par::primitive(G.g1, qc, w);
+      constexpr double lo = 0x1p-64, hi = 0x1p64;
+      u = w[0] >= lo && w[0] <= hi && w[3] >= lo && w[3] <= hi &&
+          w[1] * w[1] + w[2] * w[2] <= 64.0 * (G.gamma * w[3] / w[0]);
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        const long long c = __double_as_longlong(qc[v]);
+        for (int dy = 0; dy < 7; ++dy)
+#pragma unroll
+          for (int dx = 0; dx < 7; ++dx) u &= __double_as_longlong(S.q[v][ty + dy][tx + dx]) == c;
+      }
+    }
+    S.deep[ty][tx] = u ? 1 : 0;
+    nd += u ? 1 : 0;
+  }
+  const int n1 = __syncthreads_count(nd >= 1), n2 = __syncthreads_count(nd >= 2);
+  if (tid == 0 && n1 + n2) atomicAdd(&st->uniform, (unsigned long long)(n1 + n2));
+  const bool all_uniform = n1 + n2 == wx * wy;
+  if (!all_uniform) {
+    // ---- x faces: flux (t, f) is needed when a non-uniform cell of the tile reads it
+    for (int it = tid; it < TY * XF; it += NT) {
+      const int t = it / XF, f = it - t * XF;
+      S.fneed[it] = t < wy && f <= wx &&
+                    ((f >= 1 && !S.deep[t][f - 1]) || (f < wx && !S.deep[t][f]));
+    }
+    __syncthreads();
+    // C: x face values of rows -2 .. wy + 1 (kp_faces<1>)
+    for (int it = tid; it < (TY + 4) * XF; it += NT) {
+      const int r = it / XF - 2, f = it - (r + 2) * XF;
+      if (r > wy + 1 || f > wx) continue;
+      bool need = false;
+#pragma unroll
+      for (int m = -2; m <= 2; ++m) {
+        const int t = r + m;
+        need |= t >= 0 && t < wy && S.fneed[t * XF + f];
+      }
+      if (!need) continue;
+      const size_t ca = size_t(row(r)) * G.nx + col(f - 1), cb = size_t(row(r)) * G.nx + col(f);
+      const par::Eig E = par::eig(G.g1, 1, pin[3 * nc + ca], pin[ca], pin[nc + ca], pin[2 * nc + ca],
+                                  pin[3 * nc + cb], pin[cb], pin[nc + cb], pin[2 * nc + cb]);
+      double ch[4][6];
+#pragma unroll
+      for (int m = 0; m < 6; ++m) {
+        const double qq[4] = {S.q[0][r + 3][f + m], S.q[1][r + 3][f + m], S.q[2][r + 3][f + m],
+                              S.q[3][r + 3][f + m]};
+        double cc[4];
+        par::left(E, 1, qq, cc);
+#pragma unroll
+        for (int a = 0; a < 4; ++a) ch[a][m] = cc[a];
+      }
+#pragma unroll
+      for (int a = 0; a < 4; ++a) {
+        double lo, hi;
+        par::lagrange_recon(c_dev, G.recon, ch[a], lo, hi);
+        S.c[a][it] = lo;
+        S.c[4 + a][it] = hi;
+      }
+    }
+    __syncthreads();
+    // D: x fluxes (kp_flux<1>)
+    for (int it = tid; it < TY * XF; it += NT) {
+      if (!S.fneed[it]) continue;
+      const int t = it / XF, f = it - t * XF;
+      double g[8][3];
+#pragma unroll
+      for (int a = 0; a < 8; ++a) {
+        double u5[5];
+#pragma unroll
+        for (int m = 0; m < 5; ++m) u5[m] = S.c[a][(t + m) * XF + f];
+        par::gl3(c_dev, u5, g[a]);
+      }
+      const size_t ca = size_t(row(t)) * G.nx + col(f - 1), cb = size_t(row(t)) * G.nx + col(f);
+      const par::Eig E = par::eig(G.g1, 1, pin[3 * nc + ca], pin[ca], pin[nc + ca], pin[2 * nc + ca],
+                                  pin[3 * nc + cb], pin[cb], pin[nc + cb], pin[2 * nc + cb]);
+      double Fm[3][4];
+#pragma unroll
+      for (int m = 0; m < 3; ++m) {
+        const double cl[4] = {g[0][m], g[1][m], g[2][m], g[3][m]};
+        const double cr[4] = {g[4][m], g[5][m], g[6][m], g[7][m]};
+        double ql[4], qr[4], Fl[4];
+        par::right(E, 1, cl, ql);
+        par::right(E, 1, cr, qr);
+        if (G.flux == HTENO_FLUX_HLLC) par::hllc(G.g1, 1, ql, qr, Fl);
+        else par::rusanov(G.gamma, G.g1, 1, E, ql, qr, Fl);
+#pragma unroll
+        for (int v = 0; v < 4; ++v) Fm[m][v] = c_dev.gl3w[m] * Fl[v];
+      }
+#pragma unroll
+      for (int v = 0; v < 4; ++v) S.f[v][it] = (Fm[0][v] + Fm[1][v]) + Fm[2][v];
+    }
+    __syncthreads();
+    // E: x flux difference times dy of each non-uniform cell (kp_update's first term)
+    for (int it = tid; it < TY * TX; it += NT) {
+      const int t = it / TX, i = it - t * TX;
+      if (t < wy && i < wx && !S.deep[t][i]) {
+#pragma unroll
+        for (int v = 0; v < 4; ++v) S.rx[v][t][i] = (S.f[v][t * XF + i] - S.f[v][t * XF + i + 1]) * G.dy;
+      }
+    }
+    // ---- y faces: flux (g, t) of face row g (between cell rows g - 1 and g), column t
+    for (int it = tid; it < (TY + 1) * TX; it += NT) {
+      const int g = it / TX, t = it - g * TX;
+      S.fneed[it] = g <= wy && t < wx &&
+                    ((g >= 1 && !S.deep[g - 1][t]) || (g < wy && !S.deep[g][t]));
+    }
+    __syncthreads();
+    // F: y face values of columns -2 .. wx + 1 (kp_faces<2>)
+    for (int it = tid; it < (TY + 1) * YC; it += NT) {
+      const int g = it / YC, cc = it - g * YC - 2;
+      if (g > wy || cc > wx + 1) continue;
+      bool need = false;
+#pragma unroll
+      for (int m = -2; m <= 2; ++m) {
+        const int t = cc + m;
+        need |= t >= 0 && t < wx && S.fneed[g * TX + t];
+      }
+      if (!need) continue;
+      const size_t ca = size_t(row(g - 1)) * G.nx + col(cc), cb = size_t(row(g)) * G.nx + col(cc);
+      const par::Eig E = par::eig(G.g1, 2, pin[3 * nc + ca], pin[ca], pin[nc + ca], pin[2 * nc + ca],
+                                  pin[3 * nc + cb], pin[cb], pin[nc + cb], pin[2 * nc + cb]);
+      double ch[4][6];
+#pragma unroll
+      for (int m = 0; m < 6; ++m) {
+        const double qq[4] = {S.q[0][g + m][cc + 3], S.q[1][g + m][cc + 3], S.q[2][g + m][cc + 3],
+                              S.q[3][g + m][cc + 3]};
+        double c4[4];
+        par::left(E, 2, qq, c4);
+#pragma unroll
+        for (int a = 0; a < 4; ++a) ch[a][m] = c4[a];
+      }
+#pragma unroll
+      for (int a = 0; a < 4; ++a) {
+        double lo, hi;
+        par::lagrange_recon(c_dev, G.recon, ch[a], lo, hi);
+        S.c[a][it] = lo;
+        S.c[4 + a][it] = hi;
+      }
+    }
+    __syncthreads();
+    // G: y fluxes (kp_flux<2>)
+    for (int it = tid; it < (TY + 1) * TX; it += NT) {
+      if (!S.fneed[it]) continue;
+      const int g = it / TX, t = it - g * TX;
+      double gg[8][3];
+#pragma unroll
+      for (int a = 0; a < 8; ++a) {
+        double u5[5];
+#pragma unroll
+        for (int m = 0; m < 5; ++m) u5[m] = S.c[a][g * YC + t + m];
+        par::gl3(c_dev, u5, gg[a]);
+      }
+      const size_t ca = size_t(row(g - 1)) * G.nx + col(t), cb = size_t(row(g)) * G.nx + col(t);
+      const par::Eig E = par::eig(G.g1, 2, pin[3 * nc + ca], pin[ca], pin[nc + ca], pin[2 * nc + ca],
+                                  pin[3 * nc + cb], pin[cb], pin[nc + cb], pin[2 * nc + cb]);
+      double Fm[3][4];
+#pragma unroll
+      for (int m = 0; m < 3; ++m) {
+        const double cl[4] = {gg[0][m], gg[1][m], gg[2][m], gg[3][m]};
+        const double cr[4] = {gg[4][m], gg[5][m], gg[6][m], gg[7][m]};
+        double ql[4], qr[4], Fl[4];
+        par::right(E, 2, cl, ql);
+        par::right(E, 2, cr, qr);
+        if (G.flux == HTENO_FLUX_HLLC) par::hllc(G.g1, 2, ql, qr, Fl);
+        else par::rusanov(G.gamma, G.g1, 2, E, ql, qr, Fl);
+#pragma unroll
+        for (int v = 0; v < 4; ++v) Fm[m][v] = c_dev.gl3w[m] * Fl[v];
+      }
+#pragma unroll
+      for (int v = 0; v < 4; ++v) S.f[v][it] = (Fm[0][v] + Fm[1][v]) + Fm[2][v];
+    }
+    __syncthreads();
+  }
+  // H: residual and SSP-RK3 stage (kp_update)
+  double ms = 0.0;
+  int bad = 0;
+  const double dt = st->dt;
+  for (int it = tid; it < TY * TX; it += NT) {
+    const int t = it / TX, i = it - t * TX;
+    if (t >= wy || i >= wx) continue;
+    const size_t k = size_t(j0 + t) * G.nx + (i0 + i);
+    double rhs[4] = {0.0, 0.0, 0.0, 0.0};  // a uniform cell's flux pairs are equal: residual +0
+    if (!S.deep[t][i]) {
+#pragma unroll
+      for (int v = 0; v < 4; ++v)
+        rhs[v] = (S.rx[v][t][i] + (S.f[v][t * TX + i] - S.f[v][(t + 1) * TX + i]) * G.dx) / G.area + 0.0;
+    }
+    double qn[4];
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      const double cur = S.q[v][t + 3][i + 3];
+      const double base = stage == 1 ? cur : qbase[v * nc + k];
+      qn[v] = ssprk3(base, cur, rhs[v], dt, stage);
+      qout[v * nc + k] = qn[v];
+    }
+    double w[4], h, sr;
+    cell_prim(G.g1, qn, w, h, sr);
+    pout[k] = w[1];
+    pout[nc + k] = w[2];
+    pout[2 * nc + k] = h;
+    pout[3 * nc + k] = sr;
+    if (stage == 3) ms = fmax(ms, par::max_speed2(G.gamma, w));
+    bad |= (isnan(qn[0]) || isnan(qn[1]) || isnan(qn[2]) || isnan(qn[3])) ? 1 : 0;
+    bad |= (qn[0] <= 0.0 || w[3] <= 0.0) ? 2 : 0;
+  }
+  if (stage == 3) block_max_to(ms, &st->maxbits);
+  if (bad) atomicOr(&st->status, bad);
+}
+
 }  // namespace
 
 int fv2d_fp64_setup(hteno_solver* s) {
@@ -527,6 +795,54 @@ int fv2d_fp64_setup(hteno_solver* s) {
     if (e != cudaSuccess) return cuda_error(s, e, "ghost face rows");
   }
   return HTENO_OK;
+}
+
+int fv2d_fp64_set_fused(hteno_solver* s, int on) {
+  if (!on) {
+    cudaFree(s->fused64);
+    s->fused64 = nullptr;
+    s->launches_per_step = 2 + 3 * 5;
+    return HTENO_OK;
+  }
+  if (!s->fused64) {
+    cudaError_t e = cudaFuncSetAttribute(kp_stage64<kS64X, kS64Y, kS64Threads>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         int(sizeof(S64Smem<kS64X, kS64Y>)));
+    if (e != cudaSuccess) return cuda_error(s, e, "fused stage shared memory");
+    e = cudaMalloc(&s->fused64, 16 * s->ncell * sizeof(double));
+    if (e != cudaSuccess) return cuda_error(s, e, "fused stage buffers");
+  }
+  s->launches_per_step = 2 + 3;
+  return HTENO_OK;
+}
+
+void fv2d_fp64_fused_step(hteno_solver* s, const Geo& G, const Work<double>& W) {
+  cudaStream_t cs = s->stream;
+  const size_t nc = size_t(G.nx) * G.ny;
+  const long nxf = long(G.nx + 1) * G.ny, nyf = long(G.ny + 1) * G.nx;
+  const double ncd = double(nc);
+  const double fluxf = G.flux == HTENO_FLUX_HLLC ? kFluxFlopsHllc : kFluxFlopsRusanov;
+  // algorithmic bytes per cell: state with halo (38 x 22 / 32 x 16), step-start state, new state
+  // and its primitives written, the Roe cells' primitives with their halo (36 x 20 / 32 x 16)
+  const int kind = trace_kind(s, "stage", ncd * 193.0,
+                              (kFacesFlops + fluxf) * double(nxf + nyf) + kUpdateFlops * ncd);
+  double* q1 = s->fused64;
+  double* q2 = q1 + 4 * nc;
+  double* p1 = q2 + 4 * nc;
+  double* p2 = p1 + 4 * nc;
+  const dim3 grid(unsigned((G.nx + kS64X - 1) / kS64X), unsigned((G.ny + kS64Y - 1) / kS64Y));
+  const size_t smem = sizeof(S64Smem<kS64X, kS64Y>);
+  const int skip = s->uniform_skip ? 1 : 0;
+  const double* qin[3] = {s->q, q1, q2};
+  double* qout[3] = {q1, q2, s->q};
+  const double* pin[3] = {W.prim, p1, p2};
+  double* pout[3] = {p1, p2, W.prim};
+  for (int stage = 1; stage <= 3; ++stage) {
+    trace_begin(s, kind);
+    kp_stage64<kS64X, kS64Y, kS64Threads><<<grid, kS64Threads, smem, cs>>>(G, stage, qin[stage - 1], s->q, qout[stage - 1],
+                                                pin[stage - 1], pout[stage - 1], s->dstate, skip);
+    trace_end(s);
+  }
 }
 
 void fv2d_fp64_prim(hteno_solver* s, const Geo& G, const Work<double>& W, const double* q,

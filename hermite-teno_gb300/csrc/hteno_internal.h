@@ -81,6 +81,7 @@ struct hteno_solver {
   uint8_t* deep = nullptr;  // plain FV 2D: cells of uniform 7 x 7 neighbourhoods (per stage)
   bool uniform_skip = true;  // FV 2D: uniform regions take their exactly zero residual directly
   double* ghost_faces = nullptr;  // plain FV 2D with HTENO_BC_TAYLOR / _DOUBLE_MACH: ghost face rows
+  double* fused64 = nullptr;  // plain FV 2D in fused stages: q1, q2 and their primitives [4][4][ncell]
   cudaGraphExec_t step_graph = nullptr;  // 1D schemes: a run of steps replayed as one graph
   // learned routing (mixed FV 2D): classifier, threshold, audit period, masks, audit sums
   hteno_mlp* router = nullptr;
@@ -127,6 +128,7 @@ int fv2d_setup(hteno_solver* s);
 int fv2d_prepare(hteno_solver* s);  // after set_state: primitives of the new state
 int fv2d_step_async(hteno_solver* s, int nsteps);
 int fv2d_residual(hteno_solver* s, const double* q, double* rhs);
+int fv2d_fp64_set_fused(hteno_solver* s, int on);  // plain FV 2D: one launch per stage
 
 int fv1d_setup(hteno_solver* s);
 int fv1d_prepare(hteno_solver* s);

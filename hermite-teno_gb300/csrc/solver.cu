@@ -109,6 +109,7 @@ void release(hteno_solver* s) {
   cudaFree(s->route_rows);
   cudaFree(s->deep);
   cudaFree(s->ghost_faces);
+  cudaFree(s->fused64);
   cudaFree(s->q);
   cudaFree(s->q0);
   cudaFree(s->v);
@@ -383,6 +384,16 @@ int hteno_set_strict(hteno_solver* s, int on) {
   if (!s) return HTENO_ERR_INVALID_ARG;
   s->strict = on != 0;
   return HTENO_OK;
+}
+
+int hteno_set_fp64_fused(hteno_solver* s, int on) {
+  if (!s) return HTENO_ERR_INVALID_ARG;
+  const hteno_config& c = s->cfg;
+  if (c.dims != 2 || c.scheme != HTENO_SCHEME_FV || c.precision != HTENO_PREC_FP64 ||
+      c.bc > HTENO_BC_PERIODIC)
+    return set_error(s, HTENO_ERR_UNSUPPORTED,
+                     "fused stages: plain FP64 FV 2D with zero-gradient or periodic boundaries");
+  return fv2d_fp64_set_fused(s, on);
 }
 
 int hteno_launches_per_step(hteno_solver* s, int* launches) {

@@ -95,6 +95,7 @@ def lib() -> ctypes.CDLL:
         L.hteno_measure_fma_peak.argtypes = [i, _D]
         L.hteno_get_status.argtypes = [vp, ctypes.POINTER(i)]
         L.hteno_set_strict.argtypes = [vp, i]
+        L.hteno_set_fp64_fused.argtypes = [vp, i]
         L.hteno_get_counters.argtypes = [vp, ctypes.POINTER(ctypes.c_longlong)]
         L.hteno_residual_noalloc.argtypes = [ctypes.POINTER(Config), vp, vp, vp]
         L.hteno_batch_create.argtypes = [ctypes.POINTER(Config), i, ctypes.POINTER(vp)]
@@ -240,6 +241,10 @@ class Solver:
 
     def set_strict(self, on: bool = True) -> None:
         _check(lib().hteno_set_strict(self.h, int(bool(on))), self.h)
+
+    def set_fp64_fused(self, on: bool = True) -> None:
+        """Plain FP64 FV 2D stepping as one fused launch per stage (the same bits)."""
+        _check(lib().hteno_set_fp64_fused(self.h, int(bool(on))), self.h)
 
     def launches_per_step(self) -> int:
         n = ctypes.c_int()

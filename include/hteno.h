@@ -138,6 +138,14 @@ int hteno_launches_per_step(hteno_solver* s, int* launches);
 int hteno_get_status(hteno_solver* s, int* flags);
 int hteno_set_strict(hteno_solver* s, int on);
 
+/* Plain FP64 FV 2D stepping as one fused launch per stage (on = 1) instead of five (uniform-region
+ * test, faces x/y, fluxes x/y, update; on = 0, the default): tiles of 32 x 16 cells with their
+ * face values and fluxes in shared memory, so a stage reads the state once (with a 3-cell halo)
+ * and writes it once.  The same arithmetic in the same order: the same bits as the default path
+ * (FV_System2D.cpp:363-612, a stage of timeStepping).  Zero-gradient and periodic boundaries;
+ * other configurations return HTENO_ERR_UNSUPPORTED.  Holds 4 more state-sized buffers while on. */
+int hteno_set_fp64_fused(hteno_solver* s, int on);
+
 /* Work counters since the last hteno_set_state (FV 2D stepping), a measurement aid with no
  * reference counterpart (the reference computes every face):
  *   counters[0]: cell-stages whose residual was taken as exactly zero without computing their

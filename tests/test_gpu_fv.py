@@ -394,3 +394,68 @@ def test_fv2d_4096_matches_oracle(hteno_lib, cuda, oracle):
     assert n_g == n_o == 3 and t_g == t_o
     assert rel_linf(got, want) <= TOL
     np.testing.assert_array_equal(got, want)
+
+
+def gpu_run2d_fused(h, q, nsteps, fused, t_final=1e30, **kw):
+    cfg = h.config(dims=2, nx=q.shape[2], ny=q.shape[1], **kw)
+    with h.Solver(cfg) as s:
+        if fused:
+            s.set_fp64_fused(True)
+        s.set_state(q)
+        s.step(nsteps, t_final)
+        t, n, _ = s.time()
+        return s.get_state(), t, n, s.counters()["uniform_cells"], s.launches_per_step()
+
+
+@pytest.mark.parametrize("case", [
+    ((96, 80), 40, dict(flux=1, recon=0, bc=0)),    # TENO5 + HLLC, partial tiles
+    ((64, 64), 30, dict(flux=0, recon=1, bc=1)),    # teno5i + Rusanov, periodic
+    ((100, 37), 30, dict(flux=1, recon=4, bc=0)),   # WENO-Z, both edges partial
+    ((40, 150), 30, dict(flux=1, recon=2, bc=1)),   # linear weights, periodic, tall
+    ((12, 9), 20, dict(flux=1, recon=0, bc=1)),     # a grid smaller than one tile, periodic
+], ids=["teno5-hllc", "teno5i-periodic", "wenoz", "linear-periodic", "tiny-periodic"])
+def test_fp64_fused_stage_same_bits(hteno_lib, cuda, case):
+    """One fused launch per stage gives the five-launch path's state bit for bit, with the same
+    time, step count and uniform-cell count, in three launches per step."""
+    from hteno import ic
+
+    (nx, ny), steps, kw = case
+    q = ic.four_quadrant(nx, ny, 11)
+    a, ta, na, ua, la = gpu_run2d_fused(hteno_lib, q, steps, False, **kw)
+    b, tb, nb, ub, lb = gpu_run2d_fused(hteno_lib, q, steps, True, **kw)
+    np.testing.assert_array_equal(a, b)
+    assert (ta, na, ua) == (tb, nb, ub) and la == 17 and lb == 5
+
+
+def test_fp64_fused_matches_oracle(hteno_lib, cuda, oracle):
+    """The fused stage against the CPU oracle directly (TENO5 + HLLC, 96 x 80, 40 steps)."""
+    from hteno import ic
+
+    q = ic.four_quadrant(96, 80, 3)
+    got, t, n, _, _ = gpu_run2d_fused(hteno_lib, q, 40, True, flux=1, recon=0, bc=0)
+    want, t_o, n_o = oracle.fv2d_run(q, 40, flux=1, recon=0, bc=0)
+    assert n == n_o == 40 and t == t_o
+    assert rel_linf(got, want) <= TOL
+    np.testing.assert_array_equal(got, want)
+
+
+def test_fp64_fused_full_size_same_bits(hteno_lib, cuda):
+    """The headline configuration at its stated size (1024^2 four-quadrant, TENO5 + HLLC, 200
+    steps): the fused stage equals the five-launch path bit for bit (which the full-size test
+    above pins to the oracle)."""
+    from hteno import ic
+
+    q = ic.four_quadrant(1024, 1024, 0)
+    a, ta, na, ua, _ = gpu_run2d_fused(hteno_lib, q, 200, False, flux=1, recon=0, bc=0)
+    b, tb, nb, ub, _ = gpu_run2d_fused(hteno_lib, q, 200, True, flux=1, recon=0, bc=0)
+    assert (ta, na, ua) == (tb, nb, ub)
+    np.testing.assert_array_equal(a, b)
+
+
+def test_fp64_fused_rejects_other_configurations(hteno_lib, cuda):
+    h = hteno_lib
+    for kw in (dict(bc=2), dict(bc=3), dict(precision=1)):
+        with h.Solver(h.config(dims=2, nx=32, ny=32, **kw)) as s:
+            with pytest.raises(h.HtenoError) as e:
+                s.set_fp64_fused(True)
+            assert e.value.code == 7  # HTENO_ERR_UNSUPPORTED
