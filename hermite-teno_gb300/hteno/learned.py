@@ -12,8 +12,11 @@ from . import ic
 
 
 def harvest_runs(h, torch, seeds, n=1024, snapshots=(0, 20, 40), keep=0.2, capacity=None,
-                 sod_snapshots=(0, 50, 100, 150), device="cuda"):
-    """Returns (x int16 [N, 8] BF16 bits, y uint8 [N]) CUDA tensors, shuffled."""
+                 sod_snapshots=(0, 50, 100, 150), device="cuda", shuffle_seed=0):
+    """Returns (x int16 [N, 8] BF16 bits, y uint8 [N]) CUDA tensors, shuffled.  The harvest kernels
+    append rows in whatever order their threads finish, so the rows are first put in a canonical
+    order (sorted by their bits) and then shuffled by a seeded permutation: the same runs give the
+    same rows in the same order, and (training being deterministic) the same network."""
     per_2d = (2 * (n + 1) * n) * 8
     if capacity is None:
         capacity = int(len(seeds) * len(snapshots) * per_2d * keep * 1.05) + 8 * 401 * 6 * len(sod_snapshots)
@@ -40,8 +43,15 @@ def harvest_runs(h, torch, seeds, n=1024, snapshots=(0, 20, 40), keep=0.2, capac
             done = snap
             got = s.harvest(1.0, 77 + snap, x[off:], y[off:])
             off = min(capacity, off + got)
-    perm = torch.randperm(off, device=device)
-    return x[:off][perm].contiguous(), y[:off][perm].contiguous()
+    x, y = x[:off].contiguous(), y[:off].contiguous()
+    order = torch.sort(y.to(torch.int64), stable=True).indices  # least significant key first
+    keys = x.view(torch.int64)  # the 8 BF16 values of a row as two 64-bit keys
+    for k in (1, 0):
+        order = order[torch.sort(keys[order, k], stable=True).indices]
+    gen = torch.Generator(device=device)
+    gen.manual_seed(shuffle_seed)
+    perm = order[torch.randperm(off, generator=gen, device=device)]
+    return x[perm].contiguous(), y[perm].contiguous()
 
 
 def label_stats(y):

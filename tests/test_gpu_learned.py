@@ -86,6 +86,25 @@ def test_harvest_1d(hteno_lib, cuda):
     assert (ya == 7).any() and (ya != 7).any()
 
 
+def test_harvest_and_training_reproducible(hteno_lib, cuda):
+    """The whole learned pipeline is reproducible: the harvest kernels append rows in thread
+    order, harvest_runs puts them in a canonical order before its seeded shuffle, and training is
+    deterministic, so two runs give the same rows and the same network bit for bit."""
+    from hteno import learned
+
+    h = hteno_lib
+    nets = []
+    for _ in range(2):
+        x, y = learned.harvest_runs(h, cuda, seeds=[7], n=128, snapshots=(0, 10), keep=0.5,
+                                    sod_snapshots=(0, 50))
+        with h.Mlp(seed=3) as m:
+            m.train(x, y, epochs=2, batch=4096, lr=3e-3)
+            nets.append((x.cpu().numpy(), y.cpu().numpy(), m.params().copy()))
+    np.testing.assert_array_equal(nets[0][0], nets[1][0])
+    np.testing.assert_array_equal(nets[0][1], nets[1][1])
+    np.testing.assert_array_equal(nets[0][2], nets[1][2])
+
+
 def constant_classifier(h, logit):
     m = h.Mlp()
     p = np.zeros(m.nparams, dtype=np.float32)
