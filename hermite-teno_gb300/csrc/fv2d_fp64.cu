@@ -789,6 +789,12 @@ int fv2d_fp64_setup(hteno_solver* s) {
     const cudaError_t e = cudaMalloc(&s->deep, size_t(s->cfg.nx) * s->cfg.ny);
     if (e != cudaSuccess) return cuda_error(s, e, "uniform-region flags");
   }
+  if (s->cfg.precision == HTENO_PREC_FP64 && s->side && !s->side_stream) {
+    cudaError_t e = cudaStreamCreateWithFlags(&s->side_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->fork_ev, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->join_ev, cudaEventDisableTiming);
+    if (e != cudaSuccess) return cuda_error(s, e, "side stream");
+  }
   if (s->cfg.precision == HTENO_PREC_FP64 && s->cfg.bc >= HTENO_BC_TAYLOR && !s->ghost_faces) {
     const size_t n = size_t(32) * (s->cfg.nx + 1) + size_t(32) * (s->cfg.ny + 1);
     const cudaError_t e = cudaMalloc(&s->ghost_faces, n * sizeof(double));
@@ -875,6 +881,15 @@ void fv2d_fp64_stage(hteno_solver* s, const Geo& G, const Work<double>& W, int s
   // ghost face rows of the x faces ([4][8][nx + 1]) and of the y faces ([4][8][ny + 1])
   double* gx = s->ghost_faces;
   double* gy = gx ? gx + size_t(32) * (nx + 1) : nullptr;
+  // the y-direction kernels touch none of the x-direction kernels' outputs: while stepping they
+  // run on the side stream beside them, so that each kernel's last, partly filled wave of
+  // blocks overlaps the other direction's work (one stream while kernels are being timed)
+  const bool fork = stage > 0 && s->side_stream && !s->timing;
+  cudaStream_t ys = fork ? s->side_stream : cs;
+  if (fork) {
+    cudaEventRecord(s->fork_ev, cs);
+    cudaStreamWaitEvent(ys, s->fork_ev, 0);
+  }
   trace_begin(s, kf_x);
   if (gx) {
     const long n = long(nx + 1) * (ny + 4);
@@ -888,10 +903,10 @@ void fv2d_fp64_stage(hteno_solver* s, const Geo& G, const Work<double>& W, int s
   trace_begin(s, kf_y);
   if (gy) {
     const long n = long(ny + 1) * (nx + 4);
-    kp_faces_g<2><<<unsigned((n + kFaceThreads - 1) / kFaceThreads), kFaceThreads, 0, cs>>>(
+    kp_faces_g<2><<<unsigned((n + kFaceThreads - 1) / kFaceThreads), kFaceThreads, 0, ys>>>(
         G, q, W.yc, W.yroe, gy, st, deep);
   } else {
-    kp_faces<2><<<unsigned((nyf + kFaceThreads - 1) / kFaceThreads), kFaceThreads, 0, cs>>>(
+    kp_faces<2><<<unsigned((nyf + kFaceThreads - 1) / kFaceThreads), kFaceThreads, 0, ys>>>(
         G, q, W.prim, W.yc, W.yroe, st, deep);
   }
   trace_end(s);
@@ -900,9 +915,13 @@ void fv2d_fp64_stage(hteno_solver* s, const Geo& G, const Work<double>& W, int s
       G, W.xc, W.xroe, W.fx, st, deep, gx);
   trace_end(s);
   trace_begin(s, ky);
-  kp_flux<2><<<unsigned((nyf + kFaceThreads - 1) / kFaceThreads), kFaceThreads, 0, cs>>>(
+  kp_flux<2><<<unsigned((nyf + kFaceThreads - 1) / kFaceThreads), kFaceThreads, 0, ys>>>(
       G, W.yc, W.yroe, W.fy, st, deep, gy);
   trace_end(s);
+  if (fork) {
+    cudaEventRecord(s->join_ev, ys);
+    cudaStreamWaitEvent(cs, s->join_ev, 0);
+  }
   const size_t nc = size_t(nx) * ny;
   trace_begin(s, ku);
   kp_update<<<unsigned((nc + 255) / 256), 256, 0, cs>>>(G, stage, W.fx, W.fy, s->q, s->q0,

@@ -82,6 +82,11 @@ struct hteno_solver {
   bool uniform_skip = true;  // FV 2D: uniform regions take their exactly zero residual directly
   double* ghost_faces = nullptr;  // plain FV 2D with HTENO_BC_TAYLOR / _DOUBLE_MACH: ghost face rows
   double* fused64 = nullptr;  // plain FV 2D in fused stages: q1, q2 and their primitives [4][4][ncell]
+  // plain FV 2D: the y-direction face and flux kernels run on side_stream beside the x-direction
+  // ones (forked after the uniform test, joined before the update); side = false keeps one stream
+  cudaStream_t side_stream = nullptr;
+  cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
+  bool side = true;
   cudaGraphExec_t step_graph = nullptr;  // 1D schemes: a run of steps replayed as one graph
   // learned routing (mixed FV 2D): classifier, threshold, audit period, masks, audit sums
   hteno_mlp* router = nullptr;

@@ -120,6 +120,9 @@ void release(hteno_solver* s) {
   cudaFree(s->dstate);
   if (s->hstate) cudaFreeHost(s->hstate);
   for (cudaEvent_t e : s->ev) cudaEventDestroy(e);
+  if (s->fork_ev) cudaEventDestroy(s->fork_ev);
+  if (s->join_ev) cudaEventDestroy(s->join_ev);
+  if (s->side_stream) cudaStreamDestroy(s->side_stream);
   if (s->step_graph) cudaGraphExecDestroy(s->step_graph);
   if (s->own_stream && s->stream) cudaStreamDestroy(s->stream);
 }
@@ -201,6 +204,9 @@ int hteno_create(const hteno_config* cfg, hteno_solver** out) {
   // HTENO_TMA=0 stages every tile of the mixed FV 2D kernel cell by cell (the same bits)
   const char* tma = std::getenv("HTENO_TMA");
   s->tma = !(tma && tma[0] == '0');
+  // HTENO_SIDE_STREAM=0 runs the plain FV 2D y-direction kernels after the x ones on one stream
+  const char* side = std::getenv("HTENO_SIDE_STREAM");
+  s->side = !(side && side[0] == '0');
 
   auto fail = [&](int code) {
     release(s);
@@ -251,6 +257,7 @@ int hteno_destroy(hteno_solver* s) {
 int hteno_set_stream(hteno_solver* s, void* stream) {
   if (!s) return HTENO_ERR_INVALID_ARG;
   cudaStreamSynchronize(s->stream);
+  if (s->side_stream) cudaStreamSynchronize(s->side_stream);
   if (s->own_stream) cudaStreamDestroy(s->stream);
   s->stream = static_cast<cudaStream_t>(stream);
   s->own_stream = false;
