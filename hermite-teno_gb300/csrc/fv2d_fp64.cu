@@ -789,12 +789,7 @@ int fv2d_fp64_setup(hteno_solver* s) {
     const cudaError_t e = cudaMalloc(&s->deep, size_t(s->cfg.nx) * s->cfg.ny);
     if (e != cudaSuccess) return cuda_error(s, e, "uniform-region flags");
   }
-  if (s->cfg.precision == HTENO_PREC_FP64 && s->side && !s->side_stream) {
-    cudaError_t e = cudaStreamCreateWithFlags(&s->side_stream, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->fork_ev, cudaEventDisableTiming);
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->join_ev, cudaEventDisableTiming);
-    if (e != cudaSuccess) return cuda_error(s, e, "side stream");
-  }
+  if (s->cfg.precision == HTENO_PREC_FP64 && make_side_stream(s) != HTENO_OK) return HTENO_ERR_CUDA;
   if (s->cfg.precision == HTENO_PREC_FP64 && s->cfg.bc >= HTENO_BC_TAYLOR && !s->ghost_faces) {
     const size_t n = size_t(32) * (s->cfg.nx + 1) + size_t(32) * (s->cfg.ny + 1);
     const cudaError_t e = cudaMalloc(&s->ghost_faces, n * sizeof(double));

@@ -20,6 +20,7 @@ int hermite2d_setup(hteno_solver* s) {
     return set_error(s, HTENO_ERR_CUDA, "constant upload failed");
   if (s->cfg.bc != HTENO_BC_ZEROGRAD)
     return set_error(s, HTENO_ERR_UNSUPPORTED, "the Hermite 2D scheme uses zero-gradient boundaries");
+  if (make_side_stream(s) != HTENO_OK) return HTENO_ERR_CUDA;
   const int nx = s->cfg.nx, ny = s->cfg.ny;
   s->work_bytes = s->cfg.precision == HTENO_PREC_MIXED ? work_bytes_h<float>(nx, ny)
                                                        : work_bytes_h<double>(nx, ny);

@@ -815,12 +815,19 @@ void launch_step(hteno_solver* s, const GeoH& G) {
     else
       kh_limit<T><<<unsigned(nbx + nby), kLimThreads, 0, cs>>>(G, K, s->q, s->v, s->w, nbx, s->dstate);
     trace_end(s);
+    // the y faces and fluxes beside the x ones on the side stream (one stream while timing)
+    const bool fork = s->side_stream && !s->timing;
+    cudaStream_t ys = fork ? s->side_stream : cs;
+    if (fork) {
+      cudaEventRecord(s->fork_ev, cs);
+      cudaStreamWaitEvent(ys, s->fork_ev, 0);
+    }
     trace_begin(s, k_fx);
     kh_faces<T, 1><<<unsigned((nxf + kHFaceThreads - 1) / kHFaceThreads), kHFaceThreads, 0, cs>>>(
         G, K, W.qt, W.vt, W.wt, W.primt, W.xc, W.xroe, s->dstate);
     trace_end(s);
     trace_begin(s, k_fy);
-    kh_faces<T, 2><<<unsigned((nyf + kHFaceThreads - 1) / kHFaceThreads), kHFaceThreads, 0, cs>>>(
+    kh_faces<T, 2><<<unsigned((nyf + kHFaceThreads - 1) / kHFaceThreads), kHFaceThreads, 0, ys>>>(
         G, K, W.qt, W.vt, W.wt, W.primt, W.yc, W.yroe, s->dstate);
     trace_end(s);
     trace_begin(s, k_x);
@@ -828,9 +835,13 @@ void launch_step(hteno_solver* s, const GeoH& G) {
         G, W.xc, W.xroe, W.fx, s->dstate);
     trace_end(s);
     trace_begin(s, k_y);
-    kh_flux<T, 2><<<unsigned((nyf + kHFluxThreads - 1) / kHFluxThreads), kHFluxThreads, 0, cs>>>(
+    kh_flux<T, 2><<<unsigned((nyf + kHFluxThreads - 1) / kHFluxThreads), kHFluxThreads, 0, ys>>>(
         G, W.yc, W.yroe, W.fy, s->dstate);
     trace_end(s);
+    if (fork) {
+      cudaEventRecord(s->join_ev, ys);
+      cudaStreamWaitEvent(cs, s->join_ev, 0);
+    }
     trace_begin(s, k_u);
     float *qtf = nullptr, *primtf = nullptr;
     if constexpr (std::is_same<T, float>::value) {

@@ -82,8 +82,9 @@ struct hteno_solver {
   bool uniform_skip = true;  // FV 2D: uniform regions take their exactly zero residual directly
   double* ghost_faces = nullptr;  // plain FV 2D with HTENO_BC_TAYLOR / _DOUBLE_MACH: ghost face rows
   double* fused64 = nullptr;  // plain FV 2D in fused stages: q1, q2 and their primitives [4][4][ncell]
-  // plain FV 2D: the y-direction face and flux kernels run on side_stream beside the x-direction
-  // ones (forked after the uniform test, joined before the update); side = false keeps one stream
+  // plain FV 2D and Hermite 2D: the y-direction face and flux kernels run on side_stream beside
+  // the x-direction ones (forked before the faces, joined before the update); side = false keeps
+  // one stream
   cudaStream_t side_stream = nullptr;
   cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
   bool side = true;
@@ -134,6 +135,7 @@ int fv2d_prepare(hteno_solver* s);  // after set_state: primitives of the new st
 int fv2d_step_async(hteno_solver* s, int nsteps);
 int fv2d_residual(hteno_solver* s, const double* q, double* rhs);
 int fv2d_fp64_set_fused(hteno_solver* s, int on);  // plain FV 2D: one launch per stage
+int make_side_stream(hteno_solver* s);  // side_stream and its fork/join events, unless side is off
 
 int fv1d_setup(hteno_solver* s);
 int fv1d_prepare(hteno_solver* s);

@@ -128,6 +128,14 @@ void release(hteno_solver* s) {
 }
 
 }  // namespace
+
+int make_side_stream(hteno_solver* s) {
+  if (!s->side || s->side_stream) return HTENO_OK;
+  cudaError_t e = cudaStreamCreateWithFlags(&s->side_stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->fork_ev, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->join_ev, cudaEventDisableTiming);
+  return e == cudaSuccess ? HTENO_OK : cuda_error(s, e, "side stream");
+}
 }  // namespace hteno
 
 using namespace hteno;
@@ -204,7 +212,7 @@ int hteno_create(const hteno_config* cfg, hteno_solver** out) {
   // HTENO_TMA=0 stages every tile of the mixed FV 2D kernel cell by cell (the same bits)
   const char* tma = std::getenv("HTENO_TMA");
   s->tma = !(tma && tma[0] == '0');
-  // HTENO_SIDE_STREAM=0 runs the plain FV 2D y-direction kernels after the x ones on one stream
+  // HTENO_SIDE_STREAM=0 runs the FV 2D / Hermite 2D y-direction kernels after the x ones on one stream
   const char* side = std::getenv("HTENO_SIDE_STREAM");
   s->side = !(side && side[0] == '0');
 

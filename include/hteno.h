@@ -102,8 +102,9 @@ void hteno_config_default(hteno_config* cfg);
  * creation: HTENO_UNIFORM_SKIP=0 computes uniform regions in full instead of taking their exactly
  * zero residual (the results are the same bits either way); HTENO_FV2D_TILE=<k> fixes the tile
  * candidate of the mixed FV 2D kernel instead of timing them (same bits for every candidate);
- * HTENO_SIDE_STREAM=0 runs the plain FV 2D y-direction kernels after the x-direction ones on the
- * solver's stream instead of beside them on a second stream of its own (the same bits). */
+ * HTENO_SIDE_STREAM=0 runs the y-direction face and flux kernels of plain FV 2D and Hermite 2D
+ * after the x-direction ones on the solver's stream instead of beside them on a second stream of
+ * its own (the same bits). */
 int hteno_create(const hteno_config* cfg, hteno_solver** out);
 int hteno_destroy(hteno_solver* s);
 
