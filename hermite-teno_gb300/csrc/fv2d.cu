@@ -29,7 +29,7 @@ int fv2d_setup(hteno_solver* s) {
     s->launches_per_step = 2 + 3;
   } else {
     s->work_bytes = work_bytes<double>(nx, ny);
-    s->launches_per_step = 2 + 3 * 5;
+    s->launches_per_step = 2 + 3 * (5 + (s->uniform_skip ? 1 : 0));  // + the uniform-region test
   }
   cudaError_t e = cudaMalloc(&s->work, s->work_bytes);
   if (e != cudaSuccess) return cuda_error(s, e, "work buffer");

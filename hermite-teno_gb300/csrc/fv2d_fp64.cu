@@ -802,7 +802,7 @@ int fv2d_fp64_set_fused(hteno_solver* s, int on) {
   if (!on) {
     cudaFree(s->fused64);
     s->fused64 = nullptr;
-    s->launches_per_step = 2 + 3 * 5;
+    s->launches_per_step = 2 + 3 * (5 + (s->uniform_skip ? 1 : 0));
     return HTENO_OK;
   }
   if (!s->fused64) {

@@ -29,7 +29,7 @@ int hermite2d_setup(hteno_solver* s) {
   e = cudaMemset(s->v, 0, s->ncell * 4 * sizeof(double));
   if (e == cudaSuccess) e = cudaMemset(s->w, 0, s->ncell * 4 * sizeof(double));
   if (e != cudaSuccess) return cuda_error(s, e, "moment buffers");
-  s->launches_per_step = 2 + 3 * 7;
+  s->launches_per_step = 2 + 3 * 6;  // limiter, faces x/y, fluxes x/y, update
   return HTENO_OK;
 }
 

@@ -416,7 +416,7 @@ def gpu_run2d_fused(h, q, nsteps, fused, t_final=1e30, **kw):
 ], ids=["teno5-hllc", "teno5i-periodic", "wenoz", "linear-periodic", "tiny-periodic"])
 def test_fp64_fused_stage_same_bits(hteno_lib, cuda, case):
     """One fused launch per stage gives the five-launch path's state bit for bit, with the same
-    time, step count and uniform-cell count, in three launches per step."""
+    time, step count and uniform-cell count, in five launches per step instead of twenty."""
     from hteno import ic
 
     (nx, ny), steps, kw = case
@@ -424,7 +424,7 @@ def test_fp64_fused_stage_same_bits(hteno_lib, cuda, case):
     a, ta, na, ua, la = gpu_run2d_fused(hteno_lib, q, steps, False, **kw)
     b, tb, nb, ub, lb = gpu_run2d_fused(hteno_lib, q, steps, True, **kw)
     np.testing.assert_array_equal(a, b)
-    assert (ta, na, ua) == (tb, nb, ub) and la == 17 and lb == 5
+    assert (ta, na, ua) == (tb, nb, ub) and la == 20 and lb == 5
 
 
 def test_fp64_fused_matches_oracle(hteno_lib, cuda, oracle):
@@ -459,3 +459,39 @@ def test_fp64_fused_rejects_other_configurations(hteno_lib, cuda):
             with pytest.raises(h.HtenoError) as e:
                 s.set_fp64_fused(True)
             assert e.value.code == 7  # HTENO_ERR_UNSUPPORTED
+
+
+def test_launches_per_step_counts_the_launches(hteno_lib, cuda):
+    """hteno_launches_per_step (the bench's gpu_launches per step) equals the kernels a step
+    launches: those the per-kernel timing records, plus the step's begin and end kernels."""
+    import ctypes
+
+    from hteno import ic
+
+    h = hteno_lib
+    lib = h.lib()
+    n = 64
+    q = ic.four_quadrant(n, n, 5)
+    f = ic.blobs_shock_fn(5)
+    x = (np.arange(n) + 0.5) / n
+    X, Y = np.meshgrid(x, x)
+    qh = np.ascontiguousarray(f(X, Y))
+    v, w = ic.face_difference_moments(f, n, n, 0.0, 1.0, 0.0, 1.0)
+    cases = [(dict(flux=1), q, None, False), (dict(flux=1), q, None, True),
+             (dict(flux=1, precision=1), q, None, False),
+             (dict(scheme=1, flux=0, precision=1), qh, (v, w), False),
+             (dict(scheme=1, flux=0), qh, (v, w), False)]
+    for kw, q0, mom, fused in cases:
+        with h.Solver(h.config(dims=2, nx=n, ny=n, **kw)) as s:
+            if fused:
+                s.set_fp64_fused(True)
+            s.set_state(q0)
+            if mom:
+                s.set_moments(*mom)
+            lib.hteno_enable_kernel_timing(s.h, 1)
+            s.step(3)
+            kt = (h.KernelTime * 16)()
+            cnt = ctypes.c_int()
+            lib.hteno_kernel_timing(s.h, kt, 16, ctypes.byref(cnt))
+            traced = sum(kt[k].launches for k in range(cnt.value))
+            assert traced % 3 == 0 and traced // 3 + 2 == s.launches_per_step(), (kw, fused, traced)
