@@ -879,12 +879,11 @@ void fv2d_fp64_stage(hteno_solver* s, const Geo& G, const Work<double>& W, int s
   // the y-direction kernels touch none of the x-direction kernels' outputs: while stepping they
   // run on the side stream beside them, so that each kernel's last, partly filled wave of
   // blocks overlaps the other direction's work (one stream while kernels are being timed)
-  const bool fork = stage > 0 && s->side_stream && !s->timing;
+  // (if the fork cannot be recorded, the y kernels stay on the solver's stream)
+  const bool fork = stage > 0 && s->side_stream && !s->timing &&
+                    cudaEventRecord(s->fork_ev, cs) == cudaSuccess &&
+                    cudaStreamWaitEvent(s->side_stream, s->fork_ev, 0) == cudaSuccess;
   cudaStream_t ys = fork ? s->side_stream : cs;
-  if (fork) {
-    cudaEventRecord(s->fork_ev, cs);
-    cudaStreamWaitEvent(ys, s->fork_ev, 0);
-  }
   trace_begin(s, kf_x);
   if (gx) {
     const long n = long(nx + 1) * (ny + 4);
@@ -913,10 +912,10 @@ void fv2d_fp64_stage(hteno_solver* s, const Geo& G, const Work<double>& W, int s
   kp_flux<2><<<unsigned((nyf + kFaceThreads - 1) / kFaceThreads), kFaceThreads, 0, ys>>>(
       G, W.yc, W.yroe, W.fy, st, deep, gy);
   trace_end(s);
-  if (fork) {
-    cudaEventRecord(s->join_ev, ys);
-    cudaStreamWaitEvent(cs, s->join_ev, 0);
-  }
+  // the join; if it cannot be recorded, wait for the side stream on the host instead
+  if (fork && (cudaEventRecord(s->join_ev, ys) != cudaSuccess ||
+               cudaStreamWaitEvent(cs, s->join_ev, 0) != cudaSuccess))
+    cudaStreamSynchronize(ys);
   const size_t nc = size_t(nx) * ny;
   trace_begin(s, ku);
   kp_update<<<unsigned((nc + 255) / 256), 256, 0, cs>>>(G, stage, W.fx, W.fy, s->q, s->q0,

@@ -816,12 +816,11 @@ void launch_step(hteno_solver* s, const GeoH& G) {
       kh_limit<T><<<unsigned(nbx + nby), kLimThreads, 0, cs>>>(G, K, s->q, s->v, s->w, nbx, s->dstate);
     trace_end(s);
     // the y faces and fluxes beside the x ones on the side stream (one stream while timing)
-    const bool fork = s->side_stream && !s->timing;
+    // (if the fork cannot be recorded, the y kernels stay on the solver's stream)
+    const bool fork = s->side_stream && !s->timing &&
+                      cudaEventRecord(s->fork_ev, cs) == cudaSuccess &&
+                      cudaStreamWaitEvent(s->side_stream, s->fork_ev, 0) == cudaSuccess;
     cudaStream_t ys = fork ? s->side_stream : cs;
-    if (fork) {
-      cudaEventRecord(s->fork_ev, cs);
-      cudaStreamWaitEvent(ys, s->fork_ev, 0);
-    }
     trace_begin(s, k_fx);
     kh_faces<T, 1><<<unsigned((nxf + kHFaceThreads - 1) / kHFaceThreads), kHFaceThreads, 0, cs>>>(
         G, K, W.qt, W.vt, W.wt, W.primt, W.xc, W.xroe, s->dstate);
@@ -838,10 +837,10 @@ void launch_step(hteno_solver* s, const GeoH& G) {
     kh_flux<T, 2><<<unsigned((nyf + kHFluxThreads - 1) / kHFluxThreads), kHFluxThreads, 0, ys>>>(
         G, W.yc, W.yroe, W.fy, s->dstate);
     trace_end(s);
-    if (fork) {
-      cudaEventRecord(s->join_ev, ys);
-      cudaStreamWaitEvent(cs, s->join_ev, 0);
-    }
+    // the join; if it cannot be recorded, wait for the side stream on the host instead
+    if (fork && (cudaEventRecord(s->join_ev, ys) != cudaSuccess ||
+                 cudaStreamWaitEvent(cs, s->join_ev, 0) != cudaSuccess))
+      cudaStreamSynchronize(ys);
     trace_begin(s, k_u);
     float *qtf = nullptr, *primtf = nullptr;
     if constexpr (std::is_same<T, float>::value) {
