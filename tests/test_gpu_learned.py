@@ -251,9 +251,9 @@ def trained(hteno_lib, cuda):
 def test_trained_router_accuracy(hteno_lib, cuda, trained):
     """Route a mixed 256^2 four-quadrant run: the density error against FP64 stays within the
     mixed path's bound and no shock moves by more than one cell (routing at every step costs
-    some accuracy on this small grid: its L1 error is within 5x of the plain mixed run's).  The network routes non-flat stencils; the FP64 judge's
-    counts are consistent (its share of misrouted stencils on this data, about a fifth of the
-    float-resolved ones, is what DESIGN reports; the misroutes sit on weak features, as the
+    some accuracy on this small grid: its L1 error is within 5x of the plain mixed run's).  The
+    network routes non-flat stencils; the FP64 judge's counts are consistent (on this data it
+    finds about a fifth of the float-resolved routes misrouted; those sit on weak features, as the
     density bound shows)."""
     from hteno import ic, metrics
 
