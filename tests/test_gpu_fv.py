@@ -495,3 +495,35 @@ def test_launches_per_step_counts_the_launches(hteno_lib, cuda):
             lib.hteno_kernel_timing(s.h, kt, 16, ctypes.byref(cnt))
             traced = sum(kt[k].launches for k in range(cnt.value))
             assert traced % 3 == 0 and traced // 3 + 2 == s.launches_per_step(), (kw, fused, traced)
+
+
+def test_fp64_fused_uniform_skip_and_user_stream(hteno_lib, cuda):
+    """The fused stage computes uniform regions in full with HTENO_UNIFORM_SKIP=0 and gives the same
+    bits; on a caller's stream it gives the same bits as on its own."""
+    import os
+
+    from hteno import ic
+
+    h = hteno_lib
+    q = ic.four_quadrant(160, 96, 21)
+    cfg = h.config(dims=2, nx=160, ny=96, flux=1)
+
+    def run(stream=None):
+        with h.Solver(cfg) as s:
+            if stream is not None:
+                s.set_stream(stream.cuda_stream)
+            s.set_fp64_fused(True)
+            s.set_state(q)
+            s.step(30)
+            return s.get_state(), s.counters()["uniform_cells"]
+
+    base, uni = run()
+    os.environ["HTENO_UNIFORM_SKIP"] = "0"
+    try:
+        full, uni0 = run()
+    finally:
+        os.environ.pop("HTENO_UNIFORM_SKIP", None)
+    np.testing.assert_array_equal(base, full)
+    assert uni > 0 and uni0 == 0
+    own, _ = run(cuda.cuda.Stream())
+    np.testing.assert_array_equal(base, own)
