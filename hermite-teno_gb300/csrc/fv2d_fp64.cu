@@ -20,11 +20,17 @@ std::mutex g_mu;
 #include "common_kernels.cuh"
 
 // primitives: calcPrimitiveVariable (FV_System2D.cpp:226-263)
+// The three divisions by rho share one correctly rounded reciprocal (par::quot: the same bits as
+// the divisions, Markstein).
 __device__ __forceinline__ void cell_prim(double g1, const double* q, double* w, double& h,
                                           double& sr) {
-  par::primitive(g1, q, w);
+  const par::Den d = par::den_of(q[0]);
+  w[0] = q[0];
+  w[1] = par::quot(q[1], d);
+  w[2] = par::quot(q[2], d);
+  w[3] = (q[3] - 0.5 * (q[1] * w[1] + q[2] * w[2])) * g1;  // par::primitive's pressure
   sr = sqrt(fabs(w[0]));
-  h = (q[3] + w[3]) / w[0];
+  h = par::quot(q[3] + w[3], d);
 }
 
 __global__ void kp_prim(Geo G, const double* __restrict__ q, double* __restrict__ prim,
@@ -473,10 +479,12 @@ __global__ void kp_update(Geo G, int stage, const double* __restrict__ fx,
     const size_t ox = size_t(j) * (G.nx + 1) + i, oy = size_t(j) * G.nx + i;
     double rhs[4] = {0.0, 0.0, 0.0, 0.0};  // a deep cell's flux pairs are equal: residual +0
     if (!(deep && deep[k])) {
+      const par::Den da = par::den_of(G.area);  // the four divisions by the cell area
 #pragma unroll
       for (int v = 0; v < 4; ++v)
-        rhs[v] = ((fx[v * nxf + ox] - fx[v * nxf + ox + 1]) * G.dy +
-                  (fy[v * nyf + oy] - fy[v * nyf + oy + G.nx]) * G.dx) / G.area + 0.0;
+        rhs[v] = par::quot((fx[v * nxf + ox] - fx[v * nxf + ox + 1]) * G.dy +
+                               (fy[v * nyf + oy] - fy[v * nyf + oy + G.nx]) * G.dx,
+                           da) + 0.0;
     }
     if (stage == 0) {
 #pragma unroll
@@ -754,9 +762,11 @@ __global__ void __launch_bounds__(NT, 2) kp_stage64(Geo G, int stage, const doub
     const size_t k = size_t(j0 + t) * G.nx + (i0 + i);
     double rhs[4] = {0.0, 0.0, 0.0, 0.0};  // a uniform cell's flux pairs are equal: residual +0
     if (!S.deep[t][i]) {
+      const par::Den da = par::den_of(G.area);
 #pragma unroll
       for (int v = 0; v < 4; ++v)
-        rhs[v] = (S.rx[v][t][i] + (S.f[v][t * TX + i] - S.f[v][(t + 1) * TX + i]) * G.dx) / G.area + 0.0;
+        rhs[v] = par::quot(S.rx[v][t][i] + (S.f[v][t * TX + i] - S.f[v][(t + 1) * TX + i]) * G.dx,
+                           da) + 0.0;
     }
     double qn[4];
 #pragma unroll
