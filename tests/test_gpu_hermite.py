@@ -132,3 +132,43 @@ def test_hermite1d_matches_oracle_bitwise(hteno_lib, cuda, oracle):
     assert ng == no == 40 and tg == to
     np.testing.assert_array_equal(qg, qo)
     np.testing.assert_array_equal(vg, vo)
+
+
+def test_side_stream_same_bits(hteno_lib, cuda):
+    """The y-direction kernels beside the x-direction ones on a second stream (the default) give
+    the bits of the one-stream order (HTENO_SIDE_STREAM=0): FV 2D FP64, Hermite 2D FP64 and mixed."""
+    import os
+
+    from hteno import ic
+
+    h = hteno_lib
+    n = 96
+    f = ic.blobs_shock_fn(5)
+    x = (np.arange(n) + 0.5) / n
+    X, Y = np.meshgrid(x, x)
+    qh = np.ascontiguousarray(f(X, Y))
+    v, w = ic.face_difference_moments(f, n, n, 0.0, 1.0, 0.0, 1.0)
+    qf = ic.four_quadrant(n, n, 13)
+
+    def run(kw, q, mom):
+        with h.Solver(h.config(dims=2, nx=n, ny=n, **kw)) as s:
+            s.set_state(q)
+            if mom:
+                s.set_moments(*mom)
+            s.step(6)
+            out = [s.get_state()]
+            if mom:
+                out += list(s.get_moments())
+            return out
+
+    cases = [(dict(flux=1), qf, None), (dict(scheme=1, flux=0), qh, (v, w)),
+             (dict(scheme=1, flux=0, precision=1), qh, (v, w))]
+    for kw, q, mom in cases:
+        two = run(kw, q, mom)
+        os.environ["HTENO_SIDE_STREAM"] = "0"
+        try:
+            one = run(kw, q, mom)
+        finally:
+            os.environ.pop("HTENO_SIDE_STREAM", None)
+        for a, b in zip(two, one):
+            np.testing.assert_array_equal(a, b)
