@@ -121,46 +121,95 @@ __device__ __forceinline__ double decision_rcp(double x) {
   return fma(y, fma(-x, y, 1.0), y);
 }
 
-// The fast part of a cut-off decision, in float: x_k = r_k / r_max (in (0, 1], or NaN) converted
-// on the integer pipes, a_k = x_k^6, kept where a_k >= ct * (a_0 + a_1 + a_2).  The float path's
-// relative error is below 1e-6 (x_k to 2^-24, six roundings in a_k, two in the sum), so any a_k
-// farther than 1e-5 of the limit from it is decided as exact arithmetic decides it; nearer ones
-// set *near and the caller takes the reference's own arithmetic.  NaN ratios compare false, as
-// in double.  (The FP64 pipe runs at 1/64 of the float rate on GB300; this part was 24 of the
-// decision's 43 FP64 operations.)
-__device__ __forceinline__ int cutoff_fast(const double* x, double ct, bool* near) {
+// The fast part of a cut-off decision, in float, from the ratios x_k = r_k / r_max (in (0, 1],
+// or NaN): a_k = x_k^6, kept where a_k >= ct * (a_0 + a_1 + a_2).  Any a_k farther than `band` of
+// the limit from it is decided as exact arithmetic decides it (the callers' error bounds are a
+// fraction of the band); nearer ones set *near and the caller takes the reference's own
+// arithmetic.  NaN ratios compare false, as in double.  (The FP64 pipe runs at 1/64 of the float
+// rate on GB300.)
+__device__ __forceinline__ int cutoff_core(const float* x, float ct, float band, bool* near) {
   float a[3];
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
-    const float xf = mix::d2f(x[k]);
-    const float x2 = xf * xf;
+    const float x2 = x[k] * x[k];
     a[k] = (x2 * x2) * x2;
   }
-  const float lim = float(ct) * ((a[0] + a[1]) + a[2]);
+  const float lim = ct * ((a[0] + a[1]) + a[2]);
   int pat = 0;
   bool nr = false;
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
     pat |= (a[k] < lim ? 0 : 1) << k;
-    nr |= fabsf(a[k] - lim) <= 1e-5f * lim;
+    nr |= fabsf(a[k] - lim) <= band * lim;
   }
   *near = nr;
   return pat;
 }
+// ... from double ratios (converted on the integer pipes): the float chain's relative error is
+// below 1e-6 (x_k to 2^-24, six roundings in a_k, two in the sum), well inside a band of 1e-5.
+__device__ __forceinline__ int cutoff_fast(const double* x, double ct, bool* near) {
+  const float xf[3] = {mix::d2f(x[0]), mix::d2f(x[1]), mix::d2f(x[2])};
+  return cutoff_core(xf, float(ct), 1e-5f, near);
+}
 
-// Cut-off pattern of the reference's cutOff() (:1141-1149) given SI and tau.  Fast path (ratios
-// in double, the rest in float, cutoff_fast) with a guard band of 1e-5 relative; inside the band
-// the reference's arithmetic decides.
+// The ratios x_k = r_k / r_max of r_k = 1 + tau / d_k in float, without reciprocals or r_k's
+// range: with d_min = min d_k, x_k = (d_min / d_k) (d_k + tau) / (d_min + tau).  The four doubles
+// are first scaled by one power of two (exponent bits, on the integer pipes) so that the largest
+// lies in [1, 2).  Relative error of x_k below 2^-19.7 (four inputs rounded to float, two
+// __fdividef quotients of 2 ulp and three roundings), so of a_k below 7.4e-6.  False when a value
+// is NaN, infinite, subnormal or more than 2^125 below the largest (the caller takes the double
+// path).  d_k > 0 and tau >= 0 here.
+__device__ __forceinline__ bool scaled_ratios(const double* d, double tau, float* x) {
+  const double v[4] = {d[0], d[1], d[2], tau};
+  int hi[4];
+  unsigned lo[4], e[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    hi[i] = __double2hiint(v[i]);
+    lo[i] = unsigned(__double2loint(v[i]));
+    e[i] = (unsigned(hi[i]) >> 20) & 0x7ffu;
+  }
+  const unsigned em = max(max(e[0], e[1]), max(e[2], e[3]));
+  if (em == 0x7ffu) return false;
+  float f[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    if (i == 3 && ((unsigned(hi[3]) << 1) | lo[3]) == 0u) {
+      f[3] = 0.0f;  // tau = 0: every r_k is 1
+    } else {
+      if (e[i] == 0u || e[i] + 125u < em) return false;
+      // scaled exponent e - em + 1023 in [898, 1023]: a normal float in [2^-125, 2)
+      f[i] = mix::d2f(__hiloint2double(hi[i] - (int(em) - 1023) * (1 << 20), int(lo[i])));
+    }
+  }
+  const float dmin = fminf(fminf(f[0], f[1]), f[2]);
+#pragma unroll
+  for (int k = 0; k < 3; ++k)
+    x[k] = __fdividef(dmin, f[k]) * __fdividef(f[k] + f[3], dmin + f[3]);
+  return true;
+}
+
+// Cut-off pattern of the reference's cutOff() (:1141-1149) given SI and tau.  Fast path: the
+// ratios in float from d_k = SI_k + epsz and tau (scaled_ratios, guard band 2^-13 relative, eight
+// times its error bound), or in double where the scaling cannot reach (guard band 1e-5); inside
+// the band the reference's arithmetic decides.
 __device__ __forceinline__ int cutoff_pattern(const double* SI, double tau, double epsz, double ct) {
-  double r[3], x[3];
-#pragma unroll
-  for (int k = 0; k < 3; ++k) r[k] = 1.0 + tau * decision_rcp(SI[k] + epsz);
-  const double rm = fmax(fmax(r[0], r[1]), r[2]);
-  const double inv = decision_rcp(rm);
-#pragma unroll
-  for (int k = 0; k < 3; ++k) x[k] = r[k] * inv;
+  const double d[3] = {SI[0] + epsz, SI[1] + epsz, SI[2] + epsz};
+  float xf[3];
   bool near;
-  int pat = cutoff_fast(x, ct, &near);
+  int pat;
+  if (scaled_ratios(d, tau, xf)) {
+    pat = cutoff_core(xf, float(ct), 0x1p-13f, &near);
+  } else {
+    double r[3], x[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) r[k] = 1.0 + tau * decision_rcp(d[k]);
+    const double rm = fmax(fmax(r[0], r[1]), r[2]);
+    const double inv = decision_rcp(rm);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) x[k] = r[k] * inv;
+    pat = cutoff_fast(x, ct, &near);
+  }
   if (near) {  // reference arithmetic: w_k = pow(1 + tau/(SI_k + epsz), 6) / sum
     double w[3];
 #pragma unroll
