@@ -121,6 +121,10 @@ __device__ __forceinline__ double decision_rcp(double x) {
   return fma(y, fma(-x, y, 1.0), y);
 }
 
+// Largest r whose sixth power is finite with margin (pow(2e51, 6) = 6.4e306): beyond it the
+// reference's weights overflow to inf and its normalised weights are NaN.
+constexpr double kPow6Max = 2e51;
+
 // The fast part of a cut-off decision, in float, from the ratios x_k = r_k / r_max (in (0, 1],
 // or NaN): a_k = x_k^6, kept where a_k >= ct * (a_0 + a_1 + a_2).  Any a_k farther than `band` of
 // the limit from it is decided as exact arithmetic decides it (the callers' error bounds are a
@@ -158,7 +162,8 @@ __device__ __forceinline__ int cutoff_fast(const double* x, double ct, bool* nea
 // lies in [1, 2).  Relative error of x_k below 2^-19.7 (four inputs rounded to float, two
 // __fdividef quotients of 2 ulp and three roundings), so of a_k below 7.4e-6.  False when a value
 // is NaN, infinite, subnormal or more than 2^125 below the largest (the caller takes the double
-// path).  d_k > 0 and tau >= 0 here.
+// path).  d_k > 0 and tau >= 0 here; within 2^125 every r_k <= 1 + 2^126 < kPow6Max, so the
+// reference's weights are finite.
 __device__ __forceinline__ bool scaled_ratios(const double* d, double tau, float* x) {
   const double v[4] = {d[0], d[1], d[2], tau};
   int hi[4];
@@ -209,6 +214,9 @@ __device__ __forceinline__ int cutoff_pattern(const double* SI, double tau, doub
 #pragma unroll
     for (int k = 0; k < 3; ++k) x[k] = r[k] * inv;
     pat = cutoff_fast(x, ct, &near);
+    // where pow(r, 6) overflows the reference's weights are inf / inf = NaN (a kept candidate):
+    // its own arithmetic decides
+    near = near || !(rm < kPow6Max);
   }
   if (near) {  // reference arithmetic: w_k = pow(1 + tau/(SI_k + epsz), 6) / sum
     double w[3];
@@ -270,7 +278,7 @@ __device__ __forceinline__ int cutoff_from_r(const double* r, double ct) {
   for (int k = 0; k < 3; ++k) x[k] = r[k] * inv;
   bool near;
   int pat = cutoff_fast(x, ct, &near);
-  if (near || !(rm < 1e300)) {  // the reference's arithmetic (also for overflowing ratios)
+  if (near || !(rm < kPow6Max)) {  // the reference's arithmetic (also where pow(r, 6) overflows)
     double w[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) w[k] = pow(r[k], 6.0);
