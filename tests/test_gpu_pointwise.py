@@ -211,3 +211,27 @@ def test_alternative_reconstructions(hteno_lib, cuda, oracle):
         u = np.ascontiguousarray(np.sin(0.2 + 0.03 * x)[None, :] * np.linspace(0.5, 2, 256)[:, None])
         np.testing.assert_allclose(run_lagrange(hteno_lib, cuda, kind, u, prec=1), oracle.lagrange(kind, u),
                                    rtol=5e-6, atol=5e-6)
+
+
+def test_lagrange_cutoff_edge_cases_vs_oracle(hteno_lib, cuda, oracle):
+    """TENO cut-off decisions at the ends of the fast paths' ranges, bit for bit against the
+    oracle: constant sub-stencils next to huge jumps (indicator 0, so r = 1 + tau / epsz beyond the
+    float scaling's 2^125 and, from |jump| ~ 1e6 on, weights whose pow(r, 6) overflows to inf in
+    the reference), tiny and huge magnitudes, and equal indicators."""
+    rng = np.random.default_rng(17)
+    n = 6000
+    rows = []
+    for mag in (1e-30, 1e-8, 1.0, 1e3, 1e6, 1e12, 1e20):
+        base = rng.uniform(0.5, 2.0, (n, 6))
+        const = base.copy()
+        const[:, :3] = base[:, :1]  # three equal cells: one indicator exactly 0
+        const[:, 3:] *= mag
+        rows += [const, const[:, ::-1].copy(), base * mag]
+    u = np.ascontiguousarray(np.vstack(rows))
+    scale = np.abs(u).max(axis=1, keepdims=True)
+    for kind in (0, 1):
+        got = run_lagrange(hteno_lib, cuda, kind, u)
+        want = oracle.lagrange(kind, u)
+        assert np.array_equal(np.isnan(got), np.isnan(want))
+        ok = ~np.isnan(want)
+        np.testing.assert_array_equal(got[ok], want[ok])
