@@ -10,11 +10,12 @@
 // multiply-add is fused.  Divisions and square roots are IEEE correctly rounded, as on the CPU.
 //
 // The one deliberate difference: the TENO cut-off weights (1 + tau/(SI+eps))^6 / sum only select
-// one of 8 cut-off patterns, so they are evaluated with reciprocals, the ratios to the largest
-// and a float multiply chain; when a weight lies within a relative 1e-5 of the threshold (ten
-// times the float chain's error bound), the decision is recomputed with the reference's
-// divisions and pow.  The reconstructed values use the pattern's weights from a table
-// built with the reference's own normalisation, so they are bit-identical.
+// one of 8 cut-off patterns, so they are compared in float (the ratios of the weights' bases to
+// the largest, from SI + eps and tau scaled into float range, and their sixth powers); when a
+// weight lies within a guard band of the threshold (several times the float evaluation's error
+// bound), the decision is recomputed with the reference's divisions and pow.  The indicators and
+// tau themselves are the reference's bits.  The reconstructed values use the pattern's weights
+// from a table built with the reference's own normalisation, so they are bit-identical.
 #pragma once
 
 #include "device_math.cuh"
