@@ -176,7 +176,9 @@ __device__ __forceinline__ bool scaled_ratios(const double* d, double tau, float
     e[i] = (unsigned(hi[i]) >> 20) & 0x7ffu;
   }
   const unsigned em = max(max(e[0], e[1]), max(e[2], e[3]));
-  if (em == 0x7ffu) return false;
+  // (the callers' indicators are sums of squares and tau an absolute value or a maximum of them;
+  // a sign bit, even of -0, sends the decision to the double path all the same)
+  if (em == 0x7ffu || (hi[0] | hi[1] | hi[2] | hi[3]) < 0) return false;
   float f[4];
 #pragma unroll
   for (int i = 0; i < 4; ++i) {
