@@ -44,14 +44,22 @@ def harvest_runs(h, torch, seeds, n=1024, snapshots=(0, 20, 40), keep=0.2, capac
             got = s.harvest(1.0, 77 + snap, x[off:], y[off:])
             off = min(capacity, off + got)
     x, y = x[:off].contiguous(), y[:off].contiguous()
-    order = torch.sort(y.to(torch.int64), stable=True).indices  # least significant key first
-    keys = x.view(torch.int64)  # the 8 BF16 values of a row as two 64-bit keys
-    for k in (1, 0):
-        order = order[torch.sort(keys[order, k], stable=True).indices]
+    order = canonical_order(torch, x, y)
     gen = torch.Generator(device=device)
     gen.manual_seed(shuffle_seed)
     perm = order[torch.randperm(off, generator=gen, device=device)]
     return x[perm].contiguous(), y[perm].contiguous()
+
+
+def canonical_order(torch, x, y):
+    """Indices that sort rows (x int16 [N, 8], y uint8 [N]) by their bits: x's two 64-bit halves,
+    then y (stable sorts from the least significant key), so that the same multiset of rows gives
+    the same order however the harvest kernels appended them."""
+    order = torch.sort(y.to(torch.int64), stable=True).indices
+    keys = x.view(torch.int64)  # the 8 BF16 values of a row as two 64-bit keys
+    for k in (1, 0):
+        order = order[torch.sort(keys[order, k], stable=True).indices]
+    return order
 
 
 def label_stats(y):

@@ -31,3 +31,20 @@ def test_shock_shift_beyond_the_first_window():
         b = np.zeros((8, 64))
         b[:, 20 + d:] = 1.0
         assert metrics.shock_shift(b, a) == d, d
+
+
+def test_canonical_row_order_is_independent_of_arrival_order():
+    """learned.canonical_order: the same multiset of harvested rows, appended in any order, comes
+    out in one order (what makes the harvest-to-network workflow repeat bit for bit)."""
+    import torch
+
+    from hteno import learned
+
+    g = torch.Generator().manual_seed(3)
+    x = torch.randint(-3, 3, (5000, 8), dtype=torch.int16, generator=g)
+    y = torch.randint(0, 8, (5000,), dtype=torch.uint8, generator=g)
+    o = learned.canonical_order(torch, x, y)
+    perm = torch.randperm(5000, generator=g)
+    xp, yp = x[perm].contiguous(), y[perm].contiguous()
+    op = learned.canonical_order(torch, xp, yp)
+    assert torch.equal(x[o], xp[op]) and torch.equal(y[o], yp[op])
