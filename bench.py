@@ -306,7 +306,7 @@ def fused_fp64_path(hteno, torch, cfg, stream, start_state, ref_state, steps, va
             "hbm_bytes_per_cell_update": {"fused": 3 * 193.0, "five_launch": five},
             "note": "one launch per stage reads the state once (3-cell halo) and writes it once; the "
                     "tile's halo face rows and columns and its edge fluxes are computed again by the "
-                    "neighbouring tiles (+12.6 % FP64 instructions, measured), and the FP64-bound "
+                    "neighbouring tiles (+12 % FP64 instructions, measured), and the FP64-bound "
                     "stage pays for that: the five-launch path stays the default"}
 
 
